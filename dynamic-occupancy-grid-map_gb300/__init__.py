@@ -1,0 +1,372 @@
+"""GB300-native dynamic occupancy grid map (DOGM) update — Python binding of the C ABI.
+
+The product is libdogm_gb300.so (CUDA kernels for sm_103a + the C ABI of
+include/dogm_gb300.h).  This module binds it with ctypes and mirrors the reference's
+dogm::DOGM class (dogm/include/dogm/dogm.h:20-199) for Python callers, tests and the
+bench.  There is no CPU fallback: if the library was not built, loading raises.
+
+The directory name contains hyphens, so import it with
+    importlib.import_module("dynamic-occupancy-grid-map_gb300")
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "lib", "libdogm_gb300.so")
+
+# dogm_grid_cell (dogm_types.h:13-33) and dogm_measurement_cell (dogm_types.h:35-41)
+GRID_CELL_DTYPE = np.dtype([
+    ("start_idx", "<i4"), ("end_idx", "<i4"), ("new_born_occ_mass", "<f4"), ("pers_occ_mass", "<f4"),
+    ("free_mass", "<f4"), ("occ_mass", "<f4"), ("pred_occ_mass", "<f4"), ("mu_A", "<f4"), ("mu_UA", "<f4"),
+    ("w_A", "<f4"), ("w_UA", "<f4"), ("mean_x_vel", "<f4"), ("mean_y_vel", "<f4"), ("var_x_vel", "<f4"),
+    ("var_y_vel", "<f4"), ("covar_xy_vel", "<f4")])
+MEAS_DTYPE = np.dtype([("free_mass", "<f4"), ("occ_mass", "<f4"), ("likelihood", "<f4"), ("p_A", "<f4")])
+GRID_CELL_FIELDS = GRID_CELL_DTYPE.names
+
+DOGM_OK = 0
+STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "device wait timed out",
+                5: "not ready", 6: "unsupported", 7: "over budget"}
+
+# C ABI symbols declared in include/dogm_gb300.h (checked by the CPU test suite).
+ABI_SYMBOLS = [
+    "dogm_default_options", "dogm_create", "dogm_destroy", "dogm_update", "dogm_update_batch", "dogm_synchronize",
+    "dogm_get_grid_cells", "dogm_get_grid_cells_device", "dogm_get_measurement_cells", "dogm_get_particles",
+    "dogm_get_grid_size", "dogm_get_resolution", "dogm_get_position_x", "dogm_get_position_y", "dogm_get_yaw",
+    "dogm_get_iteration", "dogm_get_particle_count", "dogm_get_new_born_particle_count", "dogm_particle_prediction",
+    "dogm_update_pose", "dogm_initialize_particles", "dogm_set_measurement_cells", "dogm_set_particles",
+    "dogm_set_replay", "dogm_clear_replay", "dogm_generate_draws", "dogm_debug_enable", "dogm_debug_export",
+    "dogm_lower_bound_f32", "dogm_host_alloc", "dogm_host_free", "dogm_device_alloc", "dogm_device_free",
+    "dogm_memcpy", "dogm_state_bytes", "dogm_last_launch_count", "dogm_last_error", "dogm_status_string",
+    "dogm_abi_version",
+]
+
+
+class Params(C.Structure):
+    """dogm::DOGM::Params (dogm.h:26-60), field order = ABI."""
+    _fields_ = [("size", C.c_float), ("resolution", C.c_float), ("particle_count", C.c_int),
+                ("new_born_particle_count", C.c_int), ("persistence_prob", C.c_float),
+                ("stddev_process_noise_position", C.c_float), ("stddev_process_noise_velocity", C.c_float),
+                ("birth_prob", C.c_float), ("stddev_velocity", C.c_float), ("init_max_velocity", C.c_float),
+                ("freespace_discount", C.c_float)]
+
+
+class Options(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("stream_id", C.c_uint32), ("resample_mode", C.c_int),
+                ("sync_each_update", C.c_int)]
+
+
+class DogmError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(path: str | None = None) -> C.CDLL:
+    """Load libdogm_gb300.so (build it with __graft_entry__.build()); raises if missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise DogmError("libdogm_gb300.so is not built (%s): run __graft_entry__.build(); "
+                        "there is no CPU fallback" % p)
+    lib = C.CDLL(p)
+    vp, f, i, u64, sz = C.c_void_p, C.c_float, C.c_int, C.c_uint64, C.c_size_t
+    sig = {
+        "dogm_default_options": ([vp], i), "dogm_create": ([vp, vp, vp], i), "dogm_destroy": ([vp], i),
+        "dogm_update": ([vp, vp, f, f, f, f, i], i),
+        "dogm_update_batch": ([vp, i, vp, vp, vp, vp, vp, i], i), "dogm_synchronize": ([vp], i),
+        "dogm_get_grid_cells": ([vp, vp, sz], i), "dogm_get_grid_cells_device": ([vp, vp, sz], i),
+        "dogm_get_measurement_cells": ([vp, vp, sz], i), "dogm_get_particles": ([vp, vp, vp, vp, vp, sz], i),
+        "dogm_get_grid_size": ([vp], i), "dogm_get_resolution": ([vp], f), "dogm_get_position_x": ([vp], f),
+        "dogm_get_position_y": ([vp], f), "dogm_get_yaw": ([vp], f), "dogm_get_iteration": ([vp], i),
+        "dogm_get_particle_count": ([vp], i), "dogm_get_new_born_particle_count": ([vp], i),
+        "dogm_particle_prediction": ([vp, f], i), "dogm_update_pose": ([vp, f, f, f], i),
+        "dogm_initialize_particles": ([vp], i), "dogm_set_measurement_cells": ([vp, vp, sz], i),
+        "dogm_set_particles": ([vp, vp, vp, vp, f, sz], i), "dogm_set_replay": ([vp, vp, vp, vp, vp], i),
+        "dogm_clear_replay": ([vp], i), "dogm_generate_draws": ([vp, i, vp, vp, vp, vp], i),
+        "dogm_debug_enable": ([vp, i], i),
+        "dogm_debug_export": ([vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
+        "dogm_lower_bound_f32": ([vp, i, vp, i, vp, i, vp], i), "dogm_host_alloc": ([vp, sz], i),
+        "dogm_host_free": ([vp], i), "dogm_device_alloc": ([vp, sz], i), "dogm_device_free": ([vp], i),
+        "dogm_memcpy": ([vp, vp, sz, i], i), "dogm_state_bytes": ([vp], sz), "dogm_last_launch_count": ([vp], i),
+        "dogm_last_error": ([], C.c_char_p), "dogm_status_string": ([i], C.c_char_p), "dogm_abi_version": ([], i),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def check(status: int, what: str = "dogm") -> None:
+    if status != DOGM_OK:
+        msg = load().dogm_last_error().decode(errors="replace")
+        raise DogmError("%s: %s (%s)" % (what, STATUS_NAMES.get(status, status), msg))
+
+
+def _ptr(a) -> C.c_void_p | None:
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return C.c_void_p(a)
+    return C.c_void_p(a.ctypes.data)
+
+
+def make_params(**kw) -> Params:
+    p = Params()
+    defaults = dict(size=50.0, resolution=0.2, particle_count=300000, new_born_particle_count=30000,
+                    persistence_prob=0.99, stddev_process_noise_position=0.1, stddev_process_noise_velocity=2.0,
+                    birth_prob=0.02, stddev_velocity=30.0, init_max_velocity=12.0, freespace_discount=0.01)
+    defaults.update(kw)
+    for k, v in defaults.items():
+        setattr(p, k, v)
+    return p
+
+
+class DeviceBuffer:
+    """Raw device allocation (cudaMalloc through the C ABI)."""
+
+    def __init__(self, nbytes: int):
+        self.nbytes = int(nbytes)
+        p = C.c_void_p()
+        check(load().dogm_device_alloc(C.byref(p), self.nbytes), "dogm_device_alloc")
+        self.ptr = p.value
+
+    def upload(self, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr)
+        assert a.nbytes <= self.nbytes
+        check(load().dogm_memcpy(C.c_void_p(self.ptr), _ptr(a), a.nbytes, 1), "dogm_memcpy H2D")
+
+    def download(self, arr: np.ndarray) -> np.ndarray:
+        check(load().dogm_memcpy(_ptr(arr), C.c_void_p(self.ptr), arr.nbytes, 2), "dogm_memcpy D2H")
+        return arr
+
+    def free(self) -> None:
+        if self.ptr:
+            load().dogm_device_free(C.c_void_p(self.ptr))
+            self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class PinnedArray:
+    """A numpy array over pinned host memory (cudaMallocHost through the C ABI)."""
+
+    def __init__(self, shape, dtype):
+        self.dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * self.dtype.itemsize
+        p = C.c_void_p()
+        check(load().dogm_host_alloc(C.byref(p), max(n, 1)), "dogm_host_alloc")
+        self.ptr = p.value
+        buf = (C.c_char * max(n, 1)).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=self.dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self) -> None:
+        if self.ptr:
+            self.array = None
+            load().dogm_host_free(C.c_void_p(self.ptr))
+            self.ptr = 0
+
+
+class DOGM:
+    """Python mirror of dogm::DOGM over the C ABI (dogm/include/dogm/dogm.h:20-199)."""
+
+    def __init__(self, params: Params, seed: int = 123456, stream_id: int = 0, sync_each_update: bool = True):
+        lib = load()
+        self.params = params
+        opt = Options()
+        check(lib.dogm_default_options(C.byref(opt)), "dogm_default_options")
+        opt.seed = seed
+        opt.stream_id = stream_id
+        opt.sync_each_update = 1 if sync_each_update else 0
+        h = C.c_void_p()
+        check(lib.dogm_create(C.byref(params), C.byref(opt), C.byref(h)), "dogm_create")
+        self.h = h
+        self.grid_size = lib.dogm_get_grid_size(h)
+        self.cell_count = self.grid_size * self.grid_size
+        self.particle_count = lib.dogm_get_particle_count(h)
+        self.new_born_particle_count = lib.dogm_get_new_born_particle_count(h)
+
+    def close(self) -> None:
+        if self.h:
+            load().dogm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- the update (dogm.cu:115-131) -----------------------------------------------------
+    def update_grid(self, meas, new_x: float, new_y: float, new_yaw: float, dt: float, device: bool = False) -> None:
+        """meas: MEAS_DTYPE array (host), an int device pointer (device=True) or None."""
+        if meas is None:
+            p = None
+        elif isinstance(meas, int):
+            p = C.c_void_p(meas)
+        else:
+            a = np.ascontiguousarray(meas)
+            assert a.nbytes == self.cell_count * 16, "measurement grid must hold grid_size^2 cells"
+            p = _ptr(a)
+        check(load().dogm_update(self.h, p, new_x, new_y, new_yaw, dt, 1 if device else 0), "dogm_update")
+
+    def synchronize(self) -> None:
+        check(load().dogm_synchronize(self.h), "dogm_synchronize")
+
+    # -- readback -------------------------------------------------------------------------
+    def get_grid_cells(self, out: np.ndarray | None = None) -> np.ndarray:
+        out = np.empty(self.cell_count, GRID_CELL_DTYPE) if out is None else out
+        check(load().dogm_get_grid_cells(self.h, _ptr(out), self.cell_count), "dogm_get_grid_cells")
+        return out
+
+    def get_measurement_cells(self) -> np.ndarray:
+        out = np.empty(self.cell_count, MEAS_DTYPE)
+        check(load().dogm_get_measurement_cells(self.h, _ptr(out), self.cell_count), "dogm_get_measurement_cells")
+        return out
+
+    def get_particles(self) -> dict:
+        n = self.particle_count
+        st = np.empty((n, 4), np.float32)
+        idx = np.empty(n, np.int32)
+        w = np.empty(n, np.float32)
+        a = np.empty(n, np.uint8)
+        check(load().dogm_get_particles(self.h, _ptr(st), _ptr(idx), _ptr(w), _ptr(a), n), "dogm_get_particles")
+        return {"state": st, "grid_cell_idx": idx, "weight": w, "associated": a}
+
+    def get_grid_size(self) -> int:
+        return load().dogm_get_grid_size(self.h)
+
+    def get_resolution(self) -> float:
+        return load().dogm_get_resolution(self.h)
+
+    def get_position_x(self) -> float:
+        return load().dogm_get_position_x(self.h)
+
+    def get_position_y(self) -> float:
+        return load().dogm_get_position_y(self.h)
+
+    def get_yaw(self) -> float:
+        return load().dogm_get_yaw(self.h)
+
+    def get_iteration(self) -> int:
+        return load().dogm_get_iteration(self.h)
+
+    def last_launch_count(self) -> int:
+        return load().dogm_last_launch_count(self.h)
+
+    # -- stages ---------------------------------------------------------------------------
+    def particle_prediction(self, dt: float) -> None:
+        check(load().dogm_particle_prediction(self.h, dt), "dogm_particle_prediction")
+
+    def update_pose(self, x: float, y: float, yaw: float) -> None:
+        check(load().dogm_update_pose(self.h, x, y, yaw), "dogm_update_pose")
+
+    def initialize_particles(self) -> None:
+        check(load().dogm_initialize_particles(self.h), "dogm_initialize_particles")
+
+    # -- state injection, replay, debug ---------------------------------------------------
+    def set_measurement_cells(self, meas: np.ndarray) -> None:
+        a = np.ascontiguousarray(meas)
+        check(load().dogm_set_measurement_cells(self.h, _ptr(a), self.cell_count), "dogm_set_measurement_cells")
+
+    def set_particles(self, state, grid_cell_idx, associated, weight: float) -> None:
+        st = np.ascontiguousarray(state, np.float32)
+        idx = np.ascontiguousarray(grid_cell_idx, np.int32)
+        a = np.ascontiguousarray(associated, np.uint8)
+        check(load().dogm_set_particles(self.h, _ptr(st), _ptr(idx), _ptr(a), weight, self.particle_count),
+              "dogm_set_particles")
+
+    def set_replay(self, init_u=None, predict_z=None, birth_z=None, resample_r=None) -> None:
+        arrs = [None if x is None else np.ascontiguousarray(x, np.float32) for x in (init_u, predict_z, birth_z)]
+        r = None if resample_r is None else np.array([resample_r], np.uint64)
+        self._replay_keep = arrs + [r]
+        check(load().dogm_set_replay(self.h, *[_ptr(x) for x in arrs], _ptr(r)), "dogm_set_replay")
+
+    def clear_replay(self) -> None:
+        check(load().dogm_clear_replay(self.h), "dogm_clear_replay")
+
+    def generate_draws(self, iteration: int) -> dict:
+        n, b = self.particle_count, self.new_born_particle_count
+        init_u = np.empty((n, 2), np.float32)
+        pz = np.empty((n, 4), np.float32)
+        bz = np.empty((max(b, 1), 2), np.float32)
+        r = np.zeros(1, np.uint64)
+        check(load().dogm_generate_draws(self.h, iteration, _ptr(init_u), _ptr(pz), _ptr(bz), _ptr(r)),
+              "dogm_generate_draws")
+        return {"init_u": init_u, "predict_z": pz, "birth_z": bz[:b], "resample_r": int(r[0])}
+
+    def debug_enable(self, enable: bool = True) -> None:
+        check(load().dogm_debug_enable(self.h, 1 if enable else 0), "dogm_debug_enable")
+
+    def debug_export(self) -> dict:
+        n, b = self.particle_count, self.new_born_particle_count
+        sc = np.empty(n, np.int32)
+        ss = np.empty((n, 4), np.float32)
+        sp = np.empty(n, np.int32)
+        bs = np.empty((max(b, 1), 4), np.float32)
+        bc = np.empty(max(b, 1), np.int32)
+        ba = np.empty(max(b, 1), np.uint8)
+        bw = np.empty(max(b, 1), np.float32)
+        rs = np.empty(n, np.int32)
+        jt = np.zeros(1, np.uint64)
+        qs = np.zeros(1, np.int32)
+        nb = np.zeros(1, np.int32)
+        check(load().dogm_debug_export(self.h, _ptr(sc), _ptr(ss), _ptr(sp), _ptr(bs), _ptr(bc), _ptr(ba), _ptr(bw),
+                                       _ptr(rs), _ptr(jt), _ptr(qs), _ptr(nb)), "dogm_debug_export")
+        return {"sorted_cell": sc, "sorted_state": ss, "sort_perm": sp, "birth_state": bs[:b], "birth_cell": bc[:b],
+                "birth_assoc": ba[:b], "birth_weight": bw[:b], "resample_src": rs, "joint_total": int(jt[0]),
+                "q_shift": int(qs[0]), "n_birth": int(nb[0])}
+
+
+def update_batch(grids: list[DOGM], meas: list, xs, ys, yaws, dts, device: bool = False) -> None:
+    """One batched update of several grids (uneven sizes allowed)."""
+    n = len(grids)
+    hs = (C.c_void_p * n)(*[g.h.value for g in grids])
+    keep = []
+    ptrs = (C.c_void_p * n)()
+    for i, m in enumerate(meas):
+        if m is None:
+            ptrs[i] = None
+        elif isinstance(m, int):
+            ptrs[i] = m
+        else:
+            a = np.ascontiguousarray(m)
+            keep.append(a)
+            ptrs[i] = a.ctypes.data
+    f = lambda v: np.ascontiguousarray(v, np.float32)
+    ax, ay, ayaw, adt = f(xs), f(ys), f(yaws), f(dts)
+    check(load().dogm_update_batch(hs, n, ptrs, _ptr(ax), _ptr(ay), _ptr(ayaw), _ptr(adt), 1 if device else 0),
+          "dogm_update_batch")
+
+
+def lower_bound_f32(accum: np.ndarray, queries: np.ndarray, clamp_last: bool = True) -> np.ndarray:
+    """Device multinomial index search (the reference's thrust::lower_bound step)."""
+    acc = np.ascontiguousarray(accum, np.float32)
+    q = np.ascontiguousarray(queries, np.float32)
+    da, dq, do = DeviceBuffer(acc.nbytes), DeviceBuffer(max(q.nbytes, 4)), DeviceBuffer(max(q.size * 4, 4))
+    da.upload(acc)
+    dq.upload(q)
+    check(load().dogm_lower_bound_f32(C.c_void_p(da.ptr), acc.size, C.c_void_p(dq.ptr), q.size, C.c_void_p(do.ptr),
+                                      1 if clamp_last else 0, None), "dogm_lower_bound_f32")
+    out = np.empty(q.size, np.int32)
+    do.download(out)
+    for b in (da, dq, do):
+        b.free()
+    return out
+
+
+def state_bytes(params: Params) -> int:
+    return int(load().dogm_state_bytes(C.byref(params)))

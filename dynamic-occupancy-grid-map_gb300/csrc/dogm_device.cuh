@@ -1,0 +1,268 @@
+// Device helpers shared by the DOGM kernels: Philox draws, exact fixed-point arithmetic,
+// the per-cell Dempster-Shafer update, tile claiming and bounded waits.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dogm_internal.h"
+
+namespace dogm_gb300 {
+
+// ---------------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel Random Numbers: As Easy as 1, 2, 3",
+// SC'11): 10 rounds of two 32x32->64 multiplies per round, Weyl-sequence key schedule.
+// ---------------------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
+    constexpr uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    constexpr uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+        const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += W0;
+        k1 += W1;
+    }
+    return c;
+}
+
+__device__ __forceinline__ U4 draw_block(const GridDesc& g, uint32_t index, uint32_t frame, uint32_t stage) {
+    return philox4x32_10(U4{index, frame, stage, g.stream_id}, g.seed_lo, g.seed_hi);
+}
+
+// 24-bit uniforms: (0,1] for logarithms and the reference's (0,1] curand_uniform range,
+// [0,1) for angles.
+__device__ __forceinline__ float u01_open0(uint32_t x) { return (float)((x >> 8) + 1u) * 5.9604644775390625e-8f; }
+__device__ __forceinline__ float u01_open1(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
+
+// Box-Muller: two standard normals from two uniforms.
+__device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b) {
+    const float u1 = u01_open0(a);
+    const float u2 = u01_open1(b);
+    const float r = sqrtf(-2.0f * logf(u1));
+    float s, c;
+    sincospif(2.0f * u2, &s, &c);
+    return make_float2(r * c, r * s);
+}
+
+// ---------------------------------------------------------------------------------------
+// Exact fixed point.  Weights and masses are quantised to multiples of 2^-S (S = q_shift,
+// chosen per grid so that every sum stays below 2^62); all scans over them are exact
+// integer scans, so any summation order gives the same bits.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long quantize(float w, int S) {
+    // round-to-nearest-even of w * 2^S for w in [0, 2]; <= 0 or NaN -> 0, > 2 clamps to 2.
+    if (!(w > 0.0f)) return 0ull;
+    if (w > 2.0f) w = 2.0f;
+    const uint32_t bits = __float_as_uint(w);
+    const int e = (int)(bits >> 23);
+    const uint32_t man = bits & 0x7fffffu;
+    const unsigned long long m = e ? (unsigned long long)(man | 0x800000u) : (unsigned long long)man;
+    const int sh = (e ? e - 150 : -149) + S;  // value = m * 2^(sh)
+    if (sh >= 0) return m << sh;
+    const int r = -sh;
+    if (r > 40) return 0ull;
+    const unsigned long long q = m >> r;
+    const unsigned long long rem = m & ((1ull << r) - 1ull);
+    const unsigned long long half = 1ull << (r - 1);
+    return q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+}
+
+struct U128 { unsigned long long hi, lo; };
+__device__ __forceinline__ U128 mul64(unsigned long long a, unsigned long long b) {
+    return U128{__umul64hi(a, b), a * b};
+}
+__device__ __forceinline__ U128 add64(U128 a, unsigned long long b) {
+    const unsigned long long lo = a.lo + b;
+    return U128{a.hi + (lo < a.lo ? 1ull : 0ull), lo};
+}
+__device__ __forceinline__ bool lt128(U128 a, U128 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool le128(U128 a, U128 b) { return !lt128(b, a); }
+
+// floor(Q * M / T) for Q <= T, T > 0: how many of M slots a prefix mass Q owns.
+// (The reference scales a float prefix sum by M / total and truncates:
+//  dogm/src/kernel/init_new_particles.cu:30-43,66-74.)
+__device__ __forceinline__ int alloc_boundary(unsigned long long Q, unsigned long long T, int M) {
+    if (T == 0ull) return 0;
+    if (Q >= T) return M;
+    const U128 qm = mul64(Q, (unsigned long long)M);
+    float f = ((float)Q / (float)T) * (float)M;
+    int b = (int)floorf(f);
+    b = b < 0 ? 0 : (b > M ? M : b);
+    while (b > 0 && lt128(qm, mul64((unsigned long long)b, T))) --b;
+    while (b < M && le128(mul64((unsigned long long)(b + 1), T), qm)) ++b;
+    return b;
+}
+
+// Systematic resampling comb: slot i takes the joint particle j with
+// A[j-1]*N <= i*T + U < A[j]*N (A = inclusive exact prefix, T = total, U in [0,T)).
+// comb_count(a) = #{ i in [0,N) : i*T + U < a*N }.  T == 0 sends every slot to particle 0.
+__device__ __forceinline__ int comb_count(unsigned long long a, unsigned long long T, unsigned long long U, int N) {
+    if (T == 0ull) return N;
+    if (a >= T) return N;
+    const U128 rhs = mul64(a, (unsigned long long)N);
+    float f = ((float)a * (float)N - (float)U) / (float)T;
+    int c = (int)ceilf(f);
+    c = c < 0 ? 0 : (c > N ? N : c);
+    // P(i): i*T + U < a*N is true for i < result, false from result on.
+    while (c > 0 && !lt128(add64(mul64((unsigned long long)(c - 1), T), U), rhs)) --c;
+    while (c < N && lt128(add64(mul64((unsigned long long)c, T), U), rhs)) ++c;
+    return c;
+}
+
+// ---------------------------------------------------------------------------------------
+// Per-cell update (FP32).  Order of operations is fixed with _rn intrinsics so the host
+// oracle reproduces every bit.  Formulas follow dogm/src/kernel/mass_update.cu:12-45 and
+// dogm/src/kernel/update_persistent_particles.cu:16-47.
+// ---------------------------------------------------------------------------------------
+struct CellOut {
+    float m_occ_pred, w_norm, free_up, occ_up, rho_b, rho_p;
+};
+
+__device__ __forceinline__ CellOut cell_masses(int n_in, float c, float free_prev, float alpha, float p_B,
+                                               float z_free, float z_occ) {
+    CellOut o;
+    float m = __fmul_rn((float)n_in, c);  // sum of the predicted weights of the cell
+    float wn = c;
+    if (m > 1.0f) {                        // mass_update.cu:75-79
+        wn = __fdiv_rn(c, m);
+        m = 1.0f;
+    }
+    const float one_m = __fsub_rn(1.0f, m);
+    const float mf = fminf(__fmul_rn(alpha, free_prev), one_m);         // predict_free_mass
+    const float unk = __fsub_rn(one_m, mf);                              // update_masses
+    const float meas_unk = __fsub_rn(__fsub_rn(1.0f, z_free), z_occ);
+    const float K = __fadd_rn(__fmul_rn(mf, z_occ), __fmul_rn(m, z_free));
+    const float den = __fsub_rn(1.0f, K);
+    const float occ = __fdiv_rn(__fadd_rn(__fadd_rn(__fmul_rn(m, meas_unk), __fmul_rn(unk, z_occ)), __fmul_rn(m, z_occ)), den);
+    const float fre = __fdiv_rn(__fadd_rn(__fadd_rn(__fmul_rn(mf, meas_unk), __fmul_rn(unk, z_free)), __fmul_rn(mf, z_free)), den);
+    // separate_newborn_part: rho_b = occ*p_B*(1-m) / (m + p_B*(1-m))
+    const float pb1m = __fmul_rn(p_B, one_m);
+    const float rb = __fdiv_rn(__fmul_rn(__fmul_rn(occ, p_B), one_m), __fadd_rn(m, pb1m));
+    o.m_occ_pred = m;
+    o.w_norm = wn;
+    o.free_up = fre;
+    o.occ_up = occ;
+    o.rho_b = rb;
+    o.rho_p = __fsub_rn(occ, rb);
+    return o;
+}
+
+// ---------------------------------------------------------------------------------------
+// Batches: tile claiming and grid lookup.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ int batch_total(const Batch* bt, int stage) { return bt->prefix[bt->n_grids][stage]; }
+
+__device__ __forceinline__ int grid_of_tile(const Batch* bt, int stage, int t) {
+    int lo = 0, hi = bt->n_grids - 1;
+    while (lo < hi) {  // largest i with prefix[i][stage] <= t
+        const int mid = (lo + hi + 1) >> 1;
+        if (bt->prefix[mid][stage] <= t) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Dynamic tile claim (tiles are taken in increasing order, which keeps decoupled
+// look-back deadlock free).  Every thread of the block gets the same tile.
+__device__ __forceinline__ int claim_tile(Batch* bt, int stage, int* smem_slot) {
+    if (threadIdx.x == 0) *smem_slot = (int)atomicAdd(&bt->counters[stage], 1u);
+    __syncthreads();
+    const int t = *smem_slot;
+    __syncthreads();
+    return t;
+}
+
+// ---------------------------------------------------------------------------------------
+// Bounded waits: every spin gives up after ~1 s, records kStatusTimeout and lets the
+// kernel finish, so a lost predecessor never hangs the GPU.
+// ---------------------------------------------------------------------------------------
+constexpr int kSpinLimit = 1 << 20;
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(const volatile uint32_t*)p; }
+__device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
+    return *(const volatile unsigned long long*)p;
+}
+__device__ __forceinline__ void st_volatile(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
+__device__ __forceinline__ void st_volatile(unsigned long long* p, unsigned long long v) {
+    *(volatile unsigned long long*)p = v;
+}
+
+__device__ __forceinline__ void flag_status(const GridDesc& g, uint32_t bits) {
+    atomicOr(&g.fs->status, bits);
+    atomicOr(g.status_out, bits);
+}
+__device__ __forceinline__ void flag_timeout(const GridDesc& g) { flag_status(g, kStatusTimeout); }
+
+// 64-bit look-back words: bit 63 inclusive, bit 62 aggregate, bits 0..61 value.
+constexpr unsigned long long kLbInc64 = 1ull << 63;
+constexpr unsigned long long kLbAgg64 = 1ull << 62;
+constexpr unsigned long long kLbVal64 = (1ull << 62) - 1ull;
+
+// Exclusive prefix of tile t from a chain of 64-bit look-back words (tile t has already
+// published its aggregate).  Called by one thread.
+__device__ __forceinline__ unsigned long long lookback64(const unsigned long long* lb, int t, const GridDesc& g) {
+    unsigned long long sum = 0ull;
+    int p = t - 1;
+    int spins = 0;
+    while (p >= 0) {
+        const unsigned long long v = ld_volatile(lb + p);
+        if (v & kLbInc64) { sum += v & kLbVal64; break; }
+        if (v & kLbAgg64) { sum += v & kLbVal64; --p; continue; }
+        if (++spins > kSpinLimit) { flag_timeout(g); break; }
+        __nanosleep(64);
+    }
+    return sum;
+}
+
+// Block-wide exclusive scan of one 64-bit value per thread (256 threads).  Returns the
+// exclusive prefix; *total receives the block sum.  scratch: >= 8 entries.
+__device__ __forceinline__ unsigned long long block_excl_scan_u64(unsigned long long v, unsigned long long* scratch,
+                                                                  unsigned long long* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) scratch[warp] = x;
+    __syncthreads();
+    unsigned long long wpre = 0ull, tot = 0ull;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+        const unsigned long long s = scratch[w];
+        if (w < warp) wpre += s;
+        tot += s;
+    }
+    __syncthreads();
+    *total = tot;
+    return wpre + x - v;
+}
+
+// Block-wide exclusive scan of one int per thread.
+__device__ __forceinline__ int block_excl_scan_i32(int v, int* scratch, int* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) scratch[warp] = x;
+    __syncthreads();
+    int wpre = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+        const int s = scratch[w];
+        if (w < warp) wpre += s;
+        tot += s;
+    }
+    __syncthreads();
+    *total = tot;
+    return wpre + x - v;
+}
+
+}  // namespace dogm_gb300

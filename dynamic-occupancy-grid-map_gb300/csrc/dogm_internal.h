@@ -1,0 +1,157 @@
+// Internal device-side layout shared by the kernels and the host runtime.
+//
+// One grid (one dogm_handle) is described by a GridDesc.  A launch processes a Batch of
+// GridDescs: every stage kernel is a persistent kernel whose blocks pull tiles from the
+// concatenated tile space of all grids in the batch, so the same launch sequence (and the
+// same CUDA graph) serves one grid or many uneven grids.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "dogm_gb300.h"
+
+namespace dogm_gb300 {
+
+// ---- tile shapes (elements per tile; 256-thread blocks everywhere) ---------------------
+constexpr int kThreads = 256;
+constexpr int kPredictTile = 4096;   // particles per predict tile (16 per thread)
+constexpr int kSortIpt = 16;         // keys per thread in a sort pass
+constexpr int kSortTile = kThreads * kSortIpt;
+constexpr int kSortMaxBits = 11;     // radix digit width <= 11 -> <= 2048 bins
+constexpr int kSortMaxBins = 1 << kSortMaxBits;
+constexpr int kSegIpt = 8;           // sorted particles per thread in the segmented reduction
+constexpr int kSegTile = kThreads * kSegIpt;
+constexpr int kCellIpt = 4;          // cells per thread in the cell passes
+constexpr int kCellTile = kThreads * kCellIpt;
+constexpr int kResIpt = 8;           // joint particles per thread in resampling
+constexpr int kResTile = kThreads * kResIpt;
+
+constexpr int kMaxKeyBits = 22;      // grid_size <= 2048 -> cells < 2^22 -> 2 radix passes
+constexpr int kMaxParticles = (1 << 24) - 1;  // sort look-back words hold 24-bit counts
+
+// Particle key word: bits 0..29 cell index, bit 30 "out of grid" (weight 0), bit 31 associated.
+constexpr uint32_t kCellMask = 0x3fffffffu;
+constexpr uint32_t kOutBit = 1u << 30;
+constexpr uint32_t kAssocBit = 1u << 31;
+
+// Philox counter word 2: which draw family.
+enum DrawStage : uint32_t { kDrawInit = 1, kDrawPredict = 2, kDrawBirth = 3, kDrawResample = 4 };
+
+// Stages that claim tiles from a work counter (look-back ordering) or iterate statically.
+enum Stage : int {
+    kStPredict = 0, kStSort0, kStSort1, kStSeg, kStCell, kStBirth, kStResample, kStInitScan, kStInitExpand,
+    kNumStages
+};
+
+// Per-grid state that lives on the device across frames.
+struct FrameState {
+    // written by one update, read by the next
+    float w_res;          // common particle weight after the last resampling (or 1/N)
+    uint32_t status;      // sticky error bits (kStatus*)
+    // per-frame accumulators (zeroed by the frame-begin kernel)
+    unsigned long long qb_total;   // sum of quantised newborn masses (exact)
+    unsigned long long joint_total;// sum of quantised joint weights (exact)
+    unsigned long long qo_total;   // first frame: sum of quantised measured occupancy
+    int n_birth;                   // newborns created this frame (B or 0)
+    int pad;
+};
+constexpr uint32_t kStatusTimeout = 1u;  // a bounded wait gave up
+constexpr uint32_t kStatusBounds = 2u;   // an index check refused a write
+
+// Partial sums of one particle segment (one cell): in-grid count and velocity moments.
+struct SegSums {
+    int n_in;
+    float vx, vy, vxx, vyy, vxy;
+};
+
+struct GridDesc {
+    // sizes
+    int N, B, C, gs;
+    int d0_bits, d1_bits;   // radix digit widths (d0 low digit)
+    int q_shift;            // fixed point: weight w -> round(w * 2^q_shift)
+    int pad0;
+    // filter parameters
+    float p_S, sigma_pos, sigma_vel, p_B, sigma_birth, init_max_vel;
+    // per-frame parameters
+    float dt, alpha;        // alpha = freespace_discount^dt (host powf, as dogm.cu:291)
+    int shift_x, shift_y;   // cells to shift (x_move, y_move of dogm.cu:177-178)
+    int shifted;            // 1 when the pose moved by more than one cell this frame
+    int copy_meas;          // 1: meas_src is a caller buffer to copy into meas_own
+    uint32_t frame;         // iteration number (Philox counter word 1)
+    uint32_t stream_id;     // Philox counter word 3
+    uint32_t seed_lo, seed_hi;
+    uint32_t epoch;         // sort look-back epoch tag (frame & 63)
+    int clear_lookback;     // 1: the frame-begin kernel zeroes the sort look-back words
+    // particles (persistent: P, sort temporaries: T, sorted: S, newborn: Bp)
+    float4* P_state; uint32_t* P_key;
+    uint32_t* T_key; uint32_t* T_idx;
+    float4* S_state; uint32_t* S_key;
+    float4* B_state; uint32_t* B_key; float* B_w;
+    // cells
+    dogm_grid_cell* cells;
+    const dogm_measurement_cell* meas_src;
+    dogm_measurement_cell* meas_own;
+    float* free_old; float* free_new;   // free mass of the previous / this frame (ping-pong)
+    int4* seg_i;            // per cell: {start, end, n_in, float_bits(sum vxy)}
+    float4* seg_f;          // per cell: {sum vx, sum vy, sum vxx, sum vyy}
+    float* rho_b;           // per cell newborn mass of this frame
+    float* w_cell;          // per cell weight of an in-grid persistent particle after reweighting
+    uint32_t* occ_bits;     // per cell occupancy bit of this frame
+    // scratch
+    uint32_t* hist;         // 2 x kSortMaxBins digit histograms
+    uint32_t* lb_sort;      // 2 x sort_tiles x kSortMaxBins look-back words
+    SegSums* seg_head;      // per segmented-reduction tile: partial of the segment entering it
+    SegSums* seg_tail;      // per tile: partial of the segment leaving it
+    unsigned long long* lb_cell;   // per cell tile: look-back of quantised newborn masses
+    unsigned long long* lb_res;    // per resample tile: look-back of quantised joint weights
+    FrameState* fs;
+    unsigned int* status_out;  // the batch-level status word
+    // replay inputs (NULL: Philox) and debug outputs (NULL: off)
+    const float2* rp_init; const float4* rp_predict; const float2* rp_birth; const unsigned long long* rp_resample;
+    int* dbg_perm; int* dbg_src;
+    // tiles per stage (sort_tiles sizes the look-back arrays)
+    int tiles[kNumStages];
+    int sort_tiles;
+    int pad1;
+};
+
+constexpr int kMaxBatch = 256;
+
+// Device copy of one batch.  The host uploads the header, prefix rows 0..n and g[0..n)
+// before every frame; the upload also zeroes the tile counters.
+struct Batch {
+    int n_grids;
+    unsigned int status;                     // OR of every grid's error bits this frame
+    unsigned int counters[kNumStages];       // dynamic tile counters
+    int prefix[kMaxBatch + 1][kNumStages];   // prefix[i][s]: tiles of stage s in grids < i
+    GridDesc g[kMaxBatch];
+};
+
+// ---- kernel launchers (defined in the .cu files) ---------------------------------------
+struct LaunchCfg {
+    int num_sms;
+    cudaStream_t stream;
+};
+
+cudaError_t prepare_kernels();  // per device, before the first launch
+cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCfg& cfg);
+cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg);
+cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_segments(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_shift_stage(const GridDesc& g, int x_move, int y_move, const LaunchCfg& cfg);
+cudaError_t launch_draws(const GridDesc& g, int iteration, float2* init_u, float4* predict_z, float2* birth_z,
+                         unsigned long long* resample_r, const LaunchCfg& cfg);
+cudaError_t launch_lower_bound(const float* accum, int n_accum, const float* q, int n_q, int* out, int clamp_last,
+                               cudaStream_t s);
+
+// Kernel launches per update (for the launch-count claim): frame-begin, predict, 2 sort
+// passes, segments, cells, newborn, resample.
+constexpr int kLaunchesPerFrame = 8;
+constexpr int kLaunchesInit = 2;
+
+}  // namespace dogm_gb300

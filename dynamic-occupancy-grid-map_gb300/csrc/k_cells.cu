@@ -1,0 +1,378 @@
+// Cell-side kernels.
+//  k_segments : one pass over the sorted particles; per cell (segment) the in-grid count
+//               and the velocity sums sum(v), sum(v^2), sum(vx*vy).  Replaces
+//               particleToGridKernel (particle_to_grid.cu:22-40), the weight-array copy and
+//               the five statistical-moment prefix scans (dogm.cu:350-384).
+//  k_cells    : one pass over all cells; fuses the predicted/free mass, the Dempster-Shafer
+//               measurement update and newborn split (mass_update.cu:57-89), the persistent
+//               reweighting (update_persistent_particles.cu:49-87), the moments
+//               (statistical_moments.cu:78-106), the ego shift of the free mass
+//               (ego_motion_compensation.cu:25-43) and the measurement copy (dogm.cu:205-208).
+//  k_newborn  : newborn allocation over an exact scan of the newborn masses and newborn
+//               initialisation (init_new_particles.cu:126-195, dogm.cu:323-348).
+#include "dogm_device.cuh"
+
+namespace dogm_gb300 {
+
+// ---------------------------------------------------------------------------------------
+// Segmented reduction over sorted particles.
+// ---------------------------------------------------------------------------------------
+struct SegRun {
+    int head;      // sorted position of the segment head inside this tile, -1 if it began earlier
+    int n;
+    float vx, vy, vxx, vyy, vxy;
+};
+
+__device__ __forceinline__ SegRun seg_combine(const SegRun& a, const SegRun& b) {
+    if (b.head >= 0) return b;
+    SegRun r;
+    r.head = a.head;
+    r.n = a.n + b.n;
+    r.vx = __fadd_rn(a.vx, b.vx);
+    r.vy = __fadd_rn(a.vy, b.vy);
+    r.vxx = __fadd_rn(a.vxx, b.vxx);
+    r.vyy = __fadd_rn(a.vyy, b.vyy);
+    r.vxy = __fadd_rn(a.vxy, b.vxy);
+    return r;
+}
+
+__device__ __forceinline__ SegRun seg_shfl_up(const SegRun& a, int o) {
+    SegRun r;
+    r.head = __shfl_up_sync(0xffffffffu, a.head, o);
+    r.n = __shfl_up_sync(0xffffffffu, a.n, o);
+    r.vx = __shfl_up_sync(0xffffffffu, a.vx, o);
+    r.vy = __shfl_up_sync(0xffffffffu, a.vy, o);
+    r.vxx = __shfl_up_sync(0xffffffffu, a.vxx, o);
+    r.vyy = __shfl_up_sync(0xffffffffu, a.vyy, o);
+    r.vxy = __shfl_up_sync(0xffffffffu, a.vxy, o);
+    return r;
+}
+
+__device__ __forceinline__ SegSums to_sums(const SegRun& r) {
+    SegSums s;
+    s.n_in = r.n;
+    s.vx = r.vx; s.vy = r.vy; s.vxx = r.vxx; s.vyy = r.vyy; s.vxy = r.vxy;
+    return s;
+}
+
+__global__ void __launch_bounds__(kThreads) k_segments(Batch* bt) {
+    __shared__ uint32_t skey[kSegTile + 2];
+    __shared__ SegRun wagg[kThreads / 32];
+    const int total = batch_total(bt, kStSeg);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const int gi = grid_of_tile(bt, kStSeg, t);
+        const GridDesc& g = bt->g[gi];
+        const int lt = t - bt->prefix[gi][kStSeg];
+        const int base = lt * kSegTile;
+        const int n = min(kSegTile, g.N - base);
+        for (int i = threadIdx.x; i < n; i += kThreads) skey[1 + i] = g.S_key[base + i];
+        if (threadIdx.x == 0) {
+            skey[0] = base > 0 ? (g.S_key[base - 1] & kCellMask) : 0xffffffffu;
+            skey[n + 1] = (base + n < g.N) ? (g.S_key[base + n] & kCellMask) : 0xffffffffu;
+        }
+        __syncthreads();
+
+        // thread items: j = tid*kSegIpt + r (blocked)
+        SegRun item[kSegIpt];
+        bool head[kSegIpt], tail[kSegIpt];
+        uint32_t cell[kSegIpt];
+        SegRun agg;
+        agg.head = -1; agg.n = 0; agg.vx = agg.vy = agg.vxx = agg.vyy = agg.vxy = 0.0f;
+#pragma unroll
+        for (int r = 0; r < kSegIpt; ++r) {
+            const int j = threadIdx.x * kSegIpt + r;
+            SegRun it;
+            it.head = -1; it.n = 0; it.vx = it.vy = it.vxx = it.vyy = it.vxy = 0.0f;
+            head[r] = tail[r] = false;
+            cell[r] = 0u;
+            if (j < n) {
+                const uint32_t kw = skey[1 + j];
+                const uint32_t c = kw & kCellMask;
+                cell[r] = c;
+                const uint32_t prev = (j == 0) ? skey[0] : (skey[j] & kCellMask);
+                const uint32_t next = (j == n - 1) ? skey[n + 1] : (skey[2 + j] & kCellMask);
+                head[r] = (c != prev);
+                tail[r] = (c != next);
+                if (!(kw & kOutBit)) {
+                    const float4 s = g.S_state[base + j];
+                    it.n = 1;
+                    it.vx = s.z;
+                    it.vy = s.w;
+                    it.vxx = __fmul_rn(s.z, s.z);
+                    it.vyy = __fmul_rn(s.w, s.w);
+                    it.vxy = __fmul_rn(s.z, s.w);
+                }
+                if (head[r]) it.head = base + j;
+            }
+            item[r] = it;
+            agg = seg_combine(agg, it);
+        }
+        // warp inclusive segmented scan of the thread aggregates
+        SegRun inc = agg;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const SegRun other = seg_shfl_up(inc, o);
+            if (lane >= o) inc = seg_combine(other, inc);
+        }
+        if (lane == 31) wagg[warp] = inc;
+        SegRun excl = seg_shfl_up(inc, 1);
+        __syncthreads();
+        SegRun wpre;
+        wpre.head = -1; wpre.n = 0; wpre.vx = wpre.vy = wpre.vxx = wpre.vyy = wpre.vxy = 0.0f;
+        for (int w = 0; w < warp; ++w) wpre = seg_combine(wpre, wagg[w]);
+        excl = (lane == 0) ? wpre : seg_combine(wpre, excl);
+
+        // re-walk and emit at segment tails
+        SegRun run = excl;
+#pragma unroll
+        for (int r = 0; r < kSegIpt; ++r) {
+            const int j = threadIdx.x * kSegIpt + r;
+            if (j >= n) break;
+            run = seg_combine(run, item[r]);
+            const int pos = base + j;
+            const uint32_t c = cell[r];
+            if (tail[r]) {
+                if (run.head >= 0) {
+                    const SegSums s = to_sums(run);
+                    g.seg_i[c] = make_int4(run.head, pos, s.n_in, __float_as_int(s.vxy));
+                    g.seg_f[c] = make_float4(s.vx, s.vy, s.vxx, s.vyy);
+                    atomicOr(&g.occ_bits[c >> 5], 1u << (c & 31));
+                } else {
+                    g.seg_head[lt] = to_sums(run);
+                    g.seg_i[c].y = pos;
+                }
+            } else if (j == n - 1) {
+                if (run.head >= 0) {
+                    g.seg_tail[lt] = to_sums(run);
+                    g.seg_i[c].x = run.head;
+                    atomicOr(&g.occ_bits[c >> 5], 1u << (c & 31));
+                } else {
+                    g.seg_head[lt] = to_sums(run);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Fused per-cell update.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_cells(Batch* bt) {
+    __shared__ int slot;
+    __shared__ unsigned long long red[kThreads / 32];
+    __shared__ unsigned long long red2[kThreads / 32];
+    const int total = batch_total(bt, kStCell);
+    for (;;) {
+        const int t = claim_tile(bt, kStCell, &slot);
+        if (t >= total) break;
+        const int gi = grid_of_tile(bt, kStCell, t);
+        const GridDesc& g = bt->g[gi];
+        const int lt = t - bt->prefix[gi][kStCell];
+        const int base = lt * kCellTile;
+        const float c_pred = __fmul_rn(g.p_S, g.fs->w_res);  // predicted weight of an in-grid particle
+        unsigned long long qb = 0ull, jq = 0ull;
+        for (int r = 0; r < kCellIpt; ++r) {
+            const int k = base + r * kThreads + threadIdx.x;
+            if (k >= g.C) break;
+            const int x = k % g.gs, y = k / g.gs;
+            const bool occupied = (g.occ_bits[k >> 5] >> (k & 31)) & 1u;
+            int start = -1, end = -1;
+            SegSums s;
+            s.n_in = 0; s.vx = s.vy = s.vxx = s.vyy = s.vxy = 0.0f;
+            if (occupied) {
+                const int4 si = g.seg_i[k];
+                start = si.x;
+                end = si.y;
+                const int ts = start / kSegTile, te = end / kSegTile;
+                if (ts == te) {
+                    const float4 sf = g.seg_f[k];
+                    s.n_in = si.z;
+                    s.vxy = __int_as_float(si.w);
+                    s.vx = sf.x; s.vy = sf.y; s.vxx = sf.z; s.vyy = sf.w;
+                } else {
+                    s = g.seg_tail[ts];
+                    for (int tt = ts + 1; tt <= te; ++tt) {
+                        const SegSums h = g.seg_head[tt];
+                        s.n_in += h.n_in;
+                        s.vx = __fadd_rn(s.vx, h.vx);
+                        s.vy = __fadd_rn(s.vy, h.vy);
+                        s.vxx = __fadd_rn(s.vxx, h.vxx);
+                        s.vyy = __fadd_rn(s.vyy, h.vyy);
+                        s.vxy = __fadd_rn(s.vxy, h.vxy);
+                    }
+                }
+            }
+            float free_prev;
+            if (g.shifted) {
+                const int sx = x + g.shift_x, sy = y + g.shift_y;
+                const bool ok = sx > 0 && sx < g.gs && sy > 0 && sy < g.gs;  // strict, as the reference
+                free_prev = ok ? g.free_old[sx + g.gs * sy] : 0.0f;
+            } else {
+                free_prev = g.free_old[k];
+            }
+            const dogm_measurement_cell m = g.meas_src[k];
+            if (g.copy_meas) g.meas_own[k] = m;
+            const CellOut o = cell_masses(s.n_in, c_pred, free_prev, g.alpha, g.p_B, m.free_mass, m.occ_mass);
+            float muA = 0.0f, muUA = 0.0f, wp = 0.0f;
+            float mx = 0.0f, my = 0.0f, vx = 0.0f, vy = 0.0f, cxy = 0.0f;
+            if (occupied) {
+                const float wu = __fmul_rn(m.likelihood, o.w_norm);
+                const float swu = __fmul_rn((float)s.n_in, wu);
+                muA = swu > 0.0f ? __fdiv_rn(o.rho_p, swu) : 0.0f;
+                muUA = o.m_occ_pred > 0.0f ? __fdiv_rn(o.rho_p, o.m_occ_pred) : 0.0f;
+                wp = __fadd_rn(__fmul_rn(__fmul_rn(m.p_A, muA), wu),
+                               __fmul_rn(__fmul_rn(__fsub_rn(1.0f, m.p_A), muUA), o.w_norm));
+                if (o.rho_p > 0.0f) {
+                    const float inv = __fdiv_rn(1.0f, o.rho_p);
+                    mx = __fmul_rn(inv, __fmul_rn(wp, s.vx));
+                    my = __fmul_rn(inv, __fmul_rn(wp, s.vy));
+                    vx = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vxx)), __fmul_rn(mx, mx));
+                    vy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vyy)), __fmul_rn(my, my));
+                    cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vxy)), __fmul_rn(mx, my));
+                }
+            }
+            float4* rec = reinterpret_cast<float4*>(g.cells + k);
+            rec[0] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
+            rec[1] = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
+            rec[2] = make_float4(muUA, 0.0f, 0.0f, mx);
+            rec[3] = make_float4(my, vx, vy, cxy);
+            g.free_new[k] = o.free_up;
+            g.rho_b[k] = o.rho_b;
+            g.w_cell[k] = wp;
+            qb += quantize(o.rho_b, g.q_shift);
+            jq += (unsigned long long)s.n_in * quantize(wp, g.q_shift);
+        }
+        unsigned long long tile_qb, tile_jq;
+        block_excl_scan_u64(qb, red, &tile_qb);
+        block_excl_scan_u64(jq, red2, &tile_jq);
+        if (threadIdx.x == 0) {
+            unsigned long long* lb = g.lb_cell;
+            if (lt == 0) {
+                st_volatile(lb, kLbInc64 | tile_qb);
+            } else {
+                st_volatile(lb + lt, kLbAgg64 | tile_qb);
+                const unsigned long long excl = lookback64(lb, lt, g);
+                st_volatile(lb + lt, kLbInc64 | (excl + tile_qb));
+            }
+            atomicAdd(&g.fs->qb_total, tile_qb);
+            atomicAdd(&g.fs->joint_total, tile_jq);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Newborn allocation and initialisation.  Cell k owns newborn slots
+// [floor(Q[k-1] B / Q), floor(Q[k] B / Q)) of the exact prefix Q of quantised newborn
+// masses; nu_A = round(n p_A) of them are associated (the reference marks nu_A + 1,
+// racing with the next cell: init_new_particles.cu:145-153).
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
+    __shared__ unsigned long long red[kThreads / 32];
+    __shared__ int bnd[kCellTile + 1];
+    __shared__ int s_nuA[kCellTile];
+    __shared__ float s_wA[kCellTile], s_wUA[kCellTile];
+    const int total = batch_total(bt, kStBirth);
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const int gi = grid_of_tile(bt, kStBirth, t);
+        const GridDesc& g = bt->g[gi];
+        const int lt = t - bt->prefix[gi][kStBirth];
+        const int base = lt * kCellTile;
+        const unsigned long long T = g.fs->qb_total;
+        const unsigned long long E = lt > 0 ? (ld_volatile(g.lb_cell + lt - 1) & kLbVal64) : 0ull;
+        unsigned long long q[kCellIpt];
+        float rb[kCellIpt];
+        unsigned long long v = 0ull;
+#pragma unroll
+        for (int j = 0; j < kCellIpt; ++j) {
+            const int k = base + threadIdx.x * kCellIpt + j;
+            rb[j] = (k < g.C) ? g.rho_b[k] : 0.0f;
+            q[j] = (k < g.C) ? quantize(rb[j], g.q_shift) : 0ull;
+            v += q[j];
+        }
+        unsigned long long tile_sum;
+        unsigned long long acc = E + block_excl_scan_u64(v, red, &tile_sum);
+        if (threadIdx.x == 0) bnd[0] = alloc_boundary(E, T, g.B);
+        int lo_c = alloc_boundary(acc, T, g.B);
+        unsigned long long jq = 0ull;
+#pragma unroll
+        for (int j = 0; j < kCellIpt; ++j) {
+            const int c = threadIdx.x * kCellIpt + j;
+            const int k = base + c;
+            acc += q[j];
+            const int hi_c = alloc_boundary(acc, T, g.B);
+            bnd[1 + c] = hi_c;
+            const int nnew = hi_c - lo_c;
+            int nuA = 0;
+            float wA = 0.0f, wUA = 0.0f;
+            if (nnew > 0 && k < g.C) {
+                const float pA = g.meas_own[k].p_A;
+                nuA = (int)roundf(__fmul_rn((float)nnew, pA));
+                const int nuUA = nnew - nuA;
+                wA = nuA > 0 ? __fdiv_rn(__fmul_rn(pA, rb[j]), (float)nuA) : 0.0f;
+                wUA = nuUA > 0 ? __fdiv_rn(__fmul_rn(__fsub_rn(1.0f, pA), rb[j]), (float)nuUA) : 0.0f;
+                g.cells[k].w_A = wA;
+                g.cells[k].w_UA = wUA;
+                jq += (unsigned long long)max(nuA, 0) * quantize(wA, g.q_shift) +
+                      (unsigned long long)max(nuUA, 0) * quantize(wUA, g.q_shift);
+            }
+            s_nuA[c] = nuA;
+            s_wA[c] = wA;
+            s_wUA[c] = wUA;
+            lo_c = hi_c;
+        }
+        __syncthreads();
+        const int ncell = min(kCellTile, g.C - base);
+        const int lo = bnd[0], hi = bnd[ncell];
+        const float fgs = (float)g.gs;
+        for (int s = lo + threadIdx.x; s < hi; s += kThreads) {
+            int a = 0, b = ncell - 1;
+            while (a < b) {
+                const int m = (a + b) >> 1;
+                if (bnd[1 + m] > s) b = m; else a = m + 1;
+            }
+            const int k = base + a;
+            const bool assoc = (s - bnd[a]) < s_nuA[a];
+            float2 z;
+            if (g.rp_birth) {
+                z = g.rp_birth[s];
+            } else {
+                const U4 r = draw_block(g, (uint32_t)s, g.frame, kDrawBirth);
+                z = box_muller(r.x, r.y);
+            }
+            float4 st;
+            st.x = __fadd_rn((float)(k % g.gs), 0.5f);
+            st.y = __fadd_rn(__fdiv_rn((float)k, fgs), 0.5f);  // float division, as the reference
+            st.z = __fmaf_rn(z.x, g.sigma_birth, 0.0f);
+            st.w = __fmaf_rn(z.y, g.sigma_birth, 0.0f);
+            g.B_state[s] = st;
+            g.B_key[s] = (uint32_t)k | (assoc ? kAssocBit : 0u);
+            g.B_w[s] = assoc ? s_wA[a] : s_wUA[a];
+        }
+        unsigned long long tile_jq;
+        block_excl_scan_u64(jq, red, &tile_jq);
+        if (threadIdx.x == 0) {
+            if (tile_jq) atomicAdd(&g.fs->joint_total, tile_jq);
+            if (lt == 0) g.fs->n_birth = (T > 0ull) ? g.B : 0;
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t launch_segments(const Batch* d_batch, const LaunchCfg& cfg) {
+    k_segments<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg) {
+    k_cells<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg) {
+    k_newborn<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    return cudaGetLastError();
+}
+
+}  // namespace dogm_gb300

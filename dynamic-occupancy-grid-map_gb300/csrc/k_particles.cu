@@ -1,0 +1,331 @@
+// Particle-side kernels: frame begin, prediction (with the fused ego shift), first-frame
+// particle initialisation, the stand-alone shift stage and Philox draw export.
+#include "dogm_device.cuh"
+
+namespace dogm_gb300 {
+
+// ---------------------------------------------------------------------------------------
+// Frame begin: zero the per-frame scratch of every grid in the batch.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* bt) {
+    const int stride = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int gi = 0; gi < bt->n_grids; ++gi) {
+        const GridDesc& g = bt->g[gi];
+        for (int i = tid; i < 2 * kSortMaxBins; i += stride) g.hist[i] = 0u;
+        const int words = (g.C + 31) >> 5;
+        for (int i = tid; i < words; i += stride) g.occ_bits[i] = 0u;
+        for (int i = tid; i < 2 * g.tiles[kStCell]; i += stride) g.lb_cell[i] = 0ull;
+        for (int i = tid; i < g.tiles[kStResample]; i += stride) g.lb_res[i] = 0ull;
+        if (g.clear_lookback) {
+            const size_t n = (size_t)2 * g.sort_tiles * kSortMaxBins;
+            for (size_t i = tid; i < n; i += stride) g.lb_sort[i] = 0u;
+        }
+        if (tid == 0) {
+            g.fs->status = 0u;
+            g.fs->qb_total = 0ull;
+            g.fs->joint_total = 0ull;
+            g.fs->qo_total = 0ull;
+            g.fs->n_birth = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Prediction (dogm/src/kernel/predict.cu:12-48), fused with the particle half of the ego
+// shift (dogm/src/kernel/ego_motion_compensation.cu:16-23).
+//   s' = F s + noise, F = [[1,0,dt,0],[0,1,0,dt],[0,0,1,0],[0,0,0,1]]
+// evaluated as x' = (x + dt*vx) + n_x (the grouping of the reference's mat4 x vec4);
+// the weight is not stored per particle: every persistent particle carries the common
+// weight w_res, so the predicted weight is p_S * w_res, or 0 out of the grid (bit 30).
+// mode 0: full frame (shift + digit histograms); mode 1: stage call (no histograms).
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_predict(Batch* bt, int mode) {
+    __shared__ uint32_t h0[kSortMaxBins];
+    __shared__ uint32_t h1[kSortMaxBins];
+    const int total = batch_total(bt, kStPredict);
+    const int lane = threadIdx.x & 31;
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const int gi = grid_of_tile(bt, kStPredict, t);
+        const GridDesc& g = bt->g[gi];
+        const int lt = t - bt->prefix[gi][kStPredict];
+        const int nb0 = 1 << g.d0_bits, nb1 = 1 << g.d1_bits;
+        if (mode == 0) {
+            for (int i = threadIdx.x; i < nb0; i += kThreads) h0[i] = 0u;
+            for (int i = threadIdx.x; i < nb1; i += kThreads) h1[i] = 0u;
+            __syncthreads();
+        }
+        const float gsm1 = (float)(g.gs - 1);
+        const float dt = g.dt;
+        const bool shift = (mode == 0) && g.shifted;
+        const float fsx = (float)g.shift_x, fsy = (float)g.shift_y;
+        const int base = lt * kPredictTile;
+#pragma unroll 4
+        for (int k = 0; k < kPredictTile / kThreads; ++k) {
+            const int i = base + k * kThreads + threadIdx.x;
+            const bool valid = i < g.N;
+            uint32_t key = 0xffffffffu;
+            if (valid) {
+                float4 s = g.P_state[i];
+                const uint32_t kw = g.P_key[i];
+                if (shift) {
+                    s.x = __fsub_rn(s.x, fsx);
+                    s.y = __fsub_rn(s.y, fsy);
+                }
+                float4 z;
+                if (g.rp_predict) {
+                    z = g.rp_predict[i];
+                } else {
+                    const U4 r = draw_block(g, (uint32_t)i, g.frame, kDrawPredict);
+                    const float2 a = box_muller(r.x, r.y);
+                    const float2 b = box_muller(r.z, r.w);
+                    z = make_float4(a.x, a.y, b.x, b.y);
+                }
+                const float nx = __fmaf_rn(z.x, g.sigma_pos, 0.0f);
+                const float ny = __fmaf_rn(z.y, g.sigma_pos, 0.0f);
+                const float nvx = __fmaf_rn(z.z, g.sigma_vel, 0.0f);
+                const float nvy = __fmaf_rn(z.w, g.sigma_vel, 0.0f);
+                float4 o;
+                o.x = __fadd_rn(__fadd_rn(s.x, __fmul_rn(dt, s.z)), nx);
+                o.y = __fadd_rn(__fadd_rn(s.y, __fmul_rn(dt, s.w)), ny);
+                o.z = __fadd_rn(s.z, nvx);
+                o.w = __fadd_rn(s.w, nvy);
+                const bool out = (o.x > gsm1) || (o.x < 0.0f) || (o.y > gsm1) || (o.y < 0.0f);
+                const int px = min(max(__float2int_rz(o.x), 0), g.gs - 1);
+                const int py = min(max(__float2int_rz(o.y), 0), g.gs - 1);
+                key = (uint32_t)(px + g.gs * py);
+                g.P_state[i] = o;
+                g.P_key[i] = key | (out ? kOutBit : 0u) | (kw & kAssocBit);
+            }
+            if (mode == 0) {
+                const uint32_t peers = __match_any_sync(0xffffffffu, key);
+                if (valid && lane == __ffs(peers) - 1) {
+                    const uint32_t cnt = __popc(peers);
+                    atomicAdd(&h0[key & (nb0 - 1)], cnt);
+                    atomicAdd(&h1[key >> g.d0_bits], cnt);
+                }
+            }
+        }
+        if (mode == 0) {
+            __syncthreads();
+            for (int i = threadIdx.x; i < nb0; i += kThreads)
+                if (h0[i]) atomicAdd(&g.hist[i], h0[i]);
+            for (int i = threadIdx.x; i < nb1; i += kThreads)
+                if (h1[i]) atomicAdd(&g.hist[kSortMaxBins + i], h1[i]);
+            __syncthreads();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// First frame: particles spread over the cells in proportion to the measured occupied
+// mass (dogm/src/dogm.cu:217-241, init_new_particles.cu:76-124).  The proportional
+// allocation is an exact fixed-point scan instead of a float scan scaled by N / total.
+// An all-zero measurement spreads the particles uniformly (the reference divides by 0).
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_init_scan(Batch* bt) {
+    __shared__ int slot;
+    __shared__ unsigned long long red[kThreads / 32];
+    const int total = batch_total(bt, kStInitScan);
+    for (;;) {
+        const int t = claim_tile(bt, kStInitScan, &slot);
+        if (t >= total) break;
+        const int gi = grid_of_tile(bt, kStInitScan, t);
+        const GridDesc& g = bt->g[gi];
+        const int lt = t - bt->prefix[gi][kStInitScan];
+        unsigned long long* lb = g.lb_cell + g.tiles[kStCell];  // second half: init scan
+        const int base = lt * kCellTile;
+        unsigned long long v = 0ull;
+        for (int j = 0; j < kCellIpt; ++j) {
+            const int k = base + threadIdx.x * kCellIpt + j;
+            if (k < g.C) v += quantize(g.meas_src[k].occ_mass, g.q_shift);
+        }
+        unsigned long long tile_sum;
+        block_excl_scan_u64(v, red, &tile_sum);
+        if (threadIdx.x == 0) {
+            if (lt == 0) {
+                st_volatile(lb + lt, kLbInc64 | tile_sum);
+            } else {
+                st_volatile(lb + lt, kLbAgg64 | tile_sum);
+                const unsigned long long excl = lookback64(lb, lt, g);
+                st_volatile(lb + lt, kLbInc64 | (excl + tile_sum));
+            }
+            atomicAdd(&g.fs->qo_total, tile_sum);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_init_expand(Batch* bt) {
+    __shared__ unsigned long long red[kThreads / 32];
+    __shared__ int bnd[kCellTile + 1];  // bnd[0] = first slot of the tile, bnd[1+c] = end of cell c
+    const int total = batch_total(bt, kStInitExpand);
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const int gi = grid_of_tile(bt, kStInitExpand, t);
+        const GridDesc& g = bt->g[gi];
+        const int lt = t - bt->prefix[gi][kStInitExpand];
+        const unsigned long long* lb = g.lb_cell + g.tiles[kStCell];
+        const unsigned long long T = g.fs->qo_total;
+        const bool uniform = (T == 0ull);
+        const int base = lt * kCellTile;
+        unsigned long long q[kCellIpt];
+        unsigned long long v = 0ull;
+        for (int j = 0; j < kCellIpt; ++j) {
+            const int k = base + threadIdx.x * kCellIpt + j;
+            q[j] = (k < g.C) ? (uniform ? 1ull : quantize(g.meas_src[k].occ_mass, g.q_shift)) : 0ull;
+            v += q[j];
+        }
+        unsigned long long tile_sum;
+        unsigned long long pre = block_excl_scan_u64(v, red, &tile_sum);
+        unsigned long long tile_excl = 0ull;
+        if (uniform) tile_excl = (unsigned long long)base;
+        else if (lt > 0) tile_excl = ld_volatile(lb + lt - 1) & kLbVal64;
+        const unsigned long long TT = uniform ? (unsigned long long)g.C : T;
+        if (threadIdx.x == 0) bnd[0] = alloc_boundary(tile_excl, TT, g.N);
+        unsigned long long acc = tile_excl + pre;
+        for (int j = 0; j < kCellIpt; ++j) {
+            acc += q[j];
+            bnd[1 + threadIdx.x * kCellIpt + j] = alloc_boundary(acc, TT, g.N);
+        }
+        __syncthreads();
+        const int ncell = min(kCellTile, g.C - base);
+        const int lo = bnd[0], hi = bnd[ncell];
+        const float vmax = g.init_max_vel;
+        const float span = __fsub_rn(vmax, -vmax);
+        for (int s = lo + threadIdx.x; s < hi; s += kThreads) {
+            int a = 0, b = ncell - 1;  // first cell c with bnd[1+c] > s
+            while (a < b) {
+                const int m = (a + b) >> 1;
+                if (bnd[1 + m] > s) b = m; else a = m + 1;
+            }
+            const int k = base + a;
+            float2 u;
+            if (g.rp_init) {
+                u = g.rp_init[s];
+            } else {
+                const U4 r = draw_block(g, (uint32_t)s, 0u, kDrawInit);
+                u = make_float2(u01_open0(r.x), u01_open0(r.y));
+            }
+            float4 st;
+            st.x = __fadd_rn((float)(k % g.gs), 0.5f);
+            st.y = __fadd_rn((float)(k / g.gs), 0.5f);
+            st.z = __fmaf_rn(span, __fsub_rn(1.0f, u.x), -vmax);
+            st.w = __fmaf_rn(span, __fsub_rn(1.0f, u.y), -vmax);
+            g.P_state[s] = st;
+            g.P_key[s] = (uint32_t)k;
+        }
+        if (lt == 0 && threadIdx.x == 0) g.fs->w_res = __fdiv_rn(1.0f, (float)g.N);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Stand-alone ego shift (the stage call; the update fuses it into predict and cells):
+// particles x -= x_move (ego_motion_compensation.cu:16-23) and the cell records moved by
+// (x_move, y_move) with the strict 0 < x,y bounds of ego_motion_compensation.cu:38.
+// ---------------------------------------------------------------------------------------
+__global__ void k_shift_particles(float4* st, int n, float fx, float fy) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 s = st[i];
+        s.x = __fsub_rn(s.x, fx);
+        s.y = __fsub_rn(s.y, fy);
+        st[i] = s;
+    }
+}
+
+__global__ void k_shift_cells(dogm_grid_cell* cells, const dogm_grid_cell* old_cells, float* free_new,
+                              const float* free_old, int gs, int xm, int ym) {
+    const int C = gs * gs;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < C; k += gridDim.x * blockDim.x) {
+        const int x = k % gs, y = k / gs;
+        const int nx = x + xm, ny = y + ym;
+        const bool ok = nx > 0 && nx < gs && ny > 0 && ny < gs;
+        dogm_grid_cell c;
+        float f = 0.0f;
+        if (ok) {
+            c = old_cells[nx + gs * ny];
+            f = free_old[nx + gs * ny];
+        } else {
+            memset(&c, 0, sizeof(c));
+        }
+        cells[k] = c;
+        free_new[k] = f;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Philox draw export: exactly the numbers the kernels above draw at `iteration`.
+// ---------------------------------------------------------------------------------------
+__global__ void k_draws(GridDesc g, uint32_t frame, float2* init_u, float4* predict_z, float2* birth_z,
+                        unsigned long long* resample_r) {
+    const int stride = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = tid; i < g.N; i += stride) {
+        if (init_u) {
+            const U4 r = draw_block(g, (uint32_t)i, 0u, kDrawInit);
+            init_u[i] = make_float2(u01_open0(r.x), u01_open0(r.y));
+        }
+        if (predict_z) {
+            const U4 r = draw_block(g, (uint32_t)i, frame, kDrawPredict);
+            const float2 a = box_muller(r.x, r.y);
+            const float2 b = box_muller(r.z, r.w);
+            predict_z[i] = make_float4(a.x, a.y, b.x, b.y);
+        }
+    }
+    if (birth_z)
+        for (int i = tid; i < g.B; i += stride) {
+            const U4 r = draw_block(g, (uint32_t)i, frame, kDrawBirth);
+            birth_z[i] = box_muller(r.x, r.y);
+        }
+    if (resample_r && tid == 0) {
+        const U4 r = draw_block(g, 0u, frame, kDrawResample);
+        *resample_r = ((unsigned long long)r.x << 32) | r.y;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------------------
+cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCfg& cfg) {
+    (void)n_grids;
+    k_frame_begin<<<cfg.num_sms * 2, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg) {
+    k_predict<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), stage_mode);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg) {
+    k_init_scan<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_init_expand<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shift_stage(const GridDesc& g, int x_move, int y_move, const LaunchCfg& cfg) {
+    k_shift_particles<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(g.P_state, g.N, (float)x_move, (float)y_move);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    dogm_grid_cell* old_cells = nullptr;
+    e = cudaMallocAsync((void**)&old_cells, sizeof(dogm_grid_cell) * (size_t)g.C, cfg.stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(old_cells, g.cells, sizeof(dogm_grid_cell) * (size_t)g.C, cudaMemcpyDeviceToDevice,
+                        cfg.stream);
+    if (e != cudaSuccess) return e;
+    k_shift_cells<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(g.cells, old_cells, g.free_new, g.free_old, g.gs,
+                                                                 x_move, y_move);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaFreeAsync(old_cells, cfg.stream);
+}
+
+cudaError_t launch_draws(const GridDesc& g, int iteration, float2* init_u, float4* predict_z, float2* birth_z,
+                         unsigned long long* resample_r, const LaunchCfg& cfg) {
+    k_draws<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(g, (uint32_t)iteration, init_u, predict_z, birth_z,
+                                                           resample_r);
+    return cudaGetLastError();
+}
+
+}  // namespace dogm_gb300

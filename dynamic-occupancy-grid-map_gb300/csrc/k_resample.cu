@@ -1,0 +1,151 @@
+// Resampling: one pass over the joint particle array [persistent (sorted) | newborn].
+// Replaces the joint concatenation, float scan, random draws, float sort, lower_bound and
+// gather of dogm.cu:386-423 / resampling.cu:17-68.  Joint weights are quantised to
+// 2^-q_shift and scanned exactly (decoupled look-back, integer, order-independent), and
+// systematic resampling assigns output slot i to the joint particle j with
+// A[j-1]*N <= i*T + U < A[j]*N, so each particle writes its own copies directly.
+// The new common weight is T / N (dogm.cu:417).
+#include "dogm_device.cuh"
+
+namespace dogm_gb300 {
+
+struct ResSmem {
+    float4 st[kResTile];
+    uint32_t kw[kResTile];
+    int hi[kResTile];
+    unsigned long long red[kThreads / 32];
+    unsigned long long excl;
+    int slot;
+};
+
+__global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ResSmem& sm = *reinterpret_cast<ResSmem*>(smem_raw);
+    const int total = batch_total(bt, kStResample);
+    for (;;) {
+        const int t = claim_tile(bt, kStResample, &sm.slot);
+        if (t >= total) break;
+        const int gi = grid_of_tile(bt, kStResample, t);
+        const GridDesc& g = bt->g[gi];
+        const int lt = t - bt->prefix[gi][kStResample];
+        const int base = lt * kResTile;
+        const int N = g.N;
+        const int M = N + g.fs->n_birth;
+        const unsigned long long T = g.fs->joint_total;
+        unsigned long long r64;
+        if (g.rp_resample) {
+            r64 = *g.rp_resample;
+        } else {
+            const U4 r = draw_block(g, 0u, g.frame, kDrawResample);
+            r64 = ((unsigned long long)r.x << 32) | r.y;
+        }
+        const unsigned long long U = __umul64hi(r64, T);  // floor(u * T), u = r64 / 2^64
+
+        unsigned long long q[kResIpt];
+        unsigned long long v = 0ull;
+#pragma unroll
+        for (int r = 0; r < kResIpt; ++r) {
+            const int j = threadIdx.x * kResIpt + r;
+            const int p = base + j;
+            float w = 0.0f;
+            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+            uint32_t kw = 0u;
+            if (p < N) {
+                kw = g.S_key[p];
+                s = g.S_state[p];
+                w = (kw & kOutBit) ? 0.0f : g.w_cell[kw & kCellMask];
+            } else if (p < M) {
+                const int b = p - N;
+                kw = g.B_key[b];
+                s = g.B_state[b];
+                w = g.B_w[b];
+            }
+            q[r] = (p < M) ? quantize(w, g.q_shift) : 0ull;
+            v += q[r];
+            sm.st[j] = s;
+            sm.kw[j] = kw & ~kOutBit;
+        }
+        unsigned long long tile_sum;
+        const unsigned long long pre = block_excl_scan_u64(v, sm.red, &tile_sum);
+        if (threadIdx.x == 0) {
+            unsigned long long* lb = g.lb_res;
+            unsigned long long excl = 0ull;
+            if (lt == 0) {
+                st_volatile(lb, kLbInc64 | tile_sum);
+            } else {
+                st_volatile(lb + lt, kLbAgg64 | tile_sum);
+                excl = lookback64(lb, lt, g);
+                st_volatile(lb + lt, kLbInc64 | (excl + tile_sum));
+            }
+            sm.excl = excl;
+        }
+        __syncthreads();
+        const unsigned long long tile_excl = sm.excl;
+        unsigned long long acc = tile_excl + pre;
+#pragma unroll
+        for (int r = 0; r < kResIpt; ++r) {
+            const int j = threadIdx.x * kResIpt + r;
+            acc += q[r];
+            sm.hi[j] = comb_count(acc, T, U, N);
+        }
+        __syncthreads();
+        const int lo = (base == 0) ? 0 : comb_count(tile_excl, T, U, N);
+        const int hi = sm.hi[kResTile - 1];
+        for (int s = lo + threadIdx.x; s < hi; s += kThreads) {
+            int a = 0, b = kResTile - 1;  // first item with hi > s
+            while (a < b) {
+                const int m = (a + b) >> 1;
+                if (sm.hi[m] > s) b = m; else a = m + 1;
+            }
+            g.P_state[s] = sm.st[a];
+            g.P_key[s] = sm.kw[a];
+            if (g.dbg_src) g.dbg_src[s] = base + a;
+        }
+        if (lt == 0 && threadIdx.x == 0) {
+            const float jf = ldexpf(__ull2float_rn(T), -g.q_shift);
+            g.fs->w_res = __fdiv_rn(jf, (float)N);
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t prepare_kernels() {
+    return cudaFuncSetAttribute(k_resample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ResSmem));
+}
+
+cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg) {
+    const int smem = (int)sizeof(ResSmem);
+    k_resample<<<cfg.num_sms * 2, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// Multinomial index search of the reference (resampling.cu:34-47): optional clamp of the
+// last accumulator to the largest query, then lower_bound of every sorted query.
+// ---------------------------------------------------------------------------------------
+__global__ void k_lower_bound(const float* __restrict__ acc, int n, const float* __restrict__ qv, int nq,
+                              int* __restrict__ out, int clamp_last) {
+    const float qmax = qv[nq - 1];
+    const float last = acc[n - 1];
+    const float last_eff = (clamp_last && last != qmax) ? qmax : last;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nq; i += gridDim.x * blockDim.x) {
+        const float x = qv[i];
+        int a = 0, b = n;  // first index with acc >= x
+        while (a < b) {
+            const int m = (a + b) >> 1;
+            const float am = (m == n - 1) ? last_eff : acc[m];
+            if (am < x) a = m + 1; else b = m;
+        }
+        out[i] = a;
+    }
+}
+
+cudaError_t launch_lower_bound(const float* accum, int n_accum, const float* q, int n_q, int* out, int clamp_last,
+                               cudaStream_t s) {
+    if (n_q <= 0) return cudaSuccess;
+    k_lower_bound<<<(n_q + 255) / 256 < 4096 ? (n_q + 255) / 256 : 4096, 256, 0, s>>>(accum, n_accum, q, n_q, out,
+                                                                                  clamp_last);
+    return cudaGetLastError();
+}
+
+}  // namespace dogm_gb300

@@ -1,0 +1,837 @@
+// Host runtime behind the C ABI (include/dogm_gb300.h): handle lifetime, pose bookkeeping,
+// batch upload, the per-frame launch sequence and its CUDA graph, readback and test hooks.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "dogm_internal.h"
+
+using namespace dogm_gb300;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+dogm_status fail(dogm_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+#define DOGM_CUDA(call)                                                                               \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail(e_ == cudaErrorMemoryAllocation ? DOGM_ERR_OUT_OF_MEMORY : DOGM_ERR_CUDA,     \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                          \
+    } while (0)
+
+int bitlen(unsigned long long v) {
+    int b = 0;
+    while (v) { ++b; v >>= 1; }
+    return b;
+}
+
+int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// One launch context: a device copy of a Batch, its pinned host mirror and the CUDA graphs
+// of the steady-state frame, keyed by batch size (the upload size is fixed in a graph).
+struct Ctx {
+    int device = -1;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    Batch* d_batch = nullptr;
+    Batch* h_batch = nullptr;            // pinned
+    unsigned int* h_status = nullptr;    // pinned copy of d_batch->status
+    std::map<int, cudaGraphExec_t> graphs;
+
+    ~Ctx() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        if (d_batch) cudaFree(d_batch);
+        if (h_batch) cudaFreeHost(h_batch);
+        if (h_status) cudaFreeHost(h_status);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+};
+
+dogm_status ctx_init(Ctx& c, int device) {
+    c.device = device;
+    DOGM_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
+    DOGM_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    c.own_stream = true;
+    DOGM_CUDA(cudaMalloc(&c.d_batch, sizeof(Batch)));
+    DOGM_CUDA(cudaMemset(c.d_batch, 0, sizeof(Batch)));
+    DOGM_CUDA(cudaMallocHost(&c.h_batch, sizeof(Batch)));
+    std::memset(c.h_batch, 0, sizeof(Batch));
+    DOGM_CUDA(cudaMallocHost(&c.h_status, sizeof(unsigned int)));
+    *c.h_status = 0;
+    return DOGM_OK;
+}
+
+}  // namespace
+
+struct dogm_handle {
+    int device = 0;
+    dogm_params params{};
+    dogm_options opt{};
+    int gs = 0, N = 0, B = 0, C = 0;
+    bool first_pose_received = false, first_measurement_received = false;
+    float position_x = 0.f, position_y = 0.f, yaw = 0.f;
+    int iteration = 0;
+    bool need_clear = true;
+    int last_launches = 0;
+    GridDesc desc{};                     // persistent pointers + sizes; per-frame fields set per call
+    std::vector<void*> allocations;
+    Ctx ctx;
+    // replay and debug buffers
+    float2* rp_init = nullptr;
+    float4* rp_predict = nullptr;
+    float2* rp_birth = nullptr;
+    unsigned long long* rp_resample = nullptr;
+    bool debug = false;
+};
+
+namespace {
+
+template <class T>
+dogm_status dalloc(dogm_handle* h, T** p, size_t count) {
+    void* q = nullptr;
+    const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(DOGM_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(bytes) + " B failed");
+    e = cudaMemset(q, 0, bytes);
+    if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, cudaGetErrorString(e));
+    h->allocations.push_back(q);
+    *p = static_cast<T*>(q);
+    return DOGM_OK;
+}
+
+struct Sizes {
+    int gs, N, B, C, key_bits, sort_tiles, seg_tiles, cell_tiles, res_tiles, pred_tiles;
+};
+
+dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
+    if (!(p.size > 0.f) || !(p.resolution > 0.f)) return fail(DOGM_ERR_INVALID_ARGUMENT, "size/resolution must be > 0");
+    s.gs = static_cast<int>(p.size / p.resolution);  // dogm.cu:34
+    if (s.gs < 1) return fail(DOGM_ERR_INVALID_ARGUMENT, "grid_size < 1");
+    s.C = s.gs * s.gs;
+    s.key_bits = std::max(1, bitlen((unsigned long long)(s.C - 1)));
+    if (s.key_bits > kMaxKeyBits)
+        return fail(DOGM_ERR_UNSUPPORTED, "grid_size " + std::to_string(s.gs) + " > 2048 is not supported");
+    s.N = p.particle_count;
+    s.B = p.new_born_particle_count;
+    if (s.N < 1 || s.N > kMaxParticles) return fail(DOGM_ERR_UNSUPPORTED, "particle_count must be in [1, 2^24)");
+    if (s.B < 0 || s.B > kMaxParticles) return fail(DOGM_ERR_UNSUPPORTED, "new_born_particle_count must be in [0, 2^24)");
+    s.pred_tiles = div_up(s.N, kPredictTile);
+    s.sort_tiles = div_up(s.N, kSortTile);
+    s.seg_tiles = div_up(s.N, kSegTile);
+    s.cell_tiles = div_up(s.C, kCellTile);
+    s.res_tiles = div_up((long long)s.N + s.B, kResTile);
+    return DOGM_OK;
+}
+
+void set_tiles(GridDesc& g, const Sizes& s) {
+    for (int i = 0; i < kNumStages; ++i) g.tiles[i] = 0;
+    g.tiles[kStPredict] = s.pred_tiles;
+    g.tiles[kStSort0] = s.sort_tiles;
+    g.tiles[kStSort1] = s.sort_tiles;
+    g.tiles[kStSeg] = s.seg_tiles;
+    g.tiles[kStCell] = s.cell_tiles;
+    g.tiles[kStBirth] = s.cell_tiles;
+    g.tiles[kStResample] = s.res_tiles;
+    g.tiles[kStInitScan] = s.cell_tiles;
+    g.tiles[kStInitExpand] = s.cell_tiles;
+    g.sort_tiles = s.sort_tiles;
+}
+
+// Fills the per-frame fields of h->desc.  Pose bookkeeping follows DOGM::updatePose
+// (dogm/src/dogm.cu:161-203): the first pose is stored; later poses shift the grid only
+// when |dx| or |dy| exceeds one cell, by -int(d / resolution) cells, dropping the
+// remainder and ignoring yaw.
+void pose_update(dogm_handle* h, float new_x, float new_y, float new_yaw, int* shifted, int* xm, int* ym) {
+    *shifted = 0;
+    *xm = *ym = 0;
+    if (!h->first_pose_received) {
+        h->position_x = new_x;
+        h->position_y = new_y;
+        h->yaw = new_yaw;
+        h->first_pose_received = true;
+        return;
+    }
+    const float x_diff = new_x - h->position_x;
+    const float y_diff = new_y - h->position_y;
+    const float res = h->params.resolution;
+    if (std::fabs(x_diff) > res || std::fabs(y_diff) > res) {
+        *xm = -static_cast<int>(x_diff / res);
+        *ym = -static_cast<int>(y_diff / res);
+        *shifted = 1;
+        h->position_x = new_x;
+        h->position_y = new_y;
+        h->yaw = new_yaw;
+    }
+}
+
+void fill_frame(dogm_handle* h, float dt, int shifted, int xm, int ym, const dogm_measurement_cell* meas_src,
+                int copy_meas) {
+    GridDesc& g = h->desc;
+    g.dt = dt;
+    g.alpha = std::pow(h->params.freespace_discount, dt);  // float pow, as dogm.cu:291
+    g.shifted = shifted;
+    g.shift_x = xm;
+    g.shift_y = ym;
+    g.meas_src = meas_src;
+    g.copy_meas = copy_meas;
+    g.frame = (uint32_t)h->iteration;
+    g.epoch = (uint32_t)(h->iteration & 63);
+    g.clear_lookback = (h->need_clear || (h->iteration & 63) == 0) ? 1 : 0;
+    g.rp_init = h->rp_init;
+    g.rp_predict = h->rp_predict;
+    g.rp_birth = h->rp_birth;
+    g.rp_resample = h->rp_resample;
+}
+
+// Writes n grid descriptors and the per-stage tile prefix into the pinned mirror.
+// init_mask[i] != 0 schedules the first-frame initialisation of grid i.
+void build_batch(Ctx& c, dogm_handle* const* hs, int n, const std::vector<int>& init_mask) {
+    Batch& b = *c.h_batch;
+    b.n_grids = n;
+    b.status = 0u;
+    for (int s = 0; s < kNumStages; ++s) b.counters[s] = 0u;
+    for (int s = 0; s < kNumStages; ++s) b.prefix[0][s] = 0;
+    for (int i = 0; i < n; ++i) {
+        b.g[i] = hs[i]->desc;
+        b.g[i].status_out = &c.d_batch->status;
+        for (int s = 0; s < kNumStages; ++s) {
+            int tiles = b.g[i].tiles[s];
+            if ((s == kStInitScan || s == kStInitExpand) && !init_mask[i]) tiles = 0;
+            b.prefix[i + 1][s] = b.prefix[i][s] + tiles;
+        }
+    }
+}
+
+size_t batch_head_bytes(int n) { return offsetof(Batch, prefix) + sizeof(int) * kNumStages * (size_t)(n + 1); }
+size_t batch_desc_bytes(int n) { return sizeof(GridDesc) * (size_t)n; }
+
+cudaError_t upload_batch(Ctx& c, int n) {
+    cudaError_t e = cudaMemcpyAsync(c.d_batch, c.h_batch, batch_head_bytes(n), cudaMemcpyHostToDevice, c.stream);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(&c.d_batch->g[0], &c.h_batch->g[0], batch_desc_bytes(n), cudaMemcpyHostToDevice, c.stream);
+}
+
+// The steady-state frame: 8 kernels.
+cudaError_t frame_kernels(Ctx& c) {
+    LaunchCfg cfg{c.num_sms, c.stream};
+    cudaError_t e;
+    if ((e = launch_frame_begin(c.d_batch, 0, cfg)) != cudaSuccess) return e;
+    if ((e = launch_predict(c.d_batch, 0, cfg)) != cudaSuccess) return e;
+    if ((e = launch_sort(c.d_batch, cfg)) != cudaSuccess) return e;
+    if ((e = launch_segments(c.d_batch, cfg)) != cudaSuccess) return e;
+    if ((e = launch_cells(c.d_batch, cfg)) != cudaSuccess) return e;
+    if ((e = launch_newborn(c.d_batch, cfg)) != cudaSuccess) return e;
+    return launch_resample(c.d_batch, cfg);
+}
+
+dogm_status run_frame(Ctx& c, int n, bool any_init, bool use_graph, int* launches) {
+    cudaError_t e;
+    if (any_init) {
+        // first frame of at least one grid: plain launches (init sits between begin and predict)
+        LaunchCfg cfg{c.num_sms, c.stream};
+        DOGM_CUDA(upload_batch(c, n));
+        DOGM_CUDA(launch_frame_begin(c.d_batch, 0, cfg));
+        DOGM_CUDA(launch_init_particles(c.d_batch, cfg));
+        DOGM_CUDA(launch_predict(c.d_batch, 0, cfg));
+        DOGM_CUDA(launch_sort(c.d_batch, cfg));
+        DOGM_CUDA(launch_segments(c.d_batch, cfg));
+        DOGM_CUDA(launch_cells(c.d_batch, cfg));
+        DOGM_CUDA(launch_newborn(c.d_batch, cfg));
+        DOGM_CUDA(launch_resample(c.d_batch, cfg));
+        DOGM_CUDA(cudaMemcpyAsync(c.h_status, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                  c.stream));
+        *launches = kLaunchesPerFrame + kLaunchesInit;
+        return DOGM_OK;
+    }
+    if (!use_graph) {
+        DOGM_CUDA(upload_batch(c, n));
+        DOGM_CUDA(frame_kernels(c));
+        DOGM_CUDA(cudaMemcpyAsync(c.h_status, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                  c.stream));
+        *launches = kLaunchesPerFrame;
+        return DOGM_OK;
+    }
+    auto it = c.graphs.find(n);
+    if (it == c.graphs.end()) {
+        cudaGraph_t graph;
+        DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        e = upload_batch(c, n);
+        if (e == cudaSuccess) e = frame_kernels(c);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(c.h_status, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                c.stream);
+        cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
+        if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        if (e2 != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
+        cudaGraphExec_t exec;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        it = c.graphs.emplace(n, exec).first;
+    }
+    DOGM_CUDA(cudaGraphLaunch(it->second, c.stream));
+    *launches = kLaunchesPerFrame;
+    return DOGM_OK;
+}
+
+dogm_status finish_frame(Ctx& c, dogm_handle* const* hs, int n) {
+    DOGM_CUDA(cudaStreamSynchronize(c.stream));
+    const unsigned int st = *c.h_status;
+    if (st & kStatusTimeout) {
+        for (int i = 0; i < n; ++i) hs[i]->need_clear = true;
+        return fail(DOGM_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up (look-back predecessor never published)");
+    }
+    if (st & kStatusBounds) {
+        for (int i = 0; i < n; ++i) hs[i]->need_clear = true;
+        return fail(DOGM_ERR_CUDA, "a device index check refused an out-of-range write (inconsistent histogram)");
+    }
+    return DOGM_OK;
+}
+
+// Per-frame host bookkeeping after the launches were queued.
+void advance(dogm_handle* h) {
+    std::swap(h->desc.free_old, h->desc.free_new);
+    h->iteration += 1;
+    h->need_clear = false;
+    h->first_measurement_received = true;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// Shared batch contexts, one per device.
+std::mutex g_ctx_mu;
+std::map<int, Ctx*> g_batch_ctx;
+
+template <class T>
+dogm_status upload_replay(T** dst, const void* src, size_t bytes) {
+    if (!src) {
+        if (*dst) cudaFree(*dst);
+        *dst = nullptr;
+        return DOGM_OK;
+    }
+    if (!*dst) DOGM_CUDA(cudaMalloc((void**)dst, bytes));
+    DOGM_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+    return DOGM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dogm_abi_version(void) { return DOGM_ABI_VERSION; }
+const char* dogm_last_error(void) { return g_last_error.c_str(); }
+
+const char* dogm_status_string(dogm_status s) {
+    switch (s) {
+        case DOGM_OK: return "ok";
+        case DOGM_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case DOGM_ERR_OUT_OF_MEMORY: return "out of memory";
+        case DOGM_ERR_CUDA: return "CUDA error";
+        case DOGM_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+        case DOGM_ERR_NOT_READY: return "not ready";
+        case DOGM_ERR_UNSUPPORTED: return "unsupported";
+        case DOGM_ERR_BUDGET: return "over budget";
+    }
+    return "unknown";
+}
+
+dogm_status dogm_default_options(dogm_options* opt) {
+    if (!opt) return fail(DOGM_ERR_INVALID_ARGUMENT, "opt is NULL");
+    opt->seed = 123456ull;
+    opt->stream_id = 0u;
+    opt->resample_mode = DOGM_RESAMPLE_SYSTEMATIC;
+    opt->sync_each_update = 1;
+    return DOGM_OK;
+}
+
+size_t dogm_state_bytes(const dogm_params* p) {
+    if (!p) return 0;
+    Sizes s;
+    if (derive_sizes(*p, s) != DOGM_OK) return 0;
+    const size_t N = (size_t)s.N, B = (size_t)s.B, C = (size_t)s.C;
+    size_t b = 0;
+    b += N * (16 + 4) + N * (4 + 4) + N * (16 + 4);    // P, T, S particles
+    b += B * (16 + 4 + 4);                            // newborns
+    b += C * (sizeof(dogm_grid_cell) + 2 * sizeof(dogm_measurement_cell) / 2 * 2 / 2 + 4 * 2 + 32 + 4 + 4) + C / 8;
+    b += 2 * kSortMaxBins * 4 + (size_t)2 * s.sort_tiles * kSortMaxBins * 4;
+    b += (size_t)s.seg_tiles * 2 * sizeof(SegSums) + (size_t)s.cell_tiles * 16 + (size_t)s.res_tiles * 8;
+    b += sizeof(Batch);
+    return b;
+}
+
+dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm_handle** out) {
+    if (!params || !out) return fail(DOGM_ERR_INVALID_ARGUMENT, "params/out is NULL");
+    *out = nullptr;
+    Sizes s;
+    dogm_status st = derive_sizes(*params, s);
+    if (st != DOGM_OK) return st;
+    dogm_handle* h = new dogm_handle();
+    h->params = *params;
+    if (opt) h->opt = *opt; else dogm_default_options(&h->opt);
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) { delete h; return fail(DOGM_ERR_CUDA, cudaGetErrorString(e)); }
+    h->gs = s.gs; h->N = s.N; h->B = s.B; h->C = s.C;
+    auto cleanup = [&](dogm_status s2) { dogm_destroy(h); return s2; };
+    if ((st = ctx_init(h->ctx, h->device)) != DOGM_OK) return cleanup(st);
+    if (prepare_kernels() != cudaSuccess) return cleanup(fail(DOGM_ERR_CUDA, "kernel attribute setup failed"));
+
+    GridDesc& g = h->desc;
+    g.N = s.N; g.B = s.B; g.C = s.C; g.gs = s.gs;
+    g.d0_bits = (s.key_bits + 1) / 2;
+    g.d1_bits = s.key_bits - g.d0_bits;
+    g.q_shift = 61 - bitlen((unsigned long long)s.C);
+    g.p_S = params->persistence_prob;
+    g.sigma_pos = params->stddev_process_noise_position;
+    g.sigma_vel = params->stddev_process_noise_velocity;
+    g.p_B = params->birth_prob;
+    g.sigma_birth = params->stddev_velocity;
+    g.init_max_vel = params->init_max_velocity;
+    g.stream_id = h->opt.stream_id;
+    g.seed_lo = (uint32_t)(h->opt.seed & 0xffffffffull);
+    g.seed_hi = (uint32_t)(h->opt.seed >> 32);
+    set_tiles(g, s);
+
+#define ALLOC(ptr, n) if ((st = dalloc(h, &(ptr), (n))) != DOGM_OK) return cleanup(st)
+    ALLOC(g.P_state, s.N); ALLOC(g.P_key, s.N);
+    ALLOC(g.T_key, s.N); ALLOC(g.T_idx, s.N);
+    ALLOC(g.S_state, s.N); ALLOC(g.S_key, s.N);
+    ALLOC(g.B_state, s.B); ALLOC(g.B_key, s.B); ALLOC(g.B_w, s.B);
+    ALLOC(g.cells, s.C);
+    dogm_measurement_cell* meas_own = nullptr;
+    ALLOC(meas_own, s.C);
+    g.meas_own = meas_own;
+    g.meas_src = meas_own;
+    float* fa = nullptr; float* fb = nullptr;
+    ALLOC(fa, s.C); ALLOC(fb, s.C);
+    g.free_old = fa; g.free_new = fb;
+    ALLOC(g.seg_i, s.C); ALLOC(g.seg_f, s.C);
+    ALLOC(g.rho_b, s.C); ALLOC(g.w_cell, s.C);
+    ALLOC(g.occ_bits, (s.C + 31) / 32);
+    ALLOC(g.hist, 2 * kSortMaxBins);
+    ALLOC(g.lb_sort, (size_t)2 * s.sort_tiles * kSortMaxBins);
+    ALLOC(g.seg_head, s.seg_tiles); ALLOC(g.seg_tail, s.seg_tiles);
+    ALLOC(g.lb_cell, 2 * (size_t)s.cell_tiles);
+    ALLOC(g.lb_res, s.res_tiles);
+    ALLOC(g.fs, 1);
+#undef ALLOC
+    // measurement cells start as in initGridCellsKernel (init.cu:65-80): no evidence,
+    // likelihood 1, p_A 1; cells start with zero masses and empty ranges.
+    {
+        std::vector<dogm_measurement_cell> m((size_t)s.C, dogm_measurement_cell{0.f, 0.f, 1.f, 1.f});
+        e = cudaMemcpy(meas_own, m.data(), sizeof(dogm_measurement_cell) * m.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cleanup(fail(DOGM_ERR_CUDA, cudaGetErrorString(e)));
+        std::vector<dogm_grid_cell> c((size_t)s.C);
+        for (auto& x : c) { std::memset(&x, 0, sizeof(x)); x.start_idx = -1; x.end_idx = -1; }
+        e = cudaMemcpy(g.cells, c.data(), sizeof(dogm_grid_cell) * c.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cleanup(fail(DOGM_ERR_CUDA, cudaGetErrorString(e)));
+        FrameState fs{};
+        fs.w_res = 0.0f;
+        e = cudaMemcpy(g.fs, &fs, sizeof(fs), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cleanup(fail(DOGM_ERR_CUDA, cudaGetErrorString(e)));
+    }
+    *out = h;
+    return DOGM_OK;
+}
+
+dogm_status dogm_destroy(dogm_handle* h) {
+    if (!h) return DOGM_OK;
+    DeviceGuard dg(h->device);
+    cudaDeviceSynchronize();
+    for (void* p : h->allocations) cudaFree(p);
+    for (void* p : {(void*)h->rp_init, (void*)h->rp_predict, (void*)h->rp_birth, (void*)h->rp_resample})
+        if (p) cudaFree(p);
+    delete h;
+    return DOGM_OK;
+}
+
+static dogm_status prepare_measurement(dogm_handle* h, const dogm_measurement_cell* meas, int device,
+                                       cudaStream_t stream, const dogm_measurement_cell** src, int* copy) {
+    *src = h->desc.meas_own;
+    *copy = 0;
+    if (!meas) return DOGM_OK;  // keep the resident grid
+    if (device) {
+        *src = meas;
+        *copy = 1;
+        return DOGM_OK;
+    }
+    DOGM_CUDA(cudaMemcpyAsync(h->desc.meas_own, meas, sizeof(dogm_measurement_cell) * (size_t)h->C,
+                              cudaMemcpyHostToDevice, stream));
+    return DOGM_OK;
+}
+
+dogm_status dogm_update(dogm_handle* h, const dogm_measurement_cell* meas, float new_x, float new_y, float new_yaw,
+                        float dt, int device) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    DeviceGuard dg(h->device);
+    Ctx& c = h->ctx;
+    DOGM_CUDA(cudaStreamSynchronize(c.stream));  // the pinned batch mirror is reused
+    const dogm_measurement_cell* src;
+    int copy;
+    dogm_status st = prepare_measurement(h, meas, device, c.stream, &src, &copy);
+    if (st != DOGM_OK) return st;
+    const bool init = !h->first_measurement_received;
+    int shifted, xm, ym;
+    pose_update(h, new_x, new_y, new_yaw, &shifted, &xm, &ym);
+    fill_frame(h, dt, shifted, xm, ym, src, copy);
+    dogm_handle* hs[1] = {h};
+    std::vector<int> init_mask(1, init ? 1 : 0);
+    build_batch(c, hs, 1, init_mask);
+    h->desc.clear_lookback = 0;
+    st = run_frame(c, 1, init, true, &h->last_launches);
+    if (st != DOGM_OK) { h->need_clear = true; return st; }
+    advance(h);
+    if (h->opt.sync_each_update) return finish_frame(c, hs, 1);
+    return DOGM_OK;
+}
+
+dogm_status dogm_update_batch(dogm_handle* const* hs, int n, const dogm_measurement_cell* const* meas,
+                              const float* new_x, const float* new_y, const float* new_yaw, const float* dt,
+                              int device) {
+    if (!hs || n <= 0 || n > kMaxBatch || !new_x || !new_y || !new_yaw || !dt)
+        return fail(DOGM_ERR_INVALID_ARGUMENT, "bad batch arguments");
+    const int dev = hs[0]->device;
+    for (int i = 0; i < n; ++i) {
+        if (!hs[i] || hs[i]->device != dev) return fail(DOGM_ERR_INVALID_ARGUMENT, "all handles must share a device");
+        for (int j = 0; j < i; ++j)
+            if (hs[j] == hs[i]) return fail(DOGM_ERR_INVALID_ARGUMENT, "a handle appears twice in a batch");
+    }
+    DeviceGuard dg(dev);
+    Ctx* c;
+    {
+        std::lock_guard<std::mutex> lk(g_ctx_mu);
+        auto it = g_batch_ctx.find(dev);
+        if (it == g_batch_ctx.end()) {
+            c = new Ctx();
+            dogm_status st = ctx_init(*c, dev);
+            if (st != DOGM_OK) { delete c; return st; }
+            g_batch_ctx[dev] = c;
+        } else {
+            c = it->second;
+        }
+    }
+    DOGM_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<int> init_mask(n, 0);
+    bool any_init = false;
+    for (int i = 0; i < n; ++i) {
+        dogm_handle* h = hs[i];
+        DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+        const dogm_measurement_cell* src;
+        int copy;
+        dogm_status st = prepare_measurement(h, meas ? meas[i] : nullptr, device, c->stream, &src, &copy);
+        if (st != DOGM_OK) return st;
+        init_mask[i] = h->first_measurement_received ? 0 : 1;
+        any_init |= init_mask[i] != 0;
+        int shifted, xm, ym;
+        pose_update(h, new_x[i], new_y[i], new_yaw[i], &shifted, &xm, &ym);
+        fill_frame(h, dt[i], shifted, xm, ym, src, copy);
+    }
+    build_batch(*c, hs, n, init_mask);
+    int launches = 0;
+    dogm_status st = run_frame(*c, n, any_init, true, &launches);
+    if (st != DOGM_OK) {
+        for (int i = 0; i < n; ++i) hs[i]->need_clear = true;
+        return st;
+    }
+    for (int i = 0; i < n; ++i) {
+        advance(hs[i]);
+        hs[i]->last_launches = launches;
+    }
+    return finish_frame(*c, hs, n);
+}
+
+dogm_status dogm_synchronize(dogm_handle* h) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    DeviceGuard dg(h->device);
+    dogm_handle* hs[1] = {h};
+    return finish_frame(h->ctx, hs, 1);
+}
+
+dogm_status dogm_get_grid_cells(dogm_handle* h, dogm_grid_cell* host_out, size_t n) {
+    if (!h || !host_out) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n != (size_t)h->C) return fail(DOGM_ERR_INVALID_ARGUMENT, "n must equal grid_size^2");
+    DeviceGuard dg(h->device);
+    DOGM_CUDA(cudaMemcpyAsync(host_out, h->desc.cells, sizeof(dogm_grid_cell) * n, cudaMemcpyDeviceToHost,
+                              h->ctx.stream));
+    DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+    return DOGM_OK;
+}
+
+dogm_status dogm_get_grid_cells_device(dogm_handle* h, dogm_grid_cell* dev_out, size_t n) {
+    if (!h || !dev_out) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n != (size_t)h->C) return fail(DOGM_ERR_INVALID_ARGUMENT, "n must equal grid_size^2");
+    DeviceGuard dg(h->device);
+    DOGM_CUDA(cudaMemcpyAsync(dev_out, h->desc.cells, sizeof(dogm_grid_cell) * n, cudaMemcpyDeviceToDevice,
+                              h->ctx.stream));
+    DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+    return DOGM_OK;
+}
+
+dogm_status dogm_get_measurement_cells(dogm_handle* h, dogm_measurement_cell* host_out, size_t n) {
+    if (!h || !host_out) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n != (size_t)h->C) return fail(DOGM_ERR_INVALID_ARGUMENT, "n must equal grid_size^2");
+    DeviceGuard dg(h->device);
+    DOGM_CUDA(cudaMemcpyAsync(host_out, h->desc.meas_own, sizeof(dogm_measurement_cell) * n, cudaMemcpyDeviceToHost,
+                              h->ctx.stream));
+    DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+    return DOGM_OK;
+}
+
+dogm_status dogm_get_particles(dogm_handle* h, float* state, int* idx, float* weight, unsigned char* assoc, size_t n) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    if (n != (size_t)h->N) return fail(DOGM_ERR_INVALID_ARGUMENT, "n must equal particle_count");
+    DeviceGuard dg(h->device);
+    cudaStream_t s = h->ctx.stream;
+    std::vector<uint32_t> keys(n);
+    FrameState fs;
+    if (state) DOGM_CUDA(cudaMemcpyAsync(state, h->desc.P_state, 16 * n, cudaMemcpyDeviceToHost, s));
+    DOGM_CUDA(cudaMemcpyAsync(keys.data(), h->desc.P_key, 4 * n, cudaMemcpyDeviceToHost, s));
+    DOGM_CUDA(cudaMemcpyAsync(&fs, h->desc.fs, sizeof(fs), cudaMemcpyDeviceToHost, s));
+    DOGM_CUDA(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < n; ++i) {
+        if (idx) idx[i] = (int)(keys[i] & kCellMask);
+        if (assoc) assoc[i] = (keys[i] & kAssocBit) ? 1 : 0;
+        if (weight) weight[i] = (keys[i] & kOutBit) ? 0.0f : fs.w_res;
+    }
+    return DOGM_OK;
+}
+
+int dogm_get_grid_size(const dogm_handle* h) { return h ? h->gs : 0; }
+float dogm_get_resolution(const dogm_handle* h) { return h ? h->params.resolution : 0.f; }
+float dogm_get_position_x(const dogm_handle* h) { return h ? h->position_x : 0.f; }
+float dogm_get_position_y(const dogm_handle* h) { return h ? h->position_y : 0.f; }
+float dogm_get_yaw(const dogm_handle* h) { return h ? h->yaw : 0.f; }
+int dogm_get_iteration(const dogm_handle* h) { return h ? h->iteration : 0; }
+int dogm_get_particle_count(const dogm_handle* h) { return h ? h->N : 0; }
+int dogm_get_new_born_particle_count(const dogm_handle* h) { return h ? h->B : 0; }
+int dogm_last_launch_count(const dogm_handle* h) { return h ? h->last_launches : 0; }
+
+// ---- stage calls -----------------------------------------------------------------------
+
+dogm_status dogm_particle_prediction(dogm_handle* h, float dt) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    DeviceGuard dg(h->device);
+    Ctx& c = h->ctx;
+    DOGM_CUDA(cudaStreamSynchronize(c.stream));
+    fill_frame(h, dt, 0, 0, 0, h->desc.meas_own, 0);
+    dogm_handle* hs[1] = {h};
+    build_batch(c, hs, 1, std::vector<int>(1, 0));
+    DOGM_CUDA(upload_batch(c, 1));
+    LaunchCfg cfg{c.num_sms, c.stream};
+    DOGM_CUDA(launch_predict(c.d_batch, 1, cfg));
+    DOGM_CUDA(cudaStreamSynchronize(c.stream));
+    // the common weight becomes p_S * w (predict.cu:30); out-of-grid particles read as 0
+    FrameState fs;
+    DOGM_CUDA(cudaMemcpy(&fs, h->desc.fs, sizeof(fs), cudaMemcpyDeviceToHost));
+    fs.w_res = fs.w_res * h->params.persistence_prob;
+    DOGM_CUDA(cudaMemcpy(&h->desc.fs->w_res, &fs.w_res, sizeof(float), cudaMemcpyHostToDevice));
+    h->last_launches = 1;
+    return DOGM_OK;
+}
+
+dogm_status dogm_update_pose(dogm_handle* h, float new_x, float new_y, float new_yaw) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    DeviceGuard dg(h->device);
+    int shifted, xm, ym;
+    pose_update(h, new_x, new_y, new_yaw, &shifted, &xm, &ym);
+    if (!shifted) return DOGM_OK;
+    LaunchCfg cfg{h->ctx.num_sms, h->ctx.stream};
+    DOGM_CUDA(launch_shift_stage(h->desc, xm, ym, cfg));
+    DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+    std::swap(h->desc.free_old, h->desc.free_new);
+    return DOGM_OK;
+}
+
+dogm_status dogm_initialize_particles(dogm_handle* h) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    DeviceGuard dg(h->device);
+    Ctx& c = h->ctx;
+    DOGM_CUDA(cudaStreamSynchronize(c.stream));
+    fill_frame(h, 0.f, 0, 0, 0, h->desc.meas_own, 0);
+    dogm_handle* hs[1] = {h};
+    build_batch(c, hs, 1, std::vector<int>(1, 1));
+    DOGM_CUDA(upload_batch(c, 1));
+    LaunchCfg cfg{c.num_sms, c.stream};
+    DOGM_CUDA(launch_frame_begin(c.d_batch, 1, cfg));
+    DOGM_CUDA(launch_init_particles(c.d_batch, cfg));
+    DOGM_CUDA(cudaStreamSynchronize(c.stream));
+    h->first_measurement_received = true;
+    h->need_clear = true;
+    return DOGM_OK;
+}
+
+// ---- state injection, replay, debug ------------------------------------------------------
+
+dogm_status dogm_set_measurement_cells(dogm_handle* h, const dogm_measurement_cell* host_in, size_t n) {
+    if (!h || !host_in) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n != (size_t)h->C) return fail(DOGM_ERR_INVALID_ARGUMENT, "n must equal grid_size^2");
+    DeviceGuard dg(h->device);
+    DOGM_CUDA(cudaMemcpy(h->desc.meas_own, host_in, sizeof(dogm_measurement_cell) * n, cudaMemcpyHostToDevice));
+    return DOGM_OK;
+}
+
+dogm_status dogm_set_particles(dogm_handle* h, const float* state, const int* idx, const unsigned char* assoc,
+                               float weight, size_t n) {
+    if (!h || !state) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n != (size_t)h->N) return fail(DOGM_ERR_INVALID_ARGUMENT, "n must equal particle_count");
+    DeviceGuard dg(h->device);
+    std::vector<uint32_t> keys(n);
+    for (size_t i = 0; i < n; ++i)
+        keys[i] = (idx ? ((uint32_t)idx[i] & kCellMask) : 0u) | ((assoc && assoc[i]) ? kAssocBit : 0u);
+    DOGM_CUDA(cudaMemcpy(h->desc.P_state, state, 16 * n, cudaMemcpyHostToDevice));
+    DOGM_CUDA(cudaMemcpy(h->desc.P_key, keys.data(), 4 * n, cudaMemcpyHostToDevice));
+    DOGM_CUDA(cudaMemcpy(&h->desc.fs->w_res, &weight, sizeof(float), cudaMemcpyHostToDevice));
+    h->first_measurement_received = true;
+    return DOGM_OK;
+}
+
+dogm_status dogm_set_replay(dogm_handle* h, const float* init_u, const float* predict_z, const float* birth_z,
+                            const uint64_t* resample_r) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    DeviceGuard dg(h->device);
+    DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+    dogm_status st;
+    if ((st = upload_replay(&h->rp_init, init_u, 8 * (size_t)h->N)) != DOGM_OK) return st;
+    if ((st = upload_replay(&h->rp_predict, predict_z, 16 * (size_t)h->N)) != DOGM_OK) return st;
+    if ((st = upload_replay(&h->rp_birth, birth_z, 8 * (size_t)std::max(h->B, 1))) != DOGM_OK) return st;
+    if ((st = upload_replay(&h->rp_resample, resample_r, 8)) != DOGM_OK) return st;
+    return DOGM_OK;
+}
+
+dogm_status dogm_clear_replay(dogm_handle* h) { return dogm_set_replay(h, nullptr, nullptr, nullptr, nullptr); }
+
+dogm_status dogm_generate_draws(dogm_handle* h, int iteration, float* init_u, float* predict_z, float* birth_z,
+                                uint64_t* resample_r) {
+    if (!h || iteration < 0) return fail(DOGM_ERR_INVALID_ARGUMENT, "bad argument");
+    DeviceGuard dg(h->device);
+    cudaStream_t s = h->ctx.stream;
+    float2* di = nullptr; float4* dp = nullptr; float2* db = nullptr; unsigned long long* dr = nullptr;
+    if (init_u) DOGM_CUDA(cudaMalloc(&di, 8 * (size_t)h->N));
+    if (predict_z) DOGM_CUDA(cudaMalloc(&dp, 16 * (size_t)h->N));
+    if (birth_z && h->B > 0) DOGM_CUDA(cudaMalloc(&db, 8 * (size_t)h->B));
+    if (resample_r) DOGM_CUDA(cudaMalloc(&dr, 8));
+    LaunchCfg cfg{h->ctx.num_sms, s};
+    DOGM_CUDA(launch_draws(h->desc, iteration, di, dp, db, dr, cfg));
+    DOGM_CUDA(cudaStreamSynchronize(s));
+    if (di) DOGM_CUDA(cudaMemcpy(init_u, di, 8 * (size_t)h->N, cudaMemcpyDeviceToHost));
+    if (dp) DOGM_CUDA(cudaMemcpy(predict_z, dp, 16 * (size_t)h->N, cudaMemcpyDeviceToHost));
+    if (db) DOGM_CUDA(cudaMemcpy(birth_z, db, 8 * (size_t)h->B, cudaMemcpyDeviceToHost));
+    if (dr) DOGM_CUDA(cudaMemcpy(resample_r, dr, 8, cudaMemcpyDeviceToHost));
+    for (void* p : {(void*)di, (void*)dp, (void*)db, (void*)dr}) if (p) cudaFree(p);
+    return DOGM_OK;
+}
+
+dogm_status dogm_debug_enable(dogm_handle* h, int enable) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    DeviceGuard dg(h->device);
+    if (enable && !h->debug) {
+        dogm_status st;
+        if ((st = dalloc(h, &h->desc.dbg_perm, h->N)) != DOGM_OK) return st;
+        if ((st = dalloc(h, &h->desc.dbg_src, h->N)) != DOGM_OK) return st;
+        h->debug = true;
+    } else if (!enable) {
+        h->desc.dbg_perm = nullptr;
+        h->desc.dbg_src = nullptr;
+        h->debug = false;
+    }
+    return DOGM_OK;
+}
+
+dogm_status dogm_debug_export(dogm_handle* h, int* sorted_cell, float* sorted_state, int* sort_perm,
+                              float* birth_state, int* birth_cell, unsigned char* birth_assoc, float* birth_weight,
+                              int* resample_src, uint64_t* joint_total, int* q_shift, int* n_birth) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    DeviceGuard dg(h->device);
+    DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+    const size_t N = (size_t)h->N, B = (size_t)h->B;
+    if (sorted_cell) {
+        std::vector<uint32_t> k(N);
+        DOGM_CUDA(cudaMemcpy(k.data(), h->desc.S_key, 4 * N, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < N; ++i) sorted_cell[i] = (int)(k[i] & kCellMask);
+    }
+    if (sorted_state) DOGM_CUDA(cudaMemcpy(sorted_state, h->desc.S_state, 16 * N, cudaMemcpyDeviceToHost));
+    if (sort_perm) {
+        if (!h->debug) return fail(DOGM_ERR_NOT_READY, "enable debug before the update to export the permutation");
+        DOGM_CUDA(cudaMemcpy(sort_perm, h->desc.dbg_perm, 4 * N, cudaMemcpyDeviceToHost));
+    }
+    if (B > 0) {
+        if (birth_state) DOGM_CUDA(cudaMemcpy(birth_state, h->desc.B_state, 16 * B, cudaMemcpyDeviceToHost));
+        if (birth_weight) DOGM_CUDA(cudaMemcpy(birth_weight, h->desc.B_w, 4 * B, cudaMemcpyDeviceToHost));
+        if (birth_cell || birth_assoc) {
+            std::vector<uint32_t> k(B);
+            DOGM_CUDA(cudaMemcpy(k.data(), h->desc.B_key, 4 * B, cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < B; ++i) {
+                if (birth_cell) birth_cell[i] = (int)(k[i] & kCellMask);
+                if (birth_assoc) birth_assoc[i] = (k[i] & kAssocBit) ? 1 : 0;
+            }
+        }
+    }
+    if (resample_src) {
+        if (!h->debug) return fail(DOGM_ERR_NOT_READY, "enable debug before the update to export resample sources");
+        DOGM_CUDA(cudaMemcpy(resample_src, h->desc.dbg_src, 4 * N, cudaMemcpyDeviceToHost));
+    }
+    FrameState fs;
+    DOGM_CUDA(cudaMemcpy(&fs, h->desc.fs, sizeof(fs), cudaMemcpyDeviceToHost));
+    if (joint_total) *joint_total = fs.joint_total;
+    if (q_shift) *q_shift = h->desc.q_shift;
+    if (n_birth) *n_birth = fs.n_birth;
+    return DOGM_OK;
+}
+
+// ---- utilities ---------------------------------------------------------------------------
+
+dogm_status dogm_lower_bound_f32(const float* accum, int n_accum, const float* q, int n_q, int* out, int clamp_last,
+                                 void* stream) {
+    if (!accum || !q || !out || n_accum <= 0 || n_q < 0) return fail(DOGM_ERR_INVALID_ARGUMENT, "bad argument");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    DOGM_CUDA(launch_lower_bound(accum, n_accum, q, n_q, out, clamp_last, s));
+    DOGM_CUDA(cudaStreamSynchronize(s));
+    return DOGM_OK;
+}
+
+dogm_status dogm_host_alloc(void** ptr, size_t bytes) {
+    if (!ptr) return fail(DOGM_ERR_INVALID_ARGUMENT, "ptr is NULL");
+    DOGM_CUDA(cudaMallocHost(ptr, bytes));
+    return DOGM_OK;
+}
+dogm_status dogm_host_free(void* ptr) {
+    DOGM_CUDA(cudaFreeHost(ptr));
+    return DOGM_OK;
+}
+dogm_status dogm_device_alloc(void** ptr, size_t bytes) {
+    if (!ptr) return fail(DOGM_ERR_INVALID_ARGUMENT, "ptr is NULL");
+    DOGM_CUDA(cudaMalloc(ptr, bytes));
+    return DOGM_OK;
+}
+dogm_status dogm_device_free(void* ptr) {
+    DOGM_CUDA(cudaFree(ptr));
+    return DOGM_OK;
+}
+dogm_status dogm_memcpy(void* dst, const void* src, size_t bytes, int kind) {
+    DOGM_CUDA(cudaMemcpy(dst, src, bytes, static_cast<cudaMemcpyKind>(kind)));
+    return DOGM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+// dogm::DOGM — header-only C++ drop-in for the reference's class of the same name
+// (dogm/include/dogm/dogm.h:20-199), implemented over the C ABI in dogm_gb300.h.
+//
+// Same constructor, updateGrid, getters and public stage methods (particlePrediction,
+// initializeParticles).  The reference's remaining stage methods (particleAssignment,
+// gridCellOccupancyUpdate, updatePersistentParticles, initializeNewParticles,
+// statisticalMoments, resampling) run fused inside updateGrid and are not separate calls.
+// Error behaviour matches the reference's CHECK_ERROR (cuda_utils.h:13-24): print and
+// continue; define DOGM_GB300_THROW to throw std::runtime_error instead.
+#pragma once
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../dogm_gb300.h"
+#include "dogm_types.h"
+
+namespace dogm
+{
+
+inline void checkStatus(dogm_status s, const char* what)
+{
+    if (s == DOGM_OK)
+    {
+        return;
+    }
+#ifdef DOGM_GB300_THROW
+    throw std::runtime_error(std::string(what) + ": " + dogm_status_string(s) + " (" + dogm_last_error() + ")");
+#else
+    std::printf("GPU Kernel Error: %s %s (%s)\n", what, dogm_status_string(s), dogm_last_error());
+#endif
+}
+
+class DOGM
+{
+public:
+    // dogm.h:26-60 (same field order; layout-compatible with dogm_params)
+    struct Params
+    {
+        float size;
+        float resolution;
+        int particle_count;
+        int new_born_particle_count;
+        float persistence_prob;
+        float stddev_process_noise_position;
+        float stddev_process_noise_velocity;
+        float birth_prob;
+        float stddev_velocity;
+        float init_max_velocity;
+        float freespace_discount;
+    };
+    static_assert(sizeof(Params) == sizeof(dogm_params), "Params layout");
+
+    explicit DOGM(const Params& p, const dogm_options* opt = nullptr) : params(p), handle(nullptr)
+    {
+        checkStatus(dogm_create(reinterpret_cast<const dogm_params*>(&params), opt, &handle), "DOGM::DOGM");
+    }
+
+    ~DOGM() { dogm_destroy(handle); }
+
+    DOGM(const DOGM&) = delete;
+    DOGM& operator=(const DOGM&) = delete;
+
+    // dogm.h:80-81
+    void updateGrid(MeasurementCell* measurement_grid, float new_x, float new_y, float new_yaw, float dt,
+                    bool device = true)
+    {
+        checkStatus(dogm_update(handle, reinterpret_cast<const dogm_measurement_cell*>(measurement_grid), new_x, new_y,
+                                new_yaw, dt, device ? 1 : 0),
+                    "DOGM::updateGrid");
+    }
+
+    // dogm.h:88
+    std::vector<GridCell> getGridCells() const
+    {
+        std::vector<GridCell> cells(static_cast<size_t>(getGridSize()) * static_cast<size_t>(getGridSize()));
+        checkStatus(dogm_get_grid_cells(handle, reinterpret_cast<dogm_grid_cell*>(cells.data()), cells.size()),
+                    "DOGM::getGridCells");
+        return cells;
+    }
+
+    // dogm.h:95
+    std::vector<MeasurementCell> getMeasurementCells() const
+    {
+        std::vector<MeasurementCell> cells(static_cast<size_t>(getGridSize()) * static_cast<size_t>(getGridSize()));
+        checkStatus(
+            dogm_get_measurement_cells(handle, reinterpret_cast<dogm_measurement_cell*>(cells.data()), cells.size()),
+            "DOGM::getMeasurementCells");
+        return cells;
+    }
+
+    // dogm.h:102: a host ParticlesSoA the caller releases with .free()
+    ParticlesSoA getParticles() const
+    {
+        const int n = dogm_get_particle_count(handle);
+        ParticlesSoA particles(n, false);
+        std::vector<unsigned char> assoc(static_cast<size_t>(n));
+        checkStatus(dogm_get_particles(handle, reinterpret_cast<float*>(particles.state), particles.grid_cell_idx,
+                                       particles.weight, assoc.data(), static_cast<size_t>(n)),
+                    "DOGM::getParticles");
+        for (int i = 0; i < n; ++i)
+        {
+            particles.associated[i] = assoc[static_cast<size_t>(i)] != 0;
+        }
+        return particles;
+    }
+
+    int getGridSize() const { return dogm_get_grid_size(handle); }
+    float getResolution() const { return dogm_get_resolution(handle); }
+    float getPositionX() const { return dogm_get_position_x(handle); }
+    float getYaw() const { return dogm_get_yaw(handle); }
+    float getPositionY() const { return dogm_get_position_y(handle); }
+    int getIteration() const { return dogm_get_iteration(handle); }
+
+    // public stage methods (dogm.h:150-152)
+    void initializeParticles() { checkStatus(dogm_initialize_particles(handle), "DOGM::initializeParticles"); }
+    void particlePrediction(float dt) { checkStatus(dogm_particle_prediction(handle, dt), "DOGM::particlePrediction"); }
+
+    // private in the reference (dogm.h:144); public here so stage tests can drive it
+    void updatePose(float new_x, float new_y, float new_yaw)
+    {
+        checkStatus(dogm_update_pose(handle, new_x, new_y, new_yaw), "DOGM::updatePose");
+    }
+
+    Params params;
+    dogm_handle* handle;
+};
+
+} /* namespace dogm */

@@ -1,0 +1,154 @@
+"""GPU parity: the CUDA path against the FP32 oracle (bit-exact except the per-cell velocity
+sums, whose summation order differs) and the FP64 oracle (stated tolerances), with the
+GPU's own Philox draws replayed into the oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# Moments come from float sums in a different order: tolerance relative to the magnitude.
+MOMENT_RTOL = 2e-4
+MOMENT_ATOL = 2e-4
+EXACT_FIELDS = slice(2, 11)   # new_born .. w_UA: bit-exact
+MOMENT_FIELDS = slice(11, 16)
+
+
+def compare_frame(dogm, oracle, g, out, label):
+    cells = g.get_grid_cells()
+    ref = out["cells"]
+    assert np.array_equal(cells["start_idx"], ref[:, 0].astype(np.int32)), label + " start_idx"
+    assert np.array_equal(cells["end_idx"], ref[:, 1].astype(np.int32)), label + " end_idx"
+    names = dogm.GRID_CELL_FIELDS
+    for j in range(2, 11):
+        got, exp = cells[names[j]], ref[:, j]
+        bad = np.flatnonzero(got.view(np.uint32) != exp.view(np.uint32))
+        assert bad.size == 0, "%s field %s differs at %d cells, first %s: %r vs %r" % (
+            label, names[j], bad.size, bad[:3], got[bad[:3]], exp[bad[:3]])
+    for j in range(11, 16):
+        scale = np.maximum(np.abs(ref[:, j]), 1.0)
+        err = np.abs(cells[names[j]] - ref[:, j]) / scale
+        assert err.max() <= MOMENT_RTOL, "%s field %s rel err %g" % (label, names[j], err.max())
+    dbg = g.debug_export()
+    assert np.array_equal(dbg["sorted_cell"], (out["S_key"] & oracle.CELL_MASK).astype(np.int32)), label + " keys"
+    assert np.array_equal(dbg["sort_perm"], out["perm"]), label + " permutation"
+    assert np.array_equal(dbg["sorted_state"].view(np.uint32), out["S_state"].view(np.uint32)), label + " states"
+    assert dbg["joint_total"] == out["joint_total"], label + " joint total"
+    assert dbg["n_birth"] == out["n_birth"], label + " newborn count"
+    nb = out["n_birth"]
+    assert np.array_equal(dbg["birth_state"][:nb].view(np.uint32), out["B_state"][:nb].view(np.uint32)), label
+    assert np.array_equal(dbg["birth_weight"][:nb].view(np.uint32), out["B_w"][:nb].view(np.uint32)), label
+    assert np.array_equal(dbg["resample_src"], out["res_src"]), label + " resample indices"
+    parts = g.get_particles()
+    assert np.array_equal(parts["state"].view(np.uint32), np.asarray(out["P_state_after"]).view(np.uint32)), label
+
+
+def run_pair(dogm, oracle, scene, p, frames, meas_fn, pose_fn, seed=7, dt=0.1):
+    g = dogm.DOGM(p, seed=seed)
+    g.debug_enable(True)
+    o = oracle.OracleDOGM(p, np.float32)
+    for k in range(frames):
+        meas = meas_fn(k, g.grid_size)
+        x, y = pose_fn(k)
+        d = g.generate_draws(k)
+        g.set_replay(d["init_u"], d["predict_z"], d["birth_z"], d["resample_r"])
+        g.update_grid(meas, x, y, 0.0, dt)
+        out = o.update(meas, x, y, 0.0, dt, d)
+        out["P_state_after"] = o.P_state.copy()
+        compare_frame(dogm, oracle, g, out, "frame %d" % k)
+    g.close()
+
+
+@pytest.mark.parametrize("size,res,N,B", [(12.8, 0.2, 20000, 2000), (25.6, 0.1, 120000, 12000),
+                                          (4.0, 1.0, 3, 1), (6.4, 0.2, 50000, 0)])
+def test_replay_bit_exact_random_grids(dogm, oracle, scene, size, res, N, B):
+    p = dogm.make_params(size=size, resolution=res, particle_count=N, new_born_particle_count=B)
+    run_pair(dogm, oracle, scene, p, 4, lambda k, gs: scene.random_measurements(gs, seed=31 + k),
+             lambda k: (0.0, 0.0))
+
+
+def test_replay_bit_exact_scene_with_ego_motion(dogm, oracle, scene):
+    cfg = dict(scene.CONFIGS["small"])
+    cfg.update(size=25.6, resolution=0.1, particle_count=150000, new_born_particle_count=15000, ego_speed=10.0,
+               yaw_rate=0.1)
+    sc = scene.Scene(cfg, seed=3)
+    p = dogm.make_params(**scene.params_dict(cfg))
+    frames = [sc.frame(k) for k in range(6)]
+    run_pair(dogm, oracle, scene, p, 6, lambda k, gs: frames[k][0], lambda k: (frames[k][1], frames[k][2]))
+
+
+def test_philox_in_kernel_equals_replay(dogm, scene):
+    """The kernels' own draws equal the exported draws: replaying them changes no bit."""
+    p = dogm.make_params(size=12.8, resolution=0.2, particle_count=30000, new_born_particle_count=3000)
+    a = dogm.DOGM(p, seed=11)
+    b = dogm.DOGM(p, seed=11)
+    for k in range(3):
+        meas = scene.random_measurements(a.grid_size, seed=50 + k)
+        a.update_grid(meas, 0.0, 0.0, 0.0, 0.1)
+        d = b.generate_draws(k)
+        b.set_replay(d["init_u"], d["predict_z"], d["birth_z"], d["resample_r"])
+        b.update_grid(meas, 0.0, 0.0, 0.0, 0.1)
+        ca, cb = a.get_grid_cells(), b.get_grid_cells()
+        assert ca.tobytes() == cb.tobytes()
+        assert a.get_particles()["state"].tobytes() == b.get_particles()["state"].tobytes()
+
+
+def test_deterministic_and_batch_equals_alone(dogm, scene):
+    """Each grid's result is the same alone and inside a batch of uneven grids."""
+    sizes = [(12.8, 0.2, 20000, 2000), (6.4, 0.1, 40000, 4000), (20.0, 0.2, 60000, 6000)]
+    params = [dogm.make_params(size=s, resolution=r, particle_count=n, new_born_particle_count=b)
+              for s, r, n, b in sizes]
+    alone = [dogm.DOGM(p, seed=5, stream_id=i) for i, p in enumerate(params)]
+    batch = [dogm.DOGM(p, seed=5, stream_id=i) for i, p in enumerate(params)]
+    for k in range(4):
+        meas = [scene.random_measurements(g.grid_size, seed=70 + 10 * k + i) for i, g in enumerate(alone)]
+        xs = [0.3 * k * (i + 1) for i in range(3)]
+        for i, g in enumerate(alone):
+            g.update_grid(meas[i], xs[i], 0.0, 0.0, 0.1)
+        dogm.update_batch(batch, meas, xs, [0.0] * 3, [0.0] * 3, [0.1] * 3)
+        for ga, gb in zip(alone, batch):
+            assert ga.get_grid_cells().tobytes() == gb.get_grid_cells().tobytes()
+            pa, pb = ga.get_particles(), gb.get_particles()
+            assert pa["state"].tobytes() == pb["state"].tobytes()
+            assert np.array_equal(pa["grid_cell_idx"], pb["grid_cell_idx"])
+    for g in alone + batch:
+        g.close()
+
+
+def test_lower_bound_matches_searchsorted(dogm):
+    """The reference's multinomial search (resampling.cu:34-47): clamp, then lower_bound."""
+    rng = np.random.default_rng(3)
+    for n, q in [(1000, 700), (100000, 90000), (7, 20)]:
+        w = rng.random(n).astype(np.float32)
+        w[rng.random(n) < 0.2] = 0.0  # zero weights produce ties in the accumulator
+        acc = np.cumsum(w, dtype=np.float32)
+        qs = np.sort((rng.random(q) * acc[-1]).astype(np.float32))
+        qs[-1] = acc[-1] * np.float32(0.999)
+        got = dogm.lower_bound_f32(acc, qs, clamp_last=True)
+        acc2 = acc.copy()
+        if acc2[-1] != qs[-1]:
+            acc2[-1] = qs[-1]
+        assert np.array_equal(got, np.searchsorted(acc2, qs, side="left"))
+        got2 = dogm.lower_bound_f32(acc, qs, clamp_last=False)
+        assert np.array_equal(got2, np.searchsorted(acc, qs, side="left"))
+
+
+def test_fp64_tolerance_first_frame(dogm, oracle, scene):
+    """Against the double restatement on identical inputs: masses within 2e-6 absolute."""
+    p = dogm.make_params(size=25.6, resolution=0.1, particle_count=200000, new_born_particle_count=20000)
+    g = dogm.DOGM(p, seed=9)
+    o = oracle.OracleDOGM(p, np.float64)
+    meas = scene.random_measurements(g.grid_size, seed=99)
+    d = g.generate_draws(0)
+    g.set_replay(d["init_u"], d["predict_z"], d["birth_z"], d["resample_r"])
+    g.update_grid(meas, 0.0, 0.0, 0.0, 0.1)
+    out = o.update(meas, 0.0, 0.0, 0.0, 0.1, d)
+    cells = g.get_grid_cells()
+    names = dogm.GRID_CELL_FIELDS
+    # a particle within float rounding of a cell border may land in the neighbouring cell in
+    # double; compare the cells whose particle ranges agree (all but a handful)
+    same = (cells["start_idx"] == out["cells"][:, 0]) & (cells["end_idx"] == out["cells"][:, 1])
+    assert same.mean() > 0.999
+    for j in (2, 3, 4, 5, 6):
+        err = np.abs(cells[names[j]].astype(np.float64) - out["cells"][:, j])[same]
+        assert err.max() <= 2e-6, (names[j], err.max())
+    g.close()
