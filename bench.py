@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""bench.py — ms per DOGM update on one GB300 at the 2M-particle / 1.44M-cell workload.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step is one full update (ego shift, predict, sort, mass update, reweighting, newborns,
+moments, resampling) of the 1200 x 1200 grid with 2e6 persistent and 2e5 newborn particles,
+driven by a seeded synthetic scene.  Prints one JSON line (rank 0).
+  value   device time per update with the measurement grids already in HBM (CUDA events
+          on the library's stream over K back-to-back updates; the working set, > 300 MB
+          per update, is larger than the 129 MB L2, so no L2 flush is added)
+  e2e     the same through the C ABI with host buffers: pinned measurement in, H2D copy,
+          update, full grid (GridCell array) copied back to pinned host memory, per step
+  --impl reference  the reference's pipeline transcribed to C (oracle/dogm_oracle.c,
+          dogm_oracle_reference_f32) on all host cores, one full update per step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import glob
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+PKG = "dynamic-occupancy-grid-map_gb300"
+
+METRIC = "ms/update and HBM GB/s at 2M particles/1.44M cells; batched frames/s, p50/p99"
+WORKLOAD = "large"
+# Per-unit algorithmic bytes of the whole update (compulsory traffic of a single-read,
+# single-write pipeline): 152 B per particle, 29 B per newborn, 108 B per cell.
+ALG_PER_PARTICLE, ALG_PER_NEWBORN, ALG_PER_CELL = 152, 29, 108
+
+
+def stage_bytes(N: int, B: int, C_: int, n_occ: int, n_birth_cells: int) -> dict:
+    """Algorithmic bytes per launch of each kernel (what it must read and write once)."""
+    return {
+        "frame_begin": 0,
+        "predict": 40 * N,                       # state R/W 16+16, key R/W 4+4
+        "sort_pass0": 12 * N,                    # key R 4, (key, index) W 8
+        "sort_pass1": 44 * N,                    # (key, index) R 8, state gather R 16, state+key W 20
+        "segments": 20 * N + 32 * n_occ,         # key 4 + state 16 R; 32 B per occupied cell W
+        "cells": 112 * C_ + 32 * n_occ,          # meas 16 + free 4 R; record 64 + free 4 + rho_b 4 + w 4 + meas copy 16 W
+        "newborn": 4 * C_ + 24 * B + 12 * n_birth_cells,
+        "resample": 24 * (N + B) + 20 * N,       # key 4 + state 16 + weight 4 R; state+key 20 W
+    }
+
+
+def load_cudart():
+    cands = ["libcudart.so", "libcudart.so.13"] + sorted(glob.glob("/usr/local/cuda*/lib64/libcudart.so*"))
+    for c in cands:
+        try:
+            lib = C.CDLL(c)
+            lib.cudaEventCreate.argtypes = [C.c_void_p]
+            lib.cudaEventRecord.argtypes = [C.c_void_p, C.c_void_p]
+            lib.cudaEventSynchronize.argtypes = [C.c_void_p]
+            lib.cudaEventElapsedTime.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+            return lib
+        except OSError:
+            continue
+    raise RuntimeError("libcudart not found")
+
+
+class Events:
+    """CUDA events recorded on an explicit stream (the library's own)."""
+
+    def __init__(self, rt, stream: int):
+        self.rt, self.stream = rt, C.c_void_p(stream)
+
+    def new(self):
+        e = C.c_void_p()
+        assert self.rt.cudaEventCreate(C.byref(e)) == 0
+        return e
+
+    def record(self, e):
+        assert self.rt.cudaEventRecord(e, self.stream) == 0
+
+    def elapsed(self, a, b) -> float:
+        assert self.rt.cudaEventSynchronize(b) == 0
+        ms = C.c_float()
+        assert self.rt.cudaEventElapsedTime(C.byref(ms), a, b) == 0
+        return float(ms.value)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.proc = None
+        self.lines = []
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_frames(count: int, seed: int = 0):
+    import importlib
+    scene = importlib.import_module(PKG + ".scene")
+    cfg = scene.CONFIGS[WORKLOAD]
+    sc = scene.Scene(cfg, seed=seed)
+    return scene, cfg, [sc.frame(k) for k in range(count)]
+
+
+def cpu_baseline(frames, cfg, n_frames: int, threads: int = 0) -> dict:
+    """The reference's pipeline on the host cores over a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import importlib
+    import pyoracle
+    spec = importlib.util.spec_from_file_location("dogm_build", os.path.join(REPO, PKG, "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build_oracle()
+    dogm = importlib.import_module(PKG)
+    p = dogm.make_params(**importlib.import_module(PKG + ".scene").params_dict(cfg))
+    ref = pyoracle.ReferencePipeline(p, threads=threads)
+    m, x, y, yaw = frames[0]
+    ref.update(m, x, y, yaw, 0.1)  # first measurement: initialisation, not timed
+    times = []
+    for k in range(1, n_frames + 1):
+        m, x, y, yaw = frames[k % len(frames)]
+        t0 = time.perf_counter()
+        ref.update(m, x, y, yaw, 0.1)
+        times.append((time.perf_counter() - t0) * 1e3)
+    return {"value": statistics.median(times), "unit": "ms/update", "cores": ref.threads_used, "kind": "port",
+            "sample": "%d full updates of the %s workload after the first-measurement initialisation "
+                      "(dogm_oracle_reference_f32: the reference's stage sequence in float, OpenMP)"
+                      % (n_frames, WORKLOAD)}
+
+
+def run_gb300(args, rank: int, world: int):
+    import importlib
+    dogm = importlib.import_module(PKG)
+    spec = importlib.util.spec_from_file_location("dogm_build", os.path.join(REPO, PKG, "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build_cuda()
+    dogm.load()
+    K, W = args.steps, args.warmup
+    P = 5  # profiled updates
+    # frames: [0, W] warm-up, then K timed, K end-to-end, P profiled (the trajectory continues)
+    t0_, e0_, p0_ = W + 1, W + 1 + K, W + 1 + 2 * K
+    n_frames = W + 1 + 2 * K + P
+    scene, cfg, frames = make_frames(n_frames, seed=rank)
+    p = dogm.make_params(**scene.params_dict(cfg))
+    N, B = p.particle_count, p.new_born_particle_count
+    g = dogm.DOGM(p, seed=123456, stream_id=rank, sync_each_update=False)
+    C_ = g.cell_count
+    rt = load_cudart()
+    ev = Events(rt, g.stream())
+
+    # measurement grids resident in HBM
+    dbufs = []
+    for m, *_ in frames:
+        d = dogm.DeviceBuffer(m.nbytes)
+        d.upload(m)
+        dbufs.append(d)
+    # first measurement (initialisation) + warm-up (graph capture for both mirrors)
+    for k in range(W + 1):
+        m, x, y, yaw = frames[k]
+        g.update_grid(dbufs[k].ptr, x, y, yaw, 0.1, device=True)
+    g.synchronize()
+
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if world > 1 else 0)
+    barrier(world)
+    clocks.start()
+    e0, e1 = ev.new(), ev.new()
+    ev.record(e0)
+    for k in range(t0_, t0_ + K):
+        m, x, y, yaw = frames[k]
+        g.update_grid(dbufs[k].ptr, x, y, yaw, 0.1, device=True)
+    ev.record(e1)
+    total_ms = ev.elapsed(e0, e1)
+    g.synchronize()
+    clk = clocks.stop()
+    launches = g.last_launch_count() * K
+    total_ms = reduce_max(total_ms, world)
+
+    # end to end through the C ABI with host buffers (pinned), grid read back every step
+    pins = []
+    for k in range(K):
+        pa = dogm.PinnedArray((C_, 4), np.float32)
+        pa.array[:] = frames[e0_ + k][0]
+        pins.append(pa)
+    out = dogm.PinnedArray((C_,), dogm.GRID_CELL_DTYPE)
+    g.synchronize()
+    barrier(world)
+    e2, e3 = ev.new(), ev.new()
+    ev.record(e2)
+    for k in range(K):
+        _, x, y, yaw = frames[e0_ + k]
+        g.update_grid(pins[k].array, x, y, yaw, 0.1, device=False)
+        g.get_grid_cells(out.array)
+    ev.record(e3)
+    e2e_ms = reduce_max(ev.elapsed(e2, e3), world)
+    for pa in pins:
+        pa.free()
+    out.free()
+
+    # per-stage times (plain launches with an event between stages; separate from the timed loop)
+    g.profile_enable(True)
+    stage_runs = []
+    for k in range(p0_, p0_ + P):
+        m, x, y, yaw = frames[k]
+        g.update_grid(dbufs[k].ptr, x, y, yaw, 0.1, device=True)
+        g.synchronize()
+        stage_runs.append(g.stage_times())
+    g.profile_enable(False)
+    stages = {k: statistics.median(r[k] for r in stage_runs) for k in stage_runs[0]}
+    cells = g.get_grid_cells()
+    n_occ = int((cells["start_idx"] >= 0).sum())
+    n_bcells = int(((cells["w_A"] > 0) | (cells["w_UA"] > 0)).sum())
+    sb = stage_bytes(N, B, C_, n_occ, n_bcells)
+    dom = max((k for k in stages if k != "frame_begin"), key=lambda k: stages[k])
+    peaks = {}
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = sb[dom] / (stages[dom] * 1e-3) / 1e9
+    traffic = read_traffic(dom)
+
+
+    ms = total_ms / K / world
+    alg = ALG_PER_PARTICLE * N + ALG_PER_NEWBORN * B + ALG_PER_CELL * C_
+    line = {
+        "metric": METRIC, "value": round(ms, 4), "unit": "ms/update", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": round(total_ms / K, 4), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded scene: 40 vehicles + 30 pedestrians, 2160-beam lidar, "
+                                "inverse sensor model; no public dataset exists for this workload)",
+        "config": {"workload": "large: 120 x 120 m at 0.1 m (1200^2 = 1.44e6 cells), 2e6 persistent + 2e5 newborn "
+                               "particles, ego 10 m/s", "cells": C_, "particles": N, "newborn": B,
+                   "l2": "inputs larger than L2 (per-update working set > 300 MB vs 129 MB L2); no flush",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "hbm_gbs_whole_update": round(alg / (ms * 1e-3) / 1e9, 1),
+        "updates_per_s": round(1e3 / ms, 1),
+        "stage_ms": {k: round(v, 4) for k, v in stages.items()},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 3), "peak_source": peak_src, "traffic": traffic,
+                     "algorithmic_bytes": sb[dom]},
+        "e2e": {"value": round(e2e_ms / K / world, 4), "unit": "ms/update", "h2d_bytes_per_step": C_ * 16,
+                "d2h_bytes_per_step": C_ * 64},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    g.close()
+    for d in dbufs:
+        d.free()
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(frames, cfg, args.cpu_frames)
+    return line
+
+
+def read_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if present."""
+    path = os.path.join(REPO, "profiles", "ncu_traffic.md")
+    try:
+        for ln in open(path):
+            parts = [p.strip() for p in ln.strip().strip("|").split("|")]
+            if len(parts) >= 2 and parts[0] == kernel:
+                return int(float(parts[1]))
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return None
+    K, W = args.steps, args.warmup
+    _, cfg, frames = make_frames(min(K + W + 1, 12), seed=0)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import importlib
+    import pyoracle
+    spec = importlib.util.spec_from_file_location("dogm_build", os.path.join(REPO, PKG, "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build_oracle()
+    dogm = importlib.import_module(PKG)
+    p = dogm.make_params(**importlib.import_module(PKG + ".scene").params_dict(cfg))
+    ref = pyoracle.ReferencePipeline(p, threads=0)
+    for k in range(W + 1):
+        m, x, y, yaw = frames[k % len(frames)]
+        ref.update(m, x, y, yaw, 0.1)
+    t0 = time.perf_counter()
+    for k in range(K):
+        m, x, y, yaw = frames[(W + 1 + k) % len(frames)]
+        ref.update(m, x, y, yaw, 0.1)
+    ms = (time.perf_counter() - t0) * 1e3 / K
+    sample = "%d full updates of the %s workload (1.44e6 cells, 2e6 + 2e5 particles)" % (K, WORKLOAD)
+    return {"impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/update", "n_gpus": world,
+            "steps": K, "warmup": W, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "large: 120 x 120 m at 0.1 m (1200^2 cells), 2e6 + 2e5 particles",
+                       "implementation": "the reference's pipeline (dogm/src/dogm.cu:115-131) transcribed to C "
+                                         "with OpenMP; the reference itself is CUDA-only and has no CPU path"},
+            "cpu_baseline": {"value": round(ms, 3), "unit": "ms/update", "cores": ref.threads_used, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(ms, 3), "unit": "ms/update", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+_dist = None
+
+
+def barrier(world: int):
+    if world > 1 and _dist is not None:
+        _dist.barrier()
+
+
+def reduce_max(v: float, world: int) -> float:
+    if world <= 1 or _dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    _dist.all_reduce(t, op=_dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-frames", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    global _dist
+    if world > 1:
+        # one replica per GPU: the update does not shard, ranks share no data
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        _dist = dist
+    line = run_reference(args, rank, world) if args.impl == "reference" else run_gb300(args, rank, world)
+    if rank == 0 and line is not None:
+        print(json.dumps(line))
+    if _dist is not None:
+        _dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

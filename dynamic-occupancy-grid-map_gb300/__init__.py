@@ -42,7 +42,7 @@ ABI_SYMBOLS = [
     "dogm_set_replay", "dogm_clear_replay", "dogm_generate_draws", "dogm_debug_enable", "dogm_debug_export",
     "dogm_lower_bound_f32", "dogm_host_alloc", "dogm_host_free", "dogm_device_alloc", "dogm_device_free",
     "dogm_memcpy", "dogm_state_bytes", "dogm_last_launch_count", "dogm_last_error", "dogm_status_string",
-    "dogm_abi_version",
+    "dogm_abi_version", "dogm_get_stream", "dogm_profile_enable", "dogm_stage_times", "dogm_stage_name",
 ]
 
 
@@ -96,7 +96,8 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_lower_bound_f32": ([vp, i, vp, i, vp, i, vp], i), "dogm_host_alloc": ([vp, sz], i),
         "dogm_host_free": ([vp], i), "dogm_device_alloc": ([vp, sz], i), "dogm_device_free": ([vp], i),
         "dogm_memcpy": ([vp, vp, sz, i], i), "dogm_state_bytes": ([vp], sz), "dogm_last_launch_count": ([vp], i),
-        "dogm_last_error": ([], C.c_char_p), "dogm_status_string": ([i], C.c_char_p), "dogm_abi_version": ([], i),
+        "dogm_last_error": ([], C.c_char_p), "dogm_get_stream": ([vp], vp), "dogm_profile_enable": ([vp, i], i),
+        "dogm_stage_times": ([vp, vp, i], i), "dogm_stage_name": ([i], C.c_char_p), "dogm_status_string": ([i], C.c_char_p), "dogm_abi_version": ([], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -266,6 +267,19 @@ class DOGM:
 
     def last_launch_count(self) -> int:
         return load().dogm_last_launch_count(self.h)
+
+    def stream(self) -> int:
+        """The cudaStream_t the handle launches on (record CUDA events on it)."""
+        return load().dogm_get_stream(self.h) or 0
+
+    def profile_enable(self, enable: bool = True) -> None:
+        check(load().dogm_profile_enable(self.h, 1 if enable else 0), "dogm_profile_enable")
+
+    def stage_times(self) -> dict:
+        """Per-stage milliseconds of the last update (profiling enabled)."""
+        ms = np.zeros(16, np.float32)
+        n = load().dogm_stage_times(self.h, _ptr(ms), 16)
+        return {load().dogm_stage_name(i).decode(): float(ms[i]) for i in range(n)}
 
     # -- stages ---------------------------------------------------------------------------
     def particle_prediction(self, dt: float) -> None:

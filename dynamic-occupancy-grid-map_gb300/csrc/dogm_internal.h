@@ -139,6 +139,7 @@ cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCf
 cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg);
 cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg);
 cudaError_t launch_segments(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);

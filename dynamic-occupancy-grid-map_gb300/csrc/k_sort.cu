@@ -157,14 +157,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* bt) {
     }
 }
 
-cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg) {
+cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
     const size_t smem = sizeof(SortSmem);  // < 48 KB: no opt-in attribute needed
     Batch* b = const_cast<Batch*>(d_batch);
-    k_sort_pass<false><<<cfg.num_sms * 2, kThreads, smem, cfg.stream>>>(b);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_sort_pass<true><<<cfg.num_sms * 2, kThreads, smem, cfg.stream>>>(b);
+    if (pass == 0)
+        k_sort_pass<false><<<cfg.num_sms * 2, kThreads, smem, cfg.stream>>>(b);
+    else
+        k_sort_pass<true><<<cfg.num_sms * 2, kThreads, smem, cfg.stream>>>(b);
     return cudaGetLastError();
+}
+
+cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg) {
+    cudaError_t e = launch_sort_pass(d_batch, 0, cfg);
+    if (e != cudaSuccess) return e;
+    return launch_sort_pass(d_batch, 1, cfg);
 }
 
 }  // namespace dogm_gb300

@@ -38,22 +38,37 @@ int bitlen(unsigned long long v) {
 
 int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-// One launch context: a device copy of a Batch, its pinned host mirror and the CUDA graphs
-// of the steady-state frame, keyed by batch size (the upload size is fixed in a graph).
+constexpr int kStages = 8;  // frame-begin, predict, sort 0, sort 1, segments, cells, newborn, resample
+const char* const kStageNames[kStages] = {"frame_begin", "predict", "sort_pass0", "sort_pass1",
+                                          "segments",    "cells",   "newborn",    "resample"};
+
+// One launch context: a device copy of a Batch, two pinned host mirrors (the host fills one
+// while the device may still read the other, so frame k+1 is queued while frame k runs) and
+// the CUDA graphs of the steady-state frame, keyed by (batch size, mirror).
 struct Ctx {
     int device = -1;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     Batch* d_batch = nullptr;
-    Batch* h_batch = nullptr;            // pinned
-    unsigned int* h_status = nullptr;    // pinned copy of d_batch->status
+    Batch* h_batch[2] = {nullptr, nullptr};      // pinned
+    unsigned int* h_status = nullptr;            // pinned, one word per mirror
+    cudaEvent_t done[2] = {nullptr, nullptr};    // the frame that read mirror i has finished
+    bool pending[2] = {false, false};
+    int cur = 0;                                 // mirror of the frame being built
     std::map<int, cudaGraphExec_t> graphs;
+    bool profile = false;
+    cudaEvent_t ev[kStages + 1] = {};
 
     ~Ctx() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
         if (d_batch) cudaFree(d_batch);
-        if (h_batch) cudaFreeHost(h_batch);
+        for (int i = 0; i < 2; ++i) {
+            if (h_batch[i]) cudaFreeHost(h_batch[i]);
+            if (done[i]) cudaEventDestroy(done[i]);
+        }
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
         if (h_status) cudaFreeHost(h_status);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
@@ -66,10 +81,24 @@ dogm_status ctx_init(Ctx& c, int device) {
     c.own_stream = true;
     DOGM_CUDA(cudaMalloc(&c.d_batch, sizeof(Batch)));
     DOGM_CUDA(cudaMemset(c.d_batch, 0, sizeof(Batch)));
-    DOGM_CUDA(cudaMallocHost(&c.h_batch, sizeof(Batch)));
-    std::memset(c.h_batch, 0, sizeof(Batch));
-    DOGM_CUDA(cudaMallocHost(&c.h_status, sizeof(unsigned int)));
-    *c.h_status = 0;
+    for (int i = 0; i < 2; ++i) {
+        DOGM_CUDA(cudaMallocHost(&c.h_batch[i], sizeof(Batch)));
+        std::memset(c.h_batch[i], 0, sizeof(Batch));
+        DOGM_CUDA(cudaEventCreateWithFlags(&c.done[i], cudaEventDisableTiming));
+    }
+    DOGM_CUDA(cudaMallocHost(&c.h_status, 2 * sizeof(unsigned int)));
+    c.h_status[0] = c.h_status[1] = 0;
+    for (auto& e : c.ev) DOGM_CUDA(cudaEventCreate(&e));
+    return DOGM_OK;
+}
+
+// The mirror for the next frame: waits until the frame that last read it has finished.
+dogm_status acquire_mirror(Ctx& c) {
+    const int i = c.cur;
+    if (c.pending[i]) {
+        DOGM_CUDA(cudaEventSynchronize(c.done[i]));
+        c.pending[i] = false;
+    }
     return DOGM_OK;
 }
 
@@ -195,10 +224,10 @@ void fill_frame(dogm_handle* h, float dt, int shifted, int xm, int ym, const dog
     g.rp_resample = h->rp_resample;
 }
 
-// Writes n grid descriptors and the per-stage tile prefix into the pinned mirror.
-// init_mask[i] != 0 schedules the first-frame initialisation of grid i.
+// Writes n grid descriptors and the per-stage tile prefix into the current pinned mirror
+// (call acquire_mirror first).  init_mask[i] != 0 schedules grid i's first-frame init.
 void build_batch(Ctx& c, dogm_handle* const* hs, int n, const std::vector<int>& init_mask) {
-    Batch& b = *c.h_batch;
+    Batch& b = *c.h_batch[c.cur];
     b.n_grids = n;
     b.status = 0u;
     for (int s = 0; s < kNumStages; ++s) b.counters[s] = 0u;
@@ -218,77 +247,85 @@ size_t batch_head_bytes(int n) { return offsetof(Batch, prefix) + sizeof(int) * 
 size_t batch_desc_bytes(int n) { return sizeof(GridDesc) * (size_t)n; }
 
 cudaError_t upload_batch(Ctx& c, int n) {
-    cudaError_t e = cudaMemcpyAsync(c.d_batch, c.h_batch, batch_head_bytes(n), cudaMemcpyHostToDevice, c.stream);
+    Batch* h = c.h_batch[c.cur];
+    cudaError_t e = cudaMemcpyAsync(c.d_batch, h, batch_head_bytes(n), cudaMemcpyHostToDevice, c.stream);
     if (e != cudaSuccess) return e;
-    return cudaMemcpyAsync(&c.d_batch->g[0], &c.h_batch->g[0], batch_desc_bytes(n), cudaMemcpyHostToDevice, c.stream);
+    return cudaMemcpyAsync(&c.d_batch->g[0], &h->g[0], batch_desc_bytes(n), cudaMemcpyHostToDevice, c.stream);
 }
 
-// The steady-state frame: 8 kernels.
-cudaError_t frame_kernels(Ctx& c) {
+cudaError_t download_status(Ctx& c) {
+    return cudaMemcpyAsync(c.h_status + c.cur, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                           c.stream);
+}
+
+// The steady-state frame: 8 kernels; with profiling, a CUDA event before each and at the end.
+cudaError_t frame_kernels(Ctx& c, bool with_init) {
     LaunchCfg cfg{c.num_sms, c.stream};
+    const bool prof = c.profile && !with_init;
     cudaError_t e;
-    if ((e = launch_frame_begin(c.d_batch, 0, cfg)) != cudaSuccess) return e;
-    if ((e = launch_predict(c.d_batch, 0, cfg)) != cudaSuccess) return e;
-    if ((e = launch_sort(c.d_batch, cfg)) != cudaSuccess) return e;
-    if ((e = launch_segments(c.d_batch, cfg)) != cudaSuccess) return e;
-    if ((e = launch_cells(c.d_batch, cfg)) != cudaSuccess) return e;
-    if ((e = launch_newborn(c.d_batch, cfg)) != cudaSuccess) return e;
-    return launch_resample(c.d_batch, cfg);
+#define STAGE(i, call)                                                              \
+    do {                                                                            \
+        if (prof && (e = cudaEventRecord(c.ev[i], c.stream)) != cudaSuccess) return e; \
+        if ((e = (call)) != cudaSuccess) return e;                                  \
+    } while (0)
+    STAGE(0, launch_frame_begin(c.d_batch, 0, cfg));
+    if (with_init && (e = launch_init_particles(c.d_batch, cfg)) != cudaSuccess) return e;
+    STAGE(1, launch_predict(c.d_batch, 0, cfg));
+    STAGE(2, launch_sort_pass(c.d_batch, 0, cfg));
+    STAGE(3, launch_sort_pass(c.d_batch, 1, cfg));
+    STAGE(4, launch_segments(c.d_batch, cfg));
+    STAGE(5, launch_cells(c.d_batch, cfg));
+    STAGE(6, launch_newborn(c.d_batch, cfg));
+    STAGE(7, launch_resample(c.d_batch, cfg));
+#undef STAGE
+    if (prof && (e = cudaEventRecord(c.ev[kStages], c.stream)) != cudaSuccess) return e;
+    return cudaSuccess;
 }
 
-dogm_status run_frame(Ctx& c, int n, bool any_init, bool use_graph, int* launches) {
+// Queues one frame from the current mirror and advances to the other mirror.
+dogm_status run_frame(Ctx& c, int n, bool any_init, int* launches) {
     cudaError_t e;
-    if (any_init) {
-        // first frame of at least one grid: plain launches (init sits between begin and predict)
-        LaunchCfg cfg{c.num_sms, c.stream};
+    const bool plain = any_init || c.profile;
+    if (plain) {
+        // first frame of some grid (init runs between begin and predict) or per-stage timing
         DOGM_CUDA(upload_batch(c, n));
-        DOGM_CUDA(launch_frame_begin(c.d_batch, 0, cfg));
-        DOGM_CUDA(launch_init_particles(c.d_batch, cfg));
-        DOGM_CUDA(launch_predict(c.d_batch, 0, cfg));
-        DOGM_CUDA(launch_sort(c.d_batch, cfg));
-        DOGM_CUDA(launch_segments(c.d_batch, cfg));
-        DOGM_CUDA(launch_cells(c.d_batch, cfg));
-        DOGM_CUDA(launch_newborn(c.d_batch, cfg));
-        DOGM_CUDA(launch_resample(c.d_batch, cfg));
-        DOGM_CUDA(cudaMemcpyAsync(c.h_status, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
-                                  c.stream));
-        *launches = kLaunchesPerFrame + kLaunchesInit;
-        return DOGM_OK;
-    }
-    if (!use_graph) {
-        DOGM_CUDA(upload_batch(c, n));
-        DOGM_CUDA(frame_kernels(c));
-        DOGM_CUDA(cudaMemcpyAsync(c.h_status, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
-                                  c.stream));
+        DOGM_CUDA(frame_kernels(c, any_init));
+        DOGM_CUDA(download_status(c));
+        *launches = kLaunchesPerFrame + (any_init ? kLaunchesInit : 0);
+    } else {
+        const int key = n * 2 + c.cur;
+        auto it = c.graphs.find(key);
+        if (it == c.graphs.end()) {
+            cudaGraph_t graph;
+            DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            e = upload_batch(c, n);
+            if (e == cudaSuccess) e = frame_kernels(c, false);
+            if (e == cudaSuccess) e = download_status(c);
+            cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
+            if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+            if (e2 != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
+            cudaGraphExec_t exec;
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess)
+                return fail(DOGM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+            it = c.graphs.emplace(key, exec).first;
+        }
+        DOGM_CUDA(cudaGraphLaunch(it->second, c.stream));
         *launches = kLaunchesPerFrame;
-        return DOGM_OK;
     }
-    auto it = c.graphs.find(n);
-    if (it == c.graphs.end()) {
-        cudaGraph_t graph;
-        DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-        e = upload_batch(c, n);
-        if (e == cudaSuccess) e = frame_kernels(c);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(c.h_status, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
-                                c.stream);
-        cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
-        if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-        if (e2 != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
-        cudaGraphExec_t exec;
-        e = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-        it = c.graphs.emplace(n, exec).first;
-    }
-    DOGM_CUDA(cudaGraphLaunch(it->second, c.stream));
-    *launches = kLaunchesPerFrame;
+    DOGM_CUDA(cudaEventRecord(c.done[c.cur], c.stream));
+    c.pending[c.cur] = true;
+    c.cur ^= 1;
     return DOGM_OK;
 }
 
+// Waits for the context's stream and turns device status bits into a status code.
 dogm_status finish_frame(Ctx& c, dogm_handle* const* hs, int n) {
     DOGM_CUDA(cudaStreamSynchronize(c.stream));
-    const unsigned int st = *c.h_status;
+    c.pending[0] = c.pending[1] = false;
+    const unsigned int st = c.h_status[0] | c.h_status[1];
+    c.h_status[0] = c.h_status[1] = 0;
     if (st & kStatusTimeout) {
         for (int i = 0; i < n; ++i) hs[i]->need_clear = true;
         return fail(DOGM_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up (look-back predecessor never published)");
@@ -487,10 +524,11 @@ dogm_status dogm_update(dogm_handle* h, const dogm_measurement_cell* meas, float
     if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
     DeviceGuard dg(h->device);
     Ctx& c = h->ctx;
-    DOGM_CUDA(cudaStreamSynchronize(c.stream));  // the pinned batch mirror is reused
+    dogm_status st = acquire_mirror(c);  // frame k+1 is built while frame k may still run
+    if (st != DOGM_OK) return st;
     const dogm_measurement_cell* src;
     int copy;
-    dogm_status st = prepare_measurement(h, meas, device, c.stream, &src, &copy);
+    st = prepare_measurement(h, meas, device, c.stream, &src, &copy);
     if (st != DOGM_OK) return st;
     const bool init = !h->first_measurement_received;
     int shifted, xm, ym;
@@ -499,8 +537,7 @@ dogm_status dogm_update(dogm_handle* h, const dogm_measurement_cell* meas, float
     dogm_handle* hs[1] = {h};
     std::vector<int> init_mask(1, init ? 1 : 0);
     build_batch(c, hs, 1, init_mask);
-    h->desc.clear_lookback = 0;
-    st = run_frame(c, 1, init, true, &h->last_launches);
+    st = run_frame(c, 1, init, &h->last_launches);
     if (st != DOGM_OK) { h->need_clear = true; return st; }
     advance(h);
     if (h->opt.sync_each_update) return finish_frame(c, hs, 1);
@@ -533,6 +570,8 @@ dogm_status dogm_update_batch(dogm_handle* const* hs, int n, const dogm_measurem
         }
     }
     DOGM_CUDA(cudaStreamSynchronize(c->stream));
+    dogm_status st0 = acquire_mirror(*c);
+    if (st0 != DOGM_OK) return st0;
     std::vector<int> init_mask(n, 0);
     bool any_init = false;
     for (int i = 0; i < n; ++i) {
@@ -550,7 +589,7 @@ dogm_status dogm_update_batch(dogm_handle* const* hs, int n, const dogm_measurem
     }
     build_batch(*c, hs, n, init_mask);
     int launches = 0;
-    dogm_status st = run_frame(*c, n, any_init, true, &launches);
+    dogm_status st = run_frame(*c, n, any_init, &launches);
     if (st != DOGM_OK) {
         for (int i = 0; i < n; ++i) hs[i]->need_clear = true;
         return st;
@@ -637,6 +676,7 @@ dogm_status dogm_particle_prediction(dogm_handle* h, float dt) {
     DOGM_CUDA(cudaStreamSynchronize(c.stream));
     fill_frame(h, dt, 0, 0, 0, h->desc.meas_own, 0);
     dogm_handle* hs[1] = {h};
+    c.pending[0] = c.pending[1] = false;  // the stream was synchronised above
     build_batch(c, hs, 1, std::vector<int>(1, 0));
     DOGM_CUDA(upload_batch(c, 1));
     LaunchCfg cfg{c.num_sms, c.stream};
@@ -671,6 +711,7 @@ dogm_status dogm_initialize_particles(dogm_handle* h) {
     DOGM_CUDA(cudaStreamSynchronize(c.stream));
     fill_frame(h, 0.f, 0, 0, 0, h->desc.meas_own, 0);
     dogm_handle* hs[1] = {h};
+    c.pending[0] = c.pending[1] = false;  // the stream was synchronised above
     build_batch(c, hs, 1, std::vector<int>(1, 1));
     DOGM_CUDA(upload_batch(c, 1));
     LaunchCfg cfg{c.num_sms, c.stream};
@@ -799,6 +840,30 @@ dogm_status dogm_debug_export(dogm_handle* h, int* sorted_cell, float* sorted_st
     if (n_birth) *n_birth = fs.n_birth;
     return DOGM_OK;
 }
+
+// ---- measurement -------------------------------------------------------------------------
+
+void* dogm_get_stream(dogm_handle* h) { return h ? (void*)h->ctx.stream : nullptr; }
+
+dogm_status dogm_profile_enable(dogm_handle* h, int enable) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    h->ctx.profile = enable != 0;
+    return DOGM_OK;
+}
+
+int dogm_stage_times(dogm_handle* h, float* ms, int n) {
+    if (!h || !h->ctx.profile) return 0;
+    DeviceGuard dg(h->device);
+    if (cudaEventSynchronize(h->ctx.ev[kStages]) != cudaSuccess) return 0;
+    for (int i = 0; i < kStages && i < n; ++i) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, h->ctx.ev[i], h->ctx.ev[i + 1]);
+        if (ms) ms[i] = t;
+    }
+    return kStages;
+}
+
+const char* dogm_stage_name(int i) { return (i >= 0 && i < kStages) ? kStageNames[i] : ""; }
 
 // ---- utilities ---------------------------------------------------------------------------
 

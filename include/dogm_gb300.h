@@ -211,6 +211,20 @@ dogm_status dogm_memcpy(void* dst, const void* src, size_t bytes, int kind /* cu
 /* Device bytes a handle with these parameters holds (admission control). */
 size_t dogm_state_bytes(const dogm_params* params);
 
+/* ---- measurement ---------------------------------------------------------------------- */
+
+/* The cudaStream_t (as void*) the handle launches on: record CUDA events on it to time updates. */
+void* dogm_get_stream(dogm_handle* h);
+
+/* Per-stage timing (the reference has only a wall-clock timer around updateGrid,
+ * dogm/demo/main.cpp:81,91-92).  When enabled, updates run as plain launches with a CUDA
+ * event between stages instead of the CUDA graph; dogm_stage_times fills up to n values in
+ * milliseconds for the last update, in the order of dogm_stage_name(0..n-1), and returns
+ * the number of stages. */
+dogm_status dogm_profile_enable(dogm_handle* h, int enable);
+int dogm_stage_times(dogm_handle* h, float* ms, int n);
+const char* dogm_stage_name(int i);
+
 /* Number of kernel launches the last update issued, and the text of the last error. */
 int dogm_last_launch_count(const dogm_handle* h);
 const char* dogm_last_error(void);
