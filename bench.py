@@ -17,6 +17,8 @@ driven by a seeded synthetic scene.  Prints one JSON line (rank 0).
 from __future__ import annotations
 
 import argparse
+import importlib
+import importlib.util
 import ctypes as C
 import glob
 import json
