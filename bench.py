@@ -42,17 +42,21 @@ WORKLOAD = "large"
 ALG_PER_PARTICLE, ALG_PER_NEWBORN, ALG_PER_CELL = 152, 29, 108
 
 
-def stage_bytes(N: int, B: int, C_: int, n_occ: int, n_birth_cells: int) -> dict:
+def stage_bytes(N: int, B: int, C_: int, n_occ: int, n_birth_cells: int, sort_tiles: int, nb0: int,
+                nb1: int) -> dict:
     """Algorithmic bytes per launch of each kernel (what it must read and write once)."""
     return {
-        "frame_begin": 0,
-        "predict": 40 * N,                       # state R/W 16+16, key R/W 4+4
-        "sort_pass0": 12 * N,                    # key R 4, (key, index) W 8
+        "frame_begin": 4 * sort_tiles * nb1,     # zeroes the pass-1 digit counts
+        "predict": 40 * N + 4 * sort_tiles * nb0,  # state R/W 16+16, key R/W 4+4; digit counts W
+        "sort_scan0": 8 * sort_tiles * nb0,      # digit counts R, offsets W
+        "sort_pass0": 12 * N + 4 * sort_tiles * nb0,  # key R 4, (key, index) W 8; offsets R
+        "sort_scan1": 8 * sort_tiles * nb1,
         "sort_pass1": 44 * N,                    # (key, index) R 8, state gather R 16, state+key W 20
         "segments": 20 * N + 32 * n_occ,         # key 4 + state 16 R; 32 B per occupied cell W
         "cells": 112 * C_ + 32 * n_occ,          # meas 16 + free 4 R; record 64 + free 4 + rho_b 4 + w 4 + meas copy 16 W
-        "newborn": 4 * C_ + 24 * B + 12 * n_birth_cells,
-        "resample": 24 * (N + B) + 20 * N,       # key 4 + state 16 + weight 4 R; state+key 20 W
+        "newborn": 4 * C_ + 32 * n_birth_cells,   # newborn mass R; w_A/w_UA + newborn-cell list W
+        "resample": 24 * N + 20 * N,             # key 4 + state 16 + weight 4 R; state+key 20 W
+                                                 # (newborns are created in registers)
     }
 
 
@@ -260,7 +264,10 @@ def run_gb300(args, rank: int, world: int):
     cells = g.get_grid_cells()
     n_occ = int((cells["start_idx"] >= 0).sum())
     n_bcells = int(((cells["w_A"] > 0) | (cells["w_UA"] > 0)).sum())
-    sb = stage_bytes(N, B, C_, n_occ, n_bcells)
+    bits = max(1, (C_ - 1).bit_length())
+    d0 = (bits + 1) // 2
+    sort_tiles = -(-N // 4096)
+    sb = stage_bytes(N, B, C_, n_occ, n_bcells, sort_tiles, 1 << d0, 1 << (bits - d0))
     dom = max((k for k in stages if k != "frame_begin"), key=lambda k: stages[k])
     peaks = {}
     try:

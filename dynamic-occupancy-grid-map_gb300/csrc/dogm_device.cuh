@@ -176,10 +176,9 @@ __device__ __forceinline__ int claim_tile(Batch* bt, int stage, int* smem_slot) 
 }
 
 // ---------------------------------------------------------------------------------------
-// Bounded waits: every spin gives up after ~1 s, records kStatusTimeout and lets the
-// kernel finish, so a lost predecessor never hangs the GPU.
+// Status bits (kernels record failed checks and finish; the host turns them into status
+// codes).  No kernel of the update waits on another block.
 // ---------------------------------------------------------------------------------------
-constexpr int kSpinLimit = 1 << 20;
 
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t* p) { return *(const volatile uint32_t*)p; }
 __device__ __forceinline__ unsigned long long ld_volatile(const unsigned long long* p) {
@@ -195,27 +194,6 @@ __device__ __forceinline__ void flag_status(const GridDesc& g, uint32_t bits) {
     atomicOr(g.status_out, bits);
 }
 __device__ __forceinline__ void flag_timeout(const GridDesc& g) { flag_status(g, kStatusTimeout); }
-
-// 64-bit look-back words: bit 63 inclusive, bit 62 aggregate, bits 0..61 value.
-constexpr unsigned long long kLbInc64 = 1ull << 63;
-constexpr unsigned long long kLbAgg64 = 1ull << 62;
-constexpr unsigned long long kLbVal64 = (1ull << 62) - 1ull;
-
-// Exclusive prefix of tile t from a chain of 64-bit look-back words (tile t has already
-// published its aggregate).  Called by one thread.
-__device__ __forceinline__ unsigned long long lookback64(const unsigned long long* lb, int t, const GridDesc& g) {
-    unsigned long long sum = 0ull;
-    int p = t - 1;
-    int spins = 0;
-    while (p >= 0) {
-        const unsigned long long v = ld_volatile(lb + p);
-        if (v & kLbInc64) { sum += v & kLbVal64; break; }
-        if (v & kLbAgg64) { sum += v & kLbVal64; --p; continue; }
-        if (++spins > kSpinLimit) { flag_timeout(g); break; }
-        __nanosleep(64);
-    }
-    return sum;
-}
 
 // Block-wide exclusive scan of one 64-bit value per thread (256 threads).  Returns the
 // exclusive prefix; *total receives the block sum.  scratch: >= 8 entries.
@@ -240,6 +218,17 @@ __device__ __forceinline__ unsigned long long block_excl_scan_u64(unsigned long 
     __syncthreads();
     *total = tot;
     return wpre + x - v;
+}
+
+// Sum of sums[0 .. t) by the whole block (the exclusive prefix of tile t from per-tile
+// sums that a previous kernel completed; exact, so any order gives the same bits).
+__device__ __forceinline__ unsigned long long block_sum_before(const unsigned long long* sums, int t,
+                                                               unsigned long long* scratch) {
+    unsigned long long v = 0ull;
+    for (int i = threadIdx.x; i < t; i += blockDim.x) v += sums[i];
+    unsigned long long total;
+    block_excl_scan_u64(v, scratch, &total);
+    return total;
 }
 
 // Block-wide exclusive scan of one int per thread.

@@ -27,8 +27,11 @@ constexpr int kCellTile = kThreads * kCellIpt;
 constexpr int kResIpt = 8;           // joint particles per thread in resampling
 constexpr int kResTile = kThreads * kResIpt;
 
+static_assert(kPredictTile == kSortTile, "predict writes the pass-0 digit counts of the sort tiles");
+static_assert(kSegTile == kResTile, "cells add persistent weights into resample tiles by sorted position");
+
 constexpr int kMaxKeyBits = 22;      // grid_size <= 2048 -> cells < 2^22 -> 2 radix passes
-constexpr int kMaxParticles = (1 << 24) - 1;  // sort look-back words hold 24-bit counts
+constexpr int kMaxParticles = (1 << 24) - 1;  // keys, counts and slot indices stay below 2^24
 
 // Particle key word: bits 0..29 cell index, bit 30 "out of grid" (weight 0), bit 31 associated.
 constexpr uint32_t kCellMask = 0x3fffffffu;
@@ -40,8 +43,14 @@ enum DrawStage : uint32_t { kDrawInit = 1, kDrawPredict = 2, kDrawBirth = 3, kDr
 
 // Stages that claim tiles from a work counter (look-back ordering) or iterate statically.
 enum Stage : int {
-    kStPredict = 0, kStSort0, kStSort1, kStSeg, kStCell, kStBirth, kStResample, kStInitScan, kStInitExpand,
-    kNumStages
+    kStPredict = 0, kStScan0, kStSort0, kStScan1, kStSort1, kStSeg, kStCell, kStBirth, kStResample, kStInitScan,
+    kStInitExpand, kNumStages
+};
+
+// One cell that receives newborns this frame (compact per cell tile).
+struct NewbornCell {
+    int cell, first, n, nu_A;   // cell index, first newborn slot, slots, associated slots
+    float w_A, w_UA;
 };
 
 // Per-grid state that lives on the device across frames.
@@ -81,8 +90,6 @@ struct GridDesc {
     uint32_t frame;         // iteration number (Philox counter word 1)
     uint32_t stream_id;     // Philox counter word 3
     uint32_t seed_lo, seed_hi;
-    uint32_t epoch;         // sort look-back epoch tag (frame & 63)
-    int clear_lookback;     // 1: the frame-begin kernel zeroes the sort look-back words
     // particles (persistent: P, sort temporaries: T, sorted: S, newborn: Bp)
     float4* P_state; uint32_t* P_key;
     uint32_t* T_key; uint32_t* T_idx;
@@ -100,11 +107,15 @@ struct GridDesc {
     uint32_t* occ_bits;     // per cell occupancy bit of this frame
     // scratch
     uint32_t* hist;         // 2 x kSortMaxBins digit histograms
-    uint32_t* lb_sort;      // 2 x sort_tiles x kSortMaxBins look-back words
+    uint32_t* hsort;        // 2 x sort_tiles x kSortMaxBins: per-tile digit counts, then offsets
     SegSums* seg_head;      // per segmented-reduction tile: partial of the segment entering it
     SegSums* seg_tail;      // per tile: partial of the segment leaving it
-    unsigned long long* lb_cell;   // per cell tile: look-back of quantised newborn masses
-    unsigned long long* lb_res;    // per resample tile: look-back of quantised joint weights
+    unsigned long long* cell_sum;  // per cell tile: quantised newborn mass (first half) and
+                                   // first-frame occupied mass (second half)
+    unsigned long long* res_sum;   // per resample tile: quantised joint weight (exact atomics)
+    NewbornCell* nb_list;   // per cell tile, kCellTile entries: the cells that get newborns
+    int* nb_count;          // per cell tile: entries used in nb_list
+    int* nb_tile_start;     // per cell tile (+1 at the end): first newborn slot of the tile
     FrameState* fs;
     unsigned int* status_out;  // the batch-level status word
     // replay inputs (NULL: Philox) and debug outputs (NULL: off)
@@ -140,6 +151,7 @@ cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg);
 cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg);
+cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cfg);
 cudaError_t launch_segments(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);
@@ -150,9 +162,9 @@ cudaError_t launch_draws(const GridDesc& g, int iteration, float2* init_u, float
 cudaError_t launch_lower_bound(const float* accum, int n_accum, const float* q, int n_q, int* out, int clamp_last,
                                cudaStream_t s);
 
-// Kernel launches per update (for the launch-count claim): frame-begin, predict, 2 sort
-// passes, segments, cells, newborn, resample.
-constexpr int kLaunchesPerFrame = 8;
+// Kernel launches per update (for the launch-count claim): frame-begin, predict, 2 x (digit
+// scan, sort pass), segments, cells, newborn, resample.
+constexpr int kLaunchesPerFrame = 10;
 constexpr int kLaunchesInit = 2;
 
 }  // namespace dogm_gb300

@@ -8,8 +8,9 @@
 //               reweighting (update_persistent_particles.cu:49-87), the moments
 //               (statistical_moments.cu:78-106), the ego shift of the free mass
 //               (ego_motion_compensation.cu:25-43) and the measurement copy (dogm.cu:205-208).
-//  k_newborn  : newborn allocation over an exact scan of the newborn masses and newborn
-//               initialisation (init_new_particles.cu:126-195, dogm.cu:323-348).
+//  k_newborn  : newborn allocation over an exact scan of the newborn masses
+//               (init_new_particles.cu:126-155, dogm.cu:323-348); the newborn particles
+//               themselves are created where they are consumed, in the resample kernel.
 #include "dogm_device.cuh"
 
 namespace dogm_gb300 {
@@ -55,8 +56,30 @@ __device__ __forceinline__ SegSums to_sums(const SegRun& r) {
     return s;
 }
 
+__device__ __forceinline__ SegRun seg_item(uint32_t kw, float4 st, bool head, int pos) {
+    SegRun it;
+    it.head = head ? pos : -1;
+    if (kw & kOutBit) {
+        it.n = 0;
+        it.vx = it.vy = it.vxx = it.vyy = it.vxy = 0.0f;
+    } else {
+        it.n = 1;
+        it.vx = st.z;
+        it.vy = st.w;
+        it.vxx = __fmul_rn(st.z, st.z);
+        it.vyy = __fmul_rn(st.w, st.w);
+        it.vxy = __fmul_rn(st.z, st.w);
+    }
+    return it;
+}
+
+// One tile = kSegTile consecutive sorted particles, staged in shared memory with coalesced
+// loads; thread i reduces items [i*kSegIpt, (i+1)*kSegIpt) in order, then a block-wide
+// segmented scan joins the threads.  The combine order depends only on positions, so the
+// sums are deterministic.
 __global__ void __launch_bounds__(kThreads) k_segments(Batch* bt) {
     __shared__ uint32_t skey[kSegTile + 2];
+    __shared__ float2 svel[kSegTile];
     __shared__ SegRun wagg[kThreads / 32];
     const int total = batch_total(bt, kStSeg);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -66,49 +89,29 @@ __global__ void __launch_bounds__(kThreads) k_segments(Batch* bt) {
         const int lt = t - bt->prefix[gi][kStSeg];
         const int base = lt * kSegTile;
         const int n = min(kSegTile, g.N - base);
-        for (int i = threadIdx.x; i < n; i += kThreads) skey[1 + i] = g.S_key[base + i];
+        for (int i = threadIdx.x; i < n; i += kThreads) {
+            skey[1 + i] = g.S_key[base + i];
+            const float4 st = g.S_state[base + i];
+            svel[i] = make_float2(st.z, st.w);
+        }
         if (threadIdx.x == 0) {
             skey[0] = base > 0 ? (g.S_key[base - 1] & kCellMask) : 0xffffffffu;
             skey[n + 1] = (base + n < g.N) ? (g.S_key[base + n] & kCellMask) : 0xffffffffu;
         }
         __syncthreads();
 
-        // thread items: j = tid*kSegIpt + r (blocked)
-        SegRun item[kSegIpt];
-        bool head[kSegIpt], tail[kSegIpt];
-        uint32_t cell[kSegIpt];
+        const int j0 = threadIdx.x * kSegIpt;
         SegRun agg;
         agg.head = -1; agg.n = 0; agg.vx = agg.vy = agg.vxx = agg.vyy = agg.vxy = 0.0f;
-#pragma unroll
         for (int r = 0; r < kSegIpt; ++r) {
-            const int j = threadIdx.x * kSegIpt + r;
-            SegRun it;
-            it.head = -1; it.n = 0; it.vx = it.vy = it.vxx = it.vyy = it.vxy = 0.0f;
-            head[r] = tail[r] = false;
-            cell[r] = 0u;
-            if (j < n) {
-                const uint32_t kw = skey[1 + j];
-                const uint32_t c = kw & kCellMask;
-                cell[r] = c;
-                const uint32_t prev = (j == 0) ? skey[0] : (skey[j] & kCellMask);
-                const uint32_t next = (j == n - 1) ? skey[n + 1] : (skey[2 + j] & kCellMask);
-                head[r] = (c != prev);
-                tail[r] = (c != next);
-                if (!(kw & kOutBit)) {
-                    const float4 s = g.S_state[base + j];
-                    it.n = 1;
-                    it.vx = s.z;
-                    it.vy = s.w;
-                    it.vxx = __fmul_rn(s.z, s.z);
-                    it.vyy = __fmul_rn(s.w, s.w);
-                    it.vxy = __fmul_rn(s.z, s.w);
-                }
-                if (head[r]) it.head = base + j;
-            }
-            item[r] = it;
-            agg = seg_combine(agg, it);
+            const int j = j0 + r;
+            if (j >= n) break;
+            const uint32_t kw = skey[1 + j];
+            const uint32_t prev = (j == 0) ? skey[0] : (skey[j] & kCellMask);
+            const float2 v = svel[j];
+            agg = seg_combine(agg, seg_item(kw, make_float4(0.f, 0.f, v.x, v.y), (kw & kCellMask) != prev, base + j));
         }
-        // warp inclusive segmented scan of the thread aggregates
+        // block-wide exclusive segmented scan of the thread aggregates
         SegRun inc = agg;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -125,18 +128,20 @@ __global__ void __launch_bounds__(kThreads) k_segments(Batch* bt) {
 
         // re-walk and emit at segment tails
         SegRun run = excl;
-#pragma unroll
         for (int r = 0; r < kSegIpt; ++r) {
-            const int j = threadIdx.x * kSegIpt + r;
+            const int j = j0 + r;
             if (j >= n) break;
-            run = seg_combine(run, item[r]);
+            const uint32_t kw = skey[1 + j];
+            const uint32_t c = kw & kCellMask;
+            const uint32_t prev = (j == 0) ? skey[0] : (skey[j] & kCellMask);
+            const uint32_t next = (j == n - 1) ? skey[n + 1] : (skey[2 + j] & kCellMask);
+            const float2 v = svel[j];
+            run = seg_combine(run, seg_item(kw, make_float4(0.f, 0.f, v.x, v.y), c != prev, base + j));
             const int pos = base + j;
-            const uint32_t c = cell[r];
-            if (tail[r]) {
+            if (c != next) {
                 if (run.head >= 0) {
-                    const SegSums s = to_sums(run);
-                    g.seg_i[c] = make_int4(run.head, pos, s.n_in, __float_as_int(s.vxy));
-                    g.seg_f[c] = make_float4(s.vx, s.vy, s.vxx, s.vyy);
+                    g.seg_i[c] = make_int4(run.head, pos, run.n, __float_as_int(run.vxy));
+                    g.seg_f[c] = make_float4(run.vx, run.vy, run.vxx, run.vyy);
                     atomicOr(&g.occ_bits[c >> 5], 1u << (c & 31));
                 } else {
                     g.seg_head[lt] = to_sums(run);
@@ -160,13 +165,10 @@ __global__ void __launch_bounds__(kThreads) k_segments(Batch* bt) {
 // Fused per-cell update.
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_cells(Batch* bt) {
-    __shared__ int slot;
     __shared__ unsigned long long red[kThreads / 32];
     __shared__ unsigned long long red2[kThreads / 32];
     const int total = batch_total(bt, kStCell);
-    for (;;) {
-        const int t = claim_tile(bt, kStCell, &slot);
-        if (t >= total) break;
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStCell, t);
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][kStCell];
@@ -242,37 +244,53 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* bt) {
             g.rho_b[k] = o.rho_b;
             g.w_cell[k] = wp;
             qb += quantize(o.rho_b, g.q_shift);
-            jq += (unsigned long long)s.n_in * quantize(wp, g.q_shift);
+            // this cell's persistent particles sit at sorted positions [start, end]; their
+            // quantised weights go to the resample tiles that hold them (exact integer adds)
+            const unsigned long long qw = quantize(wp, g.q_shift);
+            if (s.n_in > 0 && qw > 0ull) {
+                jq += (unsigned long long)s.n_in * qw;
+                const int ts = start / kResTile, te = end / kResTile;
+                if (ts == te) {
+                    atomicAdd(&g.res_sum[ts], (unsigned long long)s.n_in * qw);
+                } else {
+                    atomicAdd(&g.res_sum[ts], (unsigned long long)g.seg_tail[ts].n_in * qw);
+                    for (int tt = ts + 1; tt <= te; ++tt)
+                        atomicAdd(&g.res_sum[tt], (unsigned long long)g.seg_head[tt].n_in * qw);
+                }
+            }
         }
         unsigned long long tile_qb, tile_jq;
         block_excl_scan_u64(qb, red, &tile_qb);
         block_excl_scan_u64(jq, red2, &tile_jq);
         if (threadIdx.x == 0) {
-            unsigned long long* lb = g.lb_cell;
-            if (lt == 0) {
-                st_volatile(lb, kLbInc64 | tile_qb);
-            } else {
-                st_volatile(lb + lt, kLbAgg64 | tile_qb);
-                const unsigned long long excl = lookback64(lb, lt, g);
-                st_volatile(lb + lt, kLbInc64 | (excl + tile_qb));
-            }
+            g.cell_sum[lt] = tile_qb;
             atomicAdd(&g.fs->qb_total, tile_qb);
-            atomicAdd(&g.fs->joint_total, tile_jq);
+            if (tile_jq) atomicAdd(&g.fs->joint_total, tile_jq);
         }
     }
 }
 
 // ---------------------------------------------------------------------------------------
-// Newborn allocation and initialisation.  Cell k owns newborn slots
-// [floor(Q[k-1] B / Q), floor(Q[k] B / Q)) of the exact prefix Q of quantised newborn
-// masses; nu_A = round(n p_A) of them are associated (the reference marks nu_A + 1,
-// racing with the next cell: init_new_particles.cu:145-153).
+// Newborn allocation.  Cell k owns newborn slots [floor(Q[k-1] B / Q), floor(Q[k] B / Q))
+// of the exact prefix Q of quantised newborn masses; nu_A = round(n p_A) of them are
+// associated (the reference marks nu_A + 1, racing with the next cell:
+// init_new_particles.cu:145-153).  Writes w_A / w_UA into the records, a compact list of
+// the tile's newborn cells (the resample kernel creates the newborns from it) and the
+// newborns' quantised weights into the resample tiles that will hold them.
 // ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void add_joint_range(unsigned long long* res_sum, long long a, long long b,
+                                                unsigned long long q) {
+    if (q == 0ull) return;
+    for (long long t = a / kResTile; t * kResTile < b; ++t) {
+        const long long lo = max(a, t * (long long)kResTile);
+        const long long hi = min(b, (t + 1) * (long long)kResTile);
+        if (hi > lo) atomicAdd(&res_sum[t], (unsigned long long)(hi - lo) * q);
+    }
+}
+
 __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
     __shared__ unsigned long long red[kThreads / 32];
-    __shared__ int bnd[kCellTile + 1];
-    __shared__ int s_nuA[kCellTile];
-    __shared__ float s_wA[kCellTile], s_wUA[kCellTile];
+    __shared__ int iscan[kThreads / 32];
     const int total = batch_total(bt, kStBirth);
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStBirth, t);
@@ -280,7 +298,7 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
         const int lt = t - bt->prefix[gi][kStBirth];
         const int base = lt * kCellTile;
         const unsigned long long T = g.fs->qb_total;
-        const unsigned long long E = lt > 0 ? (ld_volatile(g.lb_cell + lt - 1) & kLbVal64) : 0ull;
+        const unsigned long long E = block_sum_before(g.cell_sum, lt, red);
         unsigned long long q[kCellIpt];
         float rb[kCellIpt];
         unsigned long long v = 0ull;
@@ -293,68 +311,51 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
         }
         unsigned long long tile_sum;
         unsigned long long acc = E + block_excl_scan_u64(v, red, &tile_sum);
-        if (threadIdx.x == 0) bnd[0] = alloc_boundary(E, T, g.B);
         int lo_c = alloc_boundary(acc, T, g.B);
-        unsigned long long jq = 0ull;
+        if (threadIdx.x == 0) g.nb_tile_start[lt] = lo_c;
+        int bnd[kCellIpt + 1];
+        bnd[0] = lo_c;
+        int nflag = 0;
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
-            const int c = threadIdx.x * kCellIpt + j;
-            const int k = base + c;
             acc += q[j];
-            const int hi_c = alloc_boundary(acc, T, g.B);
-            bnd[1 + c] = hi_c;
-            const int nnew = hi_c - lo_c;
-            int nuA = 0;
-            float wA = 0.0f, wUA = 0.0f;
+            bnd[j + 1] = alloc_boundary(acc, T, g.B);
+            nflag += (bnd[j + 1] > bnd[j]) ? 1 : 0;
+        }
+        int ntile;
+        int pos = block_excl_scan_i32(nflag, iscan, &ntile);
+        unsigned long long jq = 0ull;
+        const long long N = g.N;
+#pragma unroll
+        for (int j = 0; j < kCellIpt; ++j) {
+            const int k = base + threadIdx.x * kCellIpt + j;
+            const int nnew = bnd[j + 1] - bnd[j];
             if (nnew > 0 && k < g.C) {
                 const float pA = g.meas_own[k].p_A;
-                nuA = (int)roundf(__fmul_rn((float)nnew, pA));
+                const int nuA = (int)roundf(__fmul_rn((float)nnew, pA));
                 const int nuUA = nnew - nuA;
-                wA = nuA > 0 ? __fdiv_rn(__fmul_rn(pA, rb[j]), (float)nuA) : 0.0f;
-                wUA = nuUA > 0 ? __fdiv_rn(__fmul_rn(__fsub_rn(1.0f, pA), rb[j]), (float)nuUA) : 0.0f;
+                const float wA = nuA > 0 ? __fdiv_rn(__fmul_rn(pA, rb[j]), (float)nuA) : 0.0f;
+                const float wUA = nuUA > 0 ? __fdiv_rn(__fmul_rn(__fsub_rn(1.0f, pA), rb[j]), (float)nuUA) : 0.0f;
                 g.cells[k].w_A = wA;
                 g.cells[k].w_UA = wUA;
-                jq += (unsigned long long)max(nuA, 0) * quantize(wA, g.q_shift) +
-                      (unsigned long long)max(nuUA, 0) * quantize(wUA, g.q_shift);
+                NewbornCell e;
+                e.cell = k; e.first = bnd[j]; e.n = nnew; e.nu_A = nuA; e.w_A = wA; e.w_UA = wUA;
+                g.nb_list[(size_t)lt * kCellTile + pos] = e;
+                ++pos;
+                const int nA = min(max(nuA, 0), nnew);
+                const unsigned long long qA = quantize(wA, g.q_shift), qU = quantize(wUA, g.q_shift);
+                jq += (unsigned long long)nA * qA + (unsigned long long)(nnew - nA) * qU;
+                add_joint_range(g.res_sum, N + bnd[j], N + bnd[j] + nA, qA);
+                add_joint_range(g.res_sum, N + bnd[j] + nA, N + bnd[j + 1], qU);
             }
-            s_nuA[c] = nuA;
-            s_wA[c] = wA;
-            s_wUA[c] = wUA;
-            lo_c = hi_c;
-        }
-        __syncthreads();
-        const int ncell = min(kCellTile, g.C - base);
-        const int lo = bnd[0], hi = bnd[ncell];
-        const float fgs = (float)g.gs;
-        for (int s = lo + threadIdx.x; s < hi; s += kThreads) {
-            int a = 0, b = ncell - 1;
-            while (a < b) {
-                const int m = (a + b) >> 1;
-                if (bnd[1 + m] > s) b = m; else a = m + 1;
-            }
-            const int k = base + a;
-            const bool assoc = (s - bnd[a]) < s_nuA[a];
-            float2 z;
-            if (g.rp_birth) {
-                z = g.rp_birth[s];
-            } else {
-                const U4 r = draw_block(g, (uint32_t)s, g.frame, kDrawBirth);
-                z = box_muller(r.x, r.y);
-            }
-            float4 st;
-            st.x = __fadd_rn((float)(k % g.gs), 0.5f);
-            st.y = __fadd_rn(__fdiv_rn((float)k, fgs), 0.5f);  // float division, as the reference
-            st.z = __fmaf_rn(z.x, g.sigma_birth, 0.0f);
-            st.w = __fmaf_rn(z.y, g.sigma_birth, 0.0f);
-            g.B_state[s] = st;
-            g.B_key[s] = (uint32_t)k | (assoc ? kAssocBit : 0u);
-            g.B_w[s] = assoc ? s_wA[a] : s_wUA[a];
         }
         unsigned long long tile_jq;
         block_excl_scan_u64(jq, red, &tile_jq);
         if (threadIdx.x == 0) {
+            g.nb_count[lt] = ntile;
             if (tile_jq) atomicAdd(&g.fs->joint_total, tile_jq);
             if (lt == 0) g.fs->n_birth = (T > 0ull) ? g.B : 0;
+            if (lt == g.tiles[kStBirth] - 1) g.nb_tile_start[lt + 1] = (T > 0ull) ? g.B : 0;
         }
         __syncthreads();
     }

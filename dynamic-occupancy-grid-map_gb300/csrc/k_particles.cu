@@ -15,12 +15,12 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* bt) {
         for (int i = tid; i < 2 * kSortMaxBins; i += stride) g.hist[i] = 0u;
         const int words = (g.C + 31) >> 5;
         for (int i = tid; i < words; i += stride) g.occ_bits[i] = 0u;
-        for (int i = tid; i < 2 * g.tiles[kStCell]; i += stride) g.lb_cell[i] = 0ull;
-        for (int i = tid; i < g.tiles[kStResample]; i += stride) g.lb_res[i] = 0ull;
-        if (g.clear_lookback) {
-            const size_t n = (size_t)2 * g.sort_tiles * kSortMaxBins;
-            for (size_t i = tid; i < n; i += stride) g.lb_sort[i] = 0u;
-        }
+        for (int i = tid; i < 2 * g.tiles[kStCell]; i += stride) g.cell_sum[i] = 0ull;
+        for (int i = tid; i < g.tiles[kStResample]; i += stride) g.res_sum[i] = 0ull;
+        // pass-1 digit counts are accumulated by pass 0 (the pass-0 counts are written whole)
+        uint32_t* h1 = g.hsort + (size_t)g.sort_tiles * kSortMaxBins;
+        const size_t n1 = (size_t)g.sort_tiles * kSortMaxBins;
+        for (size_t i = tid; i < n1; i += stride) h1[i] = 0u;
         if (tid == 0) {
             g.fs->status = 0u;
             g.fs->qb_total = 0ull;
@@ -108,8 +108,12 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* bt, int mode) {
         }
         if (mode == 0) {
             __syncthreads();
-            for (int i = threadIdx.x; i < nb0; i += kThreads)
+            // this tile's digit-0 counts (upsweep of sort pass 0: predict and sort tiles coincide)
+            uint32_t* row = g.hsort + (size_t)lt * kSortMaxBins;
+            for (int i = threadIdx.x; i < nb0; i += kThreads) {
+                row[i] = h0[i];
                 if (h0[i]) atomicAdd(&g.hist[i], h0[i]);
+            }
             for (int i = threadIdx.x; i < nb1; i += kThreads)
                 if (h1[i]) atomicAdd(&g.hist[kSortMaxBins + i], h1[i]);
             __syncthreads();
@@ -124,16 +128,12 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* bt, int mode) {
 // An all-zero measurement spreads the particles uniformly (the reference divides by 0).
 // ---------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads) k_init_scan(Batch* bt) {
-    __shared__ int slot;
     __shared__ unsigned long long red[kThreads / 32];
     const int total = batch_total(bt, kStInitScan);
-    for (;;) {
-        const int t = claim_tile(bt, kStInitScan, &slot);
-        if (t >= total) break;
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStInitScan, t);
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][kStInitScan];
-        unsigned long long* lb = g.lb_cell + g.tiles[kStCell];  // second half: init scan
         const int base = lt * kCellTile;
         unsigned long long v = 0ull;
         for (int j = 0; j < kCellIpt; ++j) {
@@ -143,13 +143,7 @@ __global__ void __launch_bounds__(kThreads) k_init_scan(Batch* bt) {
         unsigned long long tile_sum;
         block_excl_scan_u64(v, red, &tile_sum);
         if (threadIdx.x == 0) {
-            if (lt == 0) {
-                st_volatile(lb + lt, kLbInc64 | tile_sum);
-            } else {
-                st_volatile(lb + lt, kLbAgg64 | tile_sum);
-                const unsigned long long excl = lookback64(lb, lt, g);
-                st_volatile(lb + lt, kLbInc64 | (excl + tile_sum));
-            }
+            g.cell_sum[g.tiles[kStCell] + lt] = tile_sum;  // second half: first-frame masses
             atomicAdd(&g.fs->qo_total, tile_sum);
         }
     }
@@ -163,7 +157,6 @@ __global__ void __launch_bounds__(kThreads) k_init_expand(Batch* bt) {
         const int gi = grid_of_tile(bt, kStInitExpand, t);
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][kStInitExpand];
-        const unsigned long long* lb = g.lb_cell + g.tiles[kStCell];
         const unsigned long long T = g.fs->qo_total;
         const bool uniform = (T == 0ull);
         const int base = lt * kCellTile;
@@ -176,9 +169,8 @@ __global__ void __launch_bounds__(kThreads) k_init_expand(Batch* bt) {
         }
         unsigned long long tile_sum;
         unsigned long long pre = block_excl_scan_u64(v, red, &tile_sum);
-        unsigned long long tile_excl = 0ull;
-        if (uniform) tile_excl = (unsigned long long)base;
-        else if (lt > 0) tile_excl = ld_volatile(lb + lt - 1) & kLbVal64;
+        unsigned long long tile_excl = (unsigned long long)base;
+        if (!uniform) tile_excl = block_sum_before(g.cell_sum + g.tiles[kStCell], lt, red);
         const unsigned long long TT = uniform ? (unsigned long long)g.C : T;
         if (threadIdx.x == 0) bnd[0] = alloc_boundary(tile_excl, TT, g.N);
         unsigned long long acc = tile_excl + pre;

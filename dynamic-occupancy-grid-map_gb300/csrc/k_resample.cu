@@ -1,7 +1,10 @@
 // Resampling: one pass over the joint particle array [persistent (sorted) | newborn].
+// The newborns are created here from the compact per-tile lists the newborn kernel wrote
+// (the reference initialises them in initNewParticlesKernel2, init_new_particles.cu:157-195).
 // Replaces the joint concatenation, float scan, random draws, float sort, lower_bound and
 // gather of dogm.cu:386-423 / resampling.cu:17-68.  Joint weights are quantised to
-// 2^-q_shift and scanned exactly (decoupled look-back, integer, order-independent), and
+// 2^-q_shift and scanned exactly (integer, order-independent; a tile's prefix is the sum of the
+// per-tile sums that the cell and newborn kernels accumulated), and
 // systematic resampling assigns output slot i to the joint particle j with
 // A[j-1]*N <= i*T + U < A[j]*N, so each particle writes its own copies directly.
 // The new common weight is T / N (dogm.cu:417).
@@ -13,18 +16,55 @@ struct ResSmem {
     float4 st[kResTile];
     uint32_t kw[kResTile];
     int hi[kResTile];
+    NewbornCell ent[kResTile + 1];   // newborn cells whose slots meet this tile
     unsigned long long red[kThreads / 32];
-    unsigned long long excl;
-    int slot;
+    int nent;
+    int ct_lo, ct_hi;
 };
+
+// Collects (warp 0) the newborn cells whose slot ranges meet [s0, s1) into sm.ent, in slot
+// order.  Cell tile ct owns slots [start[ct], start[ct+1]).
+__device__ void gather_newborn_cells(const GridDesc& g, int s0, int s1, ResSmem& sm) {
+    const int lane = threadIdx.x & 31;
+    const int CT = g.tiles[kStBirth];
+    const int* start = g.nb_tile_start;
+    if (lane == 0) {
+        int a = 0, b = CT - 1;  // largest ct with start[ct] <= s0
+        while (a < b) {
+            const int m = (a + b + 1) >> 1;
+            if (start[m] <= s0) a = m; else b = m - 1;
+        }
+        sm.ct_lo = a;
+        sm.nent = 0;
+    }
+    __syncwarp();
+    for (int ct = sm.ct_lo; ct < CT; ++ct) {
+        if (start[ct] >= s1) break;
+        const int cnt = g.nb_count[ct];
+        const NewbornCell* list = g.nb_list + (size_t)ct * kCellTile;
+        for (int e0 = 0; e0 < cnt; e0 += 32) {
+            const int e = e0 + lane;
+            NewbornCell c;
+            bool take = false;
+            if (e < cnt) {
+                c = list[e];
+                take = c.first < s1 && c.first + c.n > s0;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, take);
+            const int base = sm.nent;
+            if (take) sm.ent[base + __popc(m & ((1u << lane) - 1u))] = c;
+            __syncwarp();
+            if (lane == 0) sm.nent = base + __popc(m);
+            __syncwarp();
+        }
+    }
+}
 
 __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ResSmem& sm = *reinterpret_cast<ResSmem*>(smem_raw);
     const int total = batch_total(bt, kStResample);
-    for (;;) {
-        const int t = claim_tile(bt, kStResample, &sm.slot);
-        if (t >= total) break;
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStResample, t);
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][kStResample];
@@ -32,6 +72,13 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
         const int N = g.N;
         const int M = N + g.fs->n_birth;
         const unsigned long long T = g.fs->joint_total;
+        // newborn slots of this tile
+        const int s0 = max(base, N) - N, s1 = min(base + kResTile, M) - N;
+        if (threadIdx.x < 32) {
+            if (s0 < s1) gather_newborn_cells(g, s0, s1, sm);
+            else if (threadIdx.x == 0) sm.nent = 0;
+        }
+        __syncthreads();
         unsigned long long r64;
         if (g.rp_resample) {
             r64 = *g.rp_resample;
@@ -43,6 +90,7 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
 
         unsigned long long q[kResIpt];
         unsigned long long v = 0ull;
+        const float fgs = (float)g.gs;
 #pragma unroll
         for (int r = 0; r < kResIpt; ++r) {
             const int j = threadIdx.x * kResIpt + r;
@@ -55,10 +103,34 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
                 s = g.S_state[p];
                 w = (kw & kOutBit) ? 0.0f : g.w_cell[kw & kCellMask];
             } else if (p < M) {
+                // newborn slot b: its cell from the compact list (init_new_particles.cu:157-195)
                 const int b = p - N;
-                kw = g.B_key[b];
-                s = g.B_state[b];
-                w = g.B_w[b];
+                int lo = 0, hi = sm.nent - 1;
+                while (lo < hi) {  // last entry with first <= b
+                    const int m = (lo + hi + 1) >> 1;
+                    if (sm.ent[m].first <= b) lo = m; else hi = m - 1;
+                }
+                const NewbornCell c = sm.ent[lo];
+                const int k = c.cell;
+                const bool assoc = (b - c.first) < c.nu_A;
+                float2 z;
+                if (g.rp_birth) {
+                    z = g.rp_birth[b];
+                } else {
+                    const U4 rr = draw_block(g, (uint32_t)b, g.frame, kDrawBirth);
+                    z = box_muller(rr.x, rr.y);
+                }
+                s.x = __fadd_rn((float)(k % g.gs), 0.5f);
+                s.y = __fadd_rn(__fdiv_rn((float)k, fgs), 0.5f);  // float division, as the reference
+                s.z = __fmaf_rn(z.x, g.sigma_birth, 0.0f);
+                s.w = __fmaf_rn(z.y, g.sigma_birth, 0.0f);
+                kw = (uint32_t)k | (assoc ? kAssocBit : 0u);
+                w = assoc ? c.w_A : c.w_UA;
+                if (g.dbg_perm) {  // debug export of the newborns
+                    g.B_state[b] = s;
+                    g.B_key[b] = kw;
+                    g.B_w[b] = w;
+                }
             }
             q[r] = (p < M) ? quantize(w, g.q_shift) : 0ull;
             v += q[r];
@@ -67,20 +139,7 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
         }
         unsigned long long tile_sum;
         const unsigned long long pre = block_excl_scan_u64(v, sm.red, &tile_sum);
-        if (threadIdx.x == 0) {
-            unsigned long long* lb = g.lb_res;
-            unsigned long long excl = 0ull;
-            if (lt == 0) {
-                st_volatile(lb, kLbInc64 | tile_sum);
-            } else {
-                st_volatile(lb + lt, kLbAgg64 | tile_sum);
-                excl = lookback64(lb, lt, g);
-                st_volatile(lb + lt, kLbInc64 | (excl + tile_sum));
-            }
-            sm.excl = excl;
-        }
-        __syncthreads();
-        const unsigned long long tile_excl = sm.excl;
+        const unsigned long long tile_excl = block_sum_before(g.res_sum, lt, sm.red);
         unsigned long long acc = tile_excl + pre;
 #pragma unroll
         for (int r = 0; r < kResIpt; ++r) {

@@ -1,22 +1,80 @@
-// Stable particle-to-cell sort: two LSD radix passes over the cell index (<= 11-bit digits)
-// with decoupled look-back across tiles.  Replaces thrust::sort_by_key with a zip payload
-// (dogm/src/dogm.cu:262-281).  Pass 0 sorts (key, index) by the low digit; pass 1 sorts by
-// the high digit and gathers the predicted particle state into sorted order, so the
-// payload moves once.  Stability makes the permutation identical to the reference's.
+// Stable particle-to-cell sort: two LSD radix passes over the cell index (<= 11-bit digits),
+// reduce-then-scan.  Replaces thrust::sort_by_key with a zip payload (dogm/src/dogm.cu:262-281).
+//   upsweep    pass 0: per-tile digit histograms written by predict (same 4096-particle tiles);
+//              pass 1: counted by pass 0 at the output position of every key
+//   k_sort_scan  column scan of the [tile][digit] histogram -> the global output offset of
+//              every (tile, digit) pair (digit base from predict's global histogram)
+//   k_sort_pass  stable warp ranking inside the tile, scatter to offset + rank; pass 1 also
+//              gathers the predicted particle state, so the payload moves once.
+// Stability makes the permutation identical to the reference's stable sort.
 #include "dogm_device.cuh"
 
 namespace dogm_gb300 {
 
-// Sort look-back word: [31:30] status, [29:24] epoch tag, [23:0] count.
-constexpr uint32_t kSortAgg = 1u << 30;
-constexpr uint32_t kSortInc = 2u << 30;
-constexpr uint32_t kSortCount = (1u << 24) - 1u;
+// ---------------------------------------------------------------------------------------
+// Column scan: for each digit b, O[t][b] = base(b) + sum_{t' < t} H[t'][b], in place.
+// Work item = (grid, group of 32 digits); 32 warps split the tiles into contiguous chunks.
+// ---------------------------------------------------------------------------------------
+constexpr int kScanWarps = 32;
 
+__global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* bt, int pass) {
+    __shared__ uint32_t chunk[kScanWarps][33];
+    __shared__ uint32_t red[kScanWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int stage = pass ? kStScan1 : kStScan0;
+    const int total = batch_total(bt, stage);
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const int gi = grid_of_tile(bt, stage, t);
+        const GridDesc& g = bt->g[gi];
+        const int group = t - bt->prefix[gi][stage];
+        const int nb = 1 << (pass ? g.d1_bits : g.d0_bits);
+        const int b = group * 32 + lane;
+        const uint32_t* hist = g.hist + pass * kSortMaxBins;
+        // digit base: sum of the global histogram over digits < b
+        uint32_t part = 0;
+        for (int i = threadIdx.x; i < group * 32; i += blockDim.x) part += hist[i];
+        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        if (lane == 0) red[warp] = part;
+        __syncthreads();
+        uint32_t base = 0;
+        for (int w = 0; w < kScanWarps; ++w) base += red[w];
+        uint32_t own = (b < nb) ? hist[b] : 0u;
+        uint32_t lanepre = own;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, lanepre, o);
+            if (lane >= o) lanepre += y;
+        }
+        base += lanepre - own;
+        // sweep 1: chunk sums
+        uint32_t* H = g.hsort + (size_t)pass * g.sort_tiles * kSortMaxBins;
+        const int T = g.sort_tiles;
+        const int per = (T + kScanWarps - 1) / kScanWarps;
+        const int t0 = warp * per, t1 = min(T, t0 + per);
+        uint32_t s = 0;
+        if (b < nb)
+            for (int tt = t0; tt < t1; ++tt) s += H[(size_t)tt * kSortMaxBins + b];
+        chunk[warp][lane] = s;
+        __syncthreads();
+        uint32_t pre = base;
+        for (int w = 0; w < warp; ++w) pre += chunk[w][lane];
+        // sweep 2: exclusive offsets in place
+        if (b < nb)
+            for (int tt = t0; tt < t1; ++tt) {
+                uint32_t* p = H + (size_t)tt * kSortMaxBins + b;
+                const uint32_t v = *p;
+                *p = pre;
+                pre += v;
+            }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Downsweep: one tile of 4096 keys per block iteration.
+// ---------------------------------------------------------------------------------------
 struct SortSmem {
     uint16_t whist[kThreads / 32][kSortMaxBins];  // per-warp digit counts, then warp offsets
-    uint32_t gbase[kSortMaxBins];                  // global base of each digit for this tile
-    int scan[kThreads / 32];
-    int slot;
+    uint32_t gbase[kSortMaxBins];                  // global offset of each digit for this tile
 };
 
 template <bool FINAL>
@@ -28,45 +86,22 @@ __global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* bt) {
     const int total = batch_total(bt, stage);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    constexpr int kBinsPerThread = kSortMaxBins / kThreads;
 
-    for (;;) {
-        const int t = claim_tile(bt, stage, &sm.slot);
-        if (t >= total) break;
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, stage, t);
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][stage];
         const int bits = pass ? g.d1_bits : g.d0_bits;
         const int shift = pass ? g.d0_bits : 0;
         const int nb = 1 << bits;
-        const uint32_t epoch = (g.epoch & 63u) << 24;
-        uint32_t* lb_all = g.lb_sort + (size_t)pass * g.sort_tiles * kSortMaxBins;
-
-        // 1. global exclusive digit offsets from the histogram predict accumulated
-        {
-            int v[kBinsPerThread];
-            int s = 0;
-#pragma unroll
-            for (int r = 0; r < kBinsPerThread; ++r) {
-                const int b = threadIdx.x * kBinsPerThread + r;
-                v[r] = (b < nb) ? (int)g.hist[pass * kSortMaxBins + b] : 0;
-                s += v[r];
-            }
-            int tot;
-            int pre = block_excl_scan_i32(s, sm.scan, &tot);
-#pragma unroll
-            for (int r = 0; r < kBinsPerThread; ++r) {
-                const int b = threadIdx.x * kBinsPerThread + r;
-                sm.gbase[b] = (uint32_t)pre;
-                pre += v[r];
-            }
-            for (int i = threadIdx.x; i < (kThreads / 32) * nb; i += kThreads) sm.whist[i / nb][i % nb] = 0;
-        }
+        const uint32_t* O = g.hsort + (size_t)pass * g.sort_tiles * kSortMaxBins + (size_t)lt * kSortMaxBins;
+        for (int i = threadIdx.x; i < nb; i += kThreads) sm.gbase[i] = O[i];
+        for (int i = threadIdx.x; i < (kThreads / 32) * nb; i += kThreads) sm.whist[i / nb][i % nb] = 0;
         __syncthreads();
 
-        // 2. load the tile warp-striped (item k of lane l: warp base + k*32 + l)
+        // load the tile warp-striped (item k of lane l: warp base + k*32 + l)
         const int base = lt * kSortTile + warp * (32 * kSortIpt);
-        uint32_t key[kSortIpt], val[kSortIpt], dig[kSortIpt];
+        uint32_t key[kSortIpt], val[kSortIpt];
         uint16_t rank[kSortIpt];
 #pragma unroll
         for (int k = 0; k < kSortIpt; ++k) {
@@ -74,87 +109,80 @@ __global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* bt) {
             if (pos < g.N) {
                 key[k] = FINAL ? g.T_key[pos] : g.P_key[pos];
                 val[k] = FINAL ? g.T_idx[pos] : (uint32_t)pos;
-                dig[k] = ((key[k] & kCellMask) >> shift) & (uint32_t)(nb - 1);
             } else {
-                key[k] = 0u;
-                val[k] = 0u;
-                dig[k] = 0xffffffffu;
+                key[k] = 0xffffffffu;
+                val[k] = 0xffffffffu;
             }
         }
-        // 3. stable rank within the warp: rounds in input order, peers by match_any
+        // stable rank within the warp: rounds in input order, peers by match_any
 #pragma unroll
         for (int k = 0; k < kSortIpt; ++k) {
-            const uint32_t peers = __match_any_sync(0xffffffffu, dig[k]);
-            const bool valid = dig[k] != 0xffffffffu;
+            const bool valid = val[k] != 0xffffffffu;
+            const uint32_t d = valid ? (((key[k] & kCellMask) >> shift) & (uint32_t)(nb - 1)) : 0xffffffffu;
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
             uint16_t before = 0;
-            if (valid) before = sm.whist[warp][dig[k]];
+            if (valid) before = sm.whist[warp][d];
             rank[k] = (uint16_t)(before + __popc(peers & lt_mask));
             __syncwarp();
-            if (valid && lane == __ffs(peers) - 1) sm.whist[warp][dig[k]] = (uint16_t)(before + __popc(peers));
+            if (valid && lane == __ffs(peers) - 1) sm.whist[warp][d] = (uint16_t)(before + __popc(peers));
             __syncwarp();
         }
         __syncthreads();
-
-        // 4. per digit: warp offsets, tile total, decoupled look-back across tiles
-        uint32_t* lb = lb_all + (size_t)lt * kSortMaxBins;
-        uint32_t tot[kBinsPerThread];
-#pragma unroll
-        for (int r = 0; r < kBinsPerThread; ++r) {
-            const int b = threadIdx.x + r * kThreads;
+        // per digit: exclusive offsets across the warps of the tile
+        for (int b = threadIdx.x; b < nb; b += kThreads) {
             uint32_t acc = 0;
-            if (b < nb) {
 #pragma unroll
-                for (int w = 0; w < kThreads / 32; ++w) {
-                    const uint32_t c = sm.whist[w][b];
-                    sm.whist[w][b] = (uint16_t)acc;
-                    acc += c;
-                }
-                st_volatile(lb + b, (lt == 0 ? kSortInc : kSortAgg) | epoch | acc);
-            }
-            tot[r] = acc;
-        }
-        if (lt > 0) {
-#pragma unroll
-            for (int r = 0; r < kBinsPerThread; ++r) {
-                const int b = threadIdx.x + r * kThreads;
-                if (b >= nb) break;
-                uint32_t excl = 0;
-                int p = lt - 1;
-                int spins = 0;
-                while (p >= 0) {
-                    const uint32_t v = ld_volatile(lb_all + (size_t)p * kSortMaxBins + b);
-                    const bool cur = (v & (63u << 24)) == epoch;
-                    if (cur && (v & kSortInc)) { excl += v & kSortCount; break; }
-                    if (cur && (v & kSortAgg)) { excl += v & kSortCount; --p; continue; }
-                    if (++spins > kSpinLimit) { flag_timeout(g); break; }
-                    __nanosleep(32);
-                }
-                st_volatile(lb + b, kSortInc | epoch | ((excl + tot[r]) & kSortCount));
-                sm.gbase[b] += excl;
+            for (int w = 0; w < kThreads / 32; ++w) {
+                const uint32_t c = sm.whist[w][b];
+                sm.whist[w][b] = (uint16_t)acc;
+                acc += c;
             }
         }
         __syncthreads();
 
-        // 5. scatter to the global sorted position
+        // scatter to the global sorted position; pass 0 also counts the pass-1 histogram
+        uint32_t* H1 = g.hsort + (size_t)g.sort_tiles * kSortMaxBins;
+        const int shift1 = g.d0_bits;
+        const uint32_t nb1m = (1u << g.d1_bits) - 1u;
 #pragma unroll
         for (int k = 0; k < kSortIpt; ++k) {
-            if (dig[k] == 0xffffffffu) continue;
-            const uint32_t out = sm.gbase[dig[k]] + sm.whist[warp][dig[k]] + rank[k];
-            if (out >= (uint32_t)g.N) {  // only a corrupted histogram can get here
-                flag_status(g, kStatusBounds);
-                continue;
+            const bool valid = val[k] != 0xffffffffu;
+            uint32_t out = 0xffffffffu;
+            if (valid) {
+                const uint32_t d = ((key[k] & kCellMask) >> shift) & (uint32_t)(nb - 1);
+                out = sm.gbase[d] + sm.whist[warp][d] + rank[k];
+                if (out >= (uint32_t)g.N) {  // only an inconsistent histogram can get here
+                    flag_status(g, kStatusBounds);
+                    out = 0xffffffffu;
+                }
             }
             if (FINAL) {
-                g.S_key[out] = key[k];
-                g.S_state[out] = g.P_state[val[k]];
-                if (g.dbg_perm) g.dbg_perm[out] = (int)val[k];
+                if (out != 0xffffffffu) {
+                    g.S_key[out] = key[k];
+                    g.S_state[out] = g.P_state[val[k]];
+                    if (g.dbg_perm) g.dbg_perm[out] = (int)val[k];
+                }
             } else {
-                g.T_key[out] = key[k];
-                g.T_idx[out] = val[k];
+                uint32_t hk = 0xffffffffu;
+                if (out != 0xffffffffu) {
+                    g.T_key[out] = key[k];
+                    g.T_idx[out] = val[k];
+                    const uint32_t d1 = ((key[k] & kCellMask) >> shift1) & nb1m;
+                    hk = ((out / (uint32_t)kSortTile) << kSortMaxBits) | d1;
+                }
+                const uint32_t peers = __match_any_sync(0xffffffffu, hk);
+                if (hk != 0xffffffffu && lane == __ffs(peers) - 1)
+                    atomicAdd(&H1[(size_t)(hk >> kSortMaxBits) * kSortMaxBins + (hk & (kSortMaxBins - 1))],
+                              (uint32_t)__popc(peers));
             }
         }
         __syncthreads();
     }
+}
+
+cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
+    k_sort_scan<<<cfg.num_sms, kScanWarps * 32, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), pass);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
@@ -168,8 +196,10 @@ cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cf
 }
 
 cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg) {
-    cudaError_t e = launch_sort_pass(d_batch, 0, cfg);
-    if (e != cudaSuccess) return e;
+    cudaError_t e;
+    if ((e = launch_sort_scan(d_batch, 0, cfg)) != cudaSuccess) return e;
+    if ((e = launch_sort_pass(d_batch, 0, cfg)) != cudaSuccess) return e;
+    if ((e = launch_sort_scan(d_batch, 1, cfg)) != cudaSuccess) return e;
     return launch_sort_pass(d_batch, 1, cfg);
 }
 

@@ -38,9 +38,9 @@ int bitlen(unsigned long long v) {
 
 int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-constexpr int kStages = 8;  // frame-begin, predict, sort 0, sort 1, segments, cells, newborn, resample
-const char* const kStageNames[kStages] = {"frame_begin", "predict", "sort_pass0", "sort_pass1",
-                                          "segments",    "cells",   "newborn",    "resample"};
+constexpr int kStages = 10;
+const char* const kStageNames[kStages] = {"frame_begin", "predict",  "sort_scan0", "sort_pass0", "sort_scan1",
+                                          "sort_pass1",  "segments", "cells",      "newborn",    "resample"};
 
 // One launch context: a device copy of a Batch, two pinned host mirrors (the host fills one
 // while the device may still read the other, so frame k+1 is queued while frame k runs) and
@@ -141,7 +141,7 @@ dogm_status dalloc(dogm_handle* h, T** p, size_t count) {
 }
 
 struct Sizes {
-    int gs, N, B, C, key_bits, sort_tiles, seg_tiles, cell_tiles, res_tiles, pred_tiles;
+    int gs, N, B, C, key_bits, sort_tiles, seg_tiles, cell_tiles, res_tiles, pred_tiles, scan0, scan1;
 };
 
 dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
@@ -161,13 +161,18 @@ dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
     s.seg_tiles = div_up(s.N, kSegTile);
     s.cell_tiles = div_up(s.C, kCellTile);
     s.res_tiles = div_up((long long)s.N + s.B, kResTile);
+    const int d0 = (s.key_bits + 1) / 2, d1 = s.key_bits - d0;
+    s.scan0 = div_up(1 << d0, 32);  // digit groups of the column scans
+    s.scan1 = div_up(1 << d1, 32);
     return DOGM_OK;
 }
 
 void set_tiles(GridDesc& g, const Sizes& s) {
     for (int i = 0; i < kNumStages; ++i) g.tiles[i] = 0;
     g.tiles[kStPredict] = s.pred_tiles;
+    g.tiles[kStScan0] = s.scan0;
     g.tiles[kStSort0] = s.sort_tiles;
+    g.tiles[kStScan1] = s.scan1;
     g.tiles[kStSort1] = s.sort_tiles;
     g.tiles[kStSeg] = s.seg_tiles;
     g.tiles[kStCell] = s.cell_tiles;
@@ -216,8 +221,6 @@ void fill_frame(dogm_handle* h, float dt, int shifted, int xm, int ym, const dog
     g.meas_src = meas_src;
     g.copy_meas = copy_meas;
     g.frame = (uint32_t)h->iteration;
-    g.epoch = (uint32_t)(h->iteration & 63);
-    g.clear_lookback = (h->need_clear || (h->iteration & 63) == 0) ? 1 : 0;
     g.rp_init = h->rp_init;
     g.rp_predict = h->rp_predict;
     g.rp_birth = h->rp_birth;
@@ -271,12 +274,14 @@ cudaError_t frame_kernels(Ctx& c, bool with_init) {
     STAGE(0, launch_frame_begin(c.d_batch, 0, cfg));
     if (with_init && (e = launch_init_particles(c.d_batch, cfg)) != cudaSuccess) return e;
     STAGE(1, launch_predict(c.d_batch, 0, cfg));
-    STAGE(2, launch_sort_pass(c.d_batch, 0, cfg));
-    STAGE(3, launch_sort_pass(c.d_batch, 1, cfg));
-    STAGE(4, launch_segments(c.d_batch, cfg));
-    STAGE(5, launch_cells(c.d_batch, cfg));
-    STAGE(6, launch_newborn(c.d_batch, cfg));
-    STAGE(7, launch_resample(c.d_batch, cfg));
+    STAGE(2, launch_sort_scan(c.d_batch, 0, cfg));
+    STAGE(3, launch_sort_pass(c.d_batch, 0, cfg));
+    STAGE(4, launch_sort_scan(c.d_batch, 1, cfg));
+    STAGE(5, launch_sort_pass(c.d_batch, 1, cfg));
+    STAGE(6, launch_segments(c.d_batch, cfg));
+    STAGE(7, launch_cells(c.d_batch, cfg));
+    STAGE(8, launch_newborn(c.d_batch, cfg));
+    STAGE(9, launch_resample(c.d_batch, cfg));
 #undef STAGE
     if (prof && (e = cudaEventRecord(c.ev[kStages], c.stream)) != cudaSuccess) return e;
     return cudaSuccess;
@@ -412,9 +417,12 @@ size_t dogm_state_bytes(const dogm_params* p) {
     size_t b = 0;
     b += N * (16 + 4) + N * (4 + 4) + N * (16 + 4);    // P, T, S particles
     b += B * (16 + 4 + 4);                            // newborns
-    b += C * (sizeof(dogm_grid_cell) + 2 * sizeof(dogm_measurement_cell) / 2 * 2 / 2 + 4 * 2 + 32 + 4 + 4) + C / 8;
+    // per cell: record 64, measurement copy 16, free mass 2 x 4, segment sums 32, newborn
+    // mass 4, cell weight 4, occupancy bit
+    b += C * (sizeof(dogm_grid_cell) + sizeof(dogm_measurement_cell) + 2 * 4 + 32 + 4 + 4) + C / 8;
     b += 2 * kSortMaxBins * 4 + (size_t)2 * s.sort_tiles * kSortMaxBins * 4;
     b += (size_t)s.seg_tiles * 2 * sizeof(SegSums) + (size_t)s.cell_tiles * 16 + (size_t)s.res_tiles * 8;
+    b += (size_t)s.cell_tiles * (kCellTile * sizeof(NewbornCell) + 8);
     b += sizeof(Batch);
     return b;
 }
@@ -468,10 +476,13 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     ALLOC(g.rho_b, s.C); ALLOC(g.w_cell, s.C);
     ALLOC(g.occ_bits, (s.C + 31) / 32);
     ALLOC(g.hist, 2 * kSortMaxBins);
-    ALLOC(g.lb_sort, (size_t)2 * s.sort_tiles * kSortMaxBins);
+    ALLOC(g.hsort, (size_t)2 * s.sort_tiles * kSortMaxBins);
     ALLOC(g.seg_head, s.seg_tiles); ALLOC(g.seg_tail, s.seg_tiles);
-    ALLOC(g.lb_cell, 2 * (size_t)s.cell_tiles);
-    ALLOC(g.lb_res, s.res_tiles);
+    ALLOC(g.cell_sum, 2 * (size_t)s.cell_tiles);
+    ALLOC(g.res_sum, s.res_tiles);
+    ALLOC(g.nb_list, (size_t)s.cell_tiles * kCellTile);
+    ALLOC(g.nb_count, s.cell_tiles);
+    ALLOC(g.nb_tile_start, (size_t)s.cell_tiles + 1);
     ALLOC(g.fs, 1);
 #undef ALLOC
     // measurement cells start as in initGridCellsKernel (init.cu:65-80): no evidence,
