@@ -278,19 +278,21 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* bt) {
 // the tile's newborn cells (the resample kernel creates the newborns from it) and the
 // newborns' quantised weights into the resample tiles that will hold them.
 // ---------------------------------------------------------------------------------------
-__device__ __forceinline__ void add_joint_range(unsigned long long* res_sum, long long a, long long b,
+__device__ __forceinline__ void add_joint_range(TileAgg& agg, unsigned long long* res_sum, long long a, long long b,
                                                 unsigned long long q) {
     if (q == 0ull) return;
     for (long long t = a / kResTile; t * kResTile < b; ++t) {
         const long long lo = max(a, t * (long long)kResTile);
         const long long hi = min(b, (t + 1) * (long long)kResTile);
-        if (hi > lo) atomicAdd(&res_sum[t], (unsigned long long)(hi - lo) * q);
+        if (hi > lo) agg_add(agg, res_sum, t, (unsigned long long)(hi - lo) * q);
     }
 }
 
 __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
     __shared__ unsigned long long red[kThreads / 32];
     __shared__ int iscan[kThreads / 32];
+    __shared__ TileAgg agg;
+    __shared__ int s_first;
     const int total = batch_total(bt, kStBirth);
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStBirth, t);
@@ -312,7 +314,13 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
         unsigned long long tile_sum;
         unsigned long long acc = E + block_excl_scan_u64(v, red, &tile_sum);
         int lo_c = alloc_boundary(acc, T, g.B);
-        if (threadIdx.x == 0) g.nb_tile_start[lt] = lo_c;
+        if (threadIdx.x == 0) {
+            g.nb_tile_start[lt] = lo_c;
+            s_first = lo_c;
+        }
+        __syncthreads();
+        agg_reset(agg, ((long long)g.N + s_first) / kResTile);
+        __syncthreads();
         int bnd[kCellIpt + 1];
         bnd[0] = lo_c;
         int nflag = 0;
@@ -345,12 +353,13 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
                 const int nA = min(max(nuA, 0), nnew);
                 const unsigned long long qA = quantize(wA, g.q_shift), qU = quantize(wUA, g.q_shift);
                 jq += (unsigned long long)nA * qA + (unsigned long long)(nnew - nA) * qU;
-                add_joint_range(g.res_sum, N + bnd[j], N + bnd[j] + nA, qA);
-                add_joint_range(g.res_sum, N + bnd[j] + nA, N + bnd[j + 1], qU);
+                add_joint_range(agg, g.res_sum, N + bnd[j], N + bnd[j] + nA, qA);
+                add_joint_range(agg, g.res_sum, N + bnd[j] + nA, N + bnd[j + 1], qU);
             }
         }
         unsigned long long tile_jq;
-        block_excl_scan_u64(jq, red, &tile_jq);
+        block_excl_scan_u64(jq, red, &tile_jq);  // (its barriers also order the shared adds)
+        agg_flush(agg, g.res_sum, g.tiles[kStResample]);
         if (threadIdx.x == 0) {
             g.nb_count[lt] = ntile;
             if (tile_jq) atomicAdd(&g.fs->joint_total, tile_jq);

@@ -15,15 +15,19 @@ namespace dogm_gb300 {
 struct ResSmem {
     float4 st[kResTile];
     uint32_t kw[kResTile];
-    int hi[kResTile];
-    NewbornCell ent[kResTile + 1];   // newborn cells whose slots meet this tile
+    union {
+        float w[kResTile];   // phase 1: weight of each item
+        int hi[kResTile];    // phase 2: end of each item's output slots
+    } u;
+    int ent_first[kResTile + 1];   // newborn cells whose slots meet this tile: first slot,
+    int2 ent_cell[kResTile + 1];   // and {cell, associated slots}
     unsigned long long red[kThreads / 32];
     int nent;
-    int ct_lo, ct_hi;
+    int ct_lo;
 };
 
-// Collects (warp 0) the newborn cells whose slot ranges meet [s0, s1) into sm.ent, in slot
-// order.  Cell tile ct owns slots [start[ct], start[ct+1]).
+// Collects (warp 0) the newborn cells whose slot ranges meet [s0, s1), in slot order.
+// Cell tile ct owns slots [start[ct], start[ct+1]).
 __device__ void gather_newborn_cells(const GridDesc& g, int s0, int s1, ResSmem& sm) {
     const int lane = threadIdx.x & 31;
     const int CT = g.tiles[kStBirth];
@@ -52,9 +56,15 @@ __device__ void gather_newborn_cells(const GridDesc& g, int s0, int s1, ResSmem&
             }
             const unsigned m = __ballot_sync(0xffffffffu, take);
             const int base = sm.nent;
-            if (take) sm.ent[base + __popc(m & ((1u << lane) - 1u))] = c;
+            if (take) {
+                const int i = base + __popc(m & ((1u << lane) - 1u));
+                if (i <= kResTile) {
+                    sm.ent_first[i] = c.first;
+                    sm.ent_cell[i] = make_int2(c.cell, c.nu_A);
+                }
+            }
             __syncwarp();
-            if (lane == 0) sm.nent = base + __popc(m);
+            if (lane == 0) sm.nent = min(base + __popc(m), kResTile + 1);
             __syncwarp();
         }
     }
@@ -72,8 +82,7 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
         const int N = g.N;
         const int M = N + g.fs->n_birth;
         const unsigned long long T = g.fs->joint_total;
-        // newborn slots of this tile
-        const int s0 = max(base, N) - N, s1 = min(base + kResTile, M) - N;
+        const int s0 = max(base, N) - N, s1 = min(base + kResTile, M) - N;  // newborn slots here
         if (threadIdx.x < 32) {
             if (s0 < s1) gather_newborn_cells(g, s0, s1, sm);
             else if (threadIdx.x == 0) sm.nent = 0;
@@ -87,13 +96,10 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
             r64 = ((unsigned long long)r.x << 32) | r.y;
         }
         const unsigned long long U = __umul64hi(r64, T);  // floor(u * T), u = r64 / 2^64
-
-        unsigned long long q[kResIpt];
-        unsigned long long v = 0ull;
         const float fgs = (float)g.gs;
-#pragma unroll
-        for (int r = 0; r < kResIpt; ++r) {
-            const int j = threadIdx.x * kResIpt + r;
+
+        // phase 1 (striped, coalesced): stage every joint item of the tile
+        for (int j = threadIdx.x; j < kResTile; j += kThreads) {
             const int p = base + j;
             float w = 0.0f;
             float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -108,11 +114,11 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
                 int lo = 0, hi = sm.nent - 1;
                 while (lo < hi) {  // last entry with first <= b
                     const int m = (lo + hi + 1) >> 1;
-                    if (sm.ent[m].first <= b) lo = m; else hi = m - 1;
+                    if (sm.ent_first[m] <= b) lo = m; else hi = m - 1;
                 }
-                const NewbornCell c = sm.ent[lo];
-                const int k = c.cell;
-                const bool assoc = (b - c.first) < c.nu_A;
+                const int2 c = sm.ent_cell[lo];
+                const int k = min(max(c.x, 0), g.C - 1);
+                const bool assoc = (b - sm.ent_first[lo]) < c.y;
                 float2 z;
                 if (g.rp_birth) {
                     z = g.rp_birth[b];
@@ -125,17 +131,26 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
                 s.z = __fmaf_rn(z.x, g.sigma_birth, 0.0f);
                 s.w = __fmaf_rn(z.y, g.sigma_birth, 0.0f);
                 kw = (uint32_t)k | (assoc ? kAssocBit : 0u);
-                w = assoc ? c.w_A : c.w_UA;
+                w = assoc ? g.cells[k].w_A : g.cells[k].w_UA;
                 if (g.dbg_perm) {  // debug export of the newborns
                     g.B_state[b] = s;
                     g.B_key[b] = kw;
                     g.B_w[b] = w;
                 }
             }
-            q[r] = (p < M) ? quantize(w, g.q_shift) : 0ull;
-            v += q[r];
             sm.st[j] = s;
             sm.kw[j] = kw & ~kOutBit;
+            sm.u.w[j] = (p < M) ? w : 0.0f;
+        }
+        __syncthreads();
+
+        // phase 2 (blocked): exact prefix of the quantised weights, output slot ranges
+        unsigned long long q[kResIpt];
+        unsigned long long v = 0ull;
+#pragma unroll
+        for (int r = 0; r < kResIpt; ++r) {
+            q[r] = quantize(sm.u.w[threadIdx.x * kResIpt + r], g.q_shift);
+            v += q[r];
         }
         unsigned long long tile_sum;
         const unsigned long long pre = block_excl_scan_u64(v, sm.red, &tile_sum);
@@ -143,18 +158,17 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
         unsigned long long acc = tile_excl + pre;
 #pragma unroll
         for (int r = 0; r < kResIpt; ++r) {
-            const int j = threadIdx.x * kResIpt + r;
             acc += q[r];
-            sm.hi[j] = comb_count(acc, T, U, N);
+            sm.u.hi[threadIdx.x * kResIpt + r] = comb_count(acc, T, U, N);
         }
         __syncthreads();
         const int lo = (base == 0) ? 0 : comb_count(tile_excl, T, U, N);
-        const int hi = sm.hi[kResTile - 1];
+        const int hi = sm.u.hi[kResTile - 1];
         for (int s = lo + threadIdx.x; s < hi; s += kThreads) {
             int a = 0, b = kResTile - 1;  // first item with hi > s
             while (a < b) {
                 const int m = (a + b) >> 1;
-                if (sm.hi[m] > s) b = m; else a = m + 1;
+                if (sm.u.hi[m] > s) b = m; else a = m + 1;
             }
             g.P_state[s] = sm.st[a];
             g.P_key[s] = sm.kw[a];
@@ -174,7 +188,7 @@ cudaError_t prepare_kernels() {
 
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg) {
     const int smem = (int)sizeof(ResSmem);
-    k_resample<<<cfg.num_sms * 2, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_resample<<<cfg.num_sms * 3, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 
