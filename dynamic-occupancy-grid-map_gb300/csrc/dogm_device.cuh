@@ -72,16 +72,20 @@ __device__ __forceinline__ unsigned long long quantize(float w, int S) {
     return q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
 }
 
-struct U128 { unsigned long long hi, lo; };
-__device__ __forceinline__ U128 mul64(unsigned long long a, unsigned long long b) {
-    return U128{__umul64hi(a, b), a * b};
+// 96-bit products of a 64-bit and a 32-bit factor (every product here is below 2^86:
+// weights < 2^62 times counts < 2^24).
+struct U96 { unsigned long long lo; unsigned int hi; };
+__device__ __forceinline__ U96 mul_u64_u32(unsigned long long a, unsigned int b) {
+    const unsigned long long p0 = (unsigned long long)(unsigned int)a * b;
+    const unsigned long long p1 = (a >> 32) * b;
+    const unsigned long long lo = p0 + (p1 << 32);
+    return U96{lo, (unsigned int)(p1 >> 32) + (lo < p0 ? 1u : 0u)};
 }
-__device__ __forceinline__ U128 add64(U128 a, unsigned long long b) {
-    const unsigned long long lo = a.lo + b;
-    return U128{a.hi + (lo < a.lo ? 1ull : 0ull), lo};
+__device__ __forceinline__ U96 add96(U96 a, unsigned long long x) {
+    const unsigned long long lo = a.lo + x;
+    return U96{lo, a.hi + (lo < a.lo ? 1u : 0u)};
 }
-__device__ __forceinline__ bool lt128(U128 a, U128 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
-__device__ __forceinline__ bool le128(U128 a, U128 b) { return !lt128(b, a); }
+__device__ __forceinline__ bool lt96(U96 a, U96 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 
 // floor(Q * M / T) for Q <= T, T > 0: how many of M slots a prefix mass Q owns.
 // (The reference scales a float prefix sum by M / total and truncates:
@@ -89,12 +93,13 @@ __device__ __forceinline__ bool le128(U128 a, U128 b) { return !lt128(b, a); }
 __device__ __forceinline__ int alloc_boundary(unsigned long long Q, unsigned long long T, int M) {
     if (T == 0ull) return 0;
     if (Q >= T) return M;
-    const U128 qm = mul64(Q, (unsigned long long)M);
-    float f = ((float)Q / (float)T) * (float)M;
-    int b = (int)floorf(f);
+    const U96 qm = mul_u64_u32(Q, (unsigned int)M);
+    const float f = __fmul_rn(__fdiv_rn(__ull2float_rn(Q), __ull2float_rn(T)), (float)M);
+    int b = (int)f;
     b = b < 0 ? 0 : (b > M ? M : b);
-    while (b > 0 && lt128(qm, mul64((unsigned long long)b, T))) --b;
-    while (b < M && le128(mul64((unsigned long long)(b + 1), T), qm)) ++b;
+    // b = largest value with b*T <= Q*M
+    while (b > 0 && lt96(qm, mul_u64_u32(T, (unsigned int)b))) --b;
+    while (b < M && !lt96(qm, mul_u64_u32(T, (unsigned int)(b + 1)))) ++b;
     return b;
 }
 
@@ -104,13 +109,14 @@ __device__ __forceinline__ int alloc_boundary(unsigned long long Q, unsigned lon
 __device__ __forceinline__ int comb_count(unsigned long long a, unsigned long long T, unsigned long long U, int N) {
     if (T == 0ull) return N;
     if (a >= T) return N;
-    const U128 rhs = mul64(a, (unsigned long long)N);
-    float f = ((float)a * (float)N - (float)U) / (float)T;
+    const U96 rhs = mul_u64_u32(a, (unsigned int)N);
+    const float f = __fdiv_rn(__fsub_rn(__fmul_rn(__ull2float_rn(a), (float)N), __ull2float_rn(U)),
+                              __ull2float_rn(T));
     int c = (int)ceilf(f);
     c = c < 0 ? 0 : (c > N ? N : c);
-    // P(i): i*T + U < a*N is true for i < result, false from result on.
-    while (c > 0 && !lt128(add64(mul64((unsigned long long)(c - 1), T), U), rhs)) --c;
-    while (c < N && lt128(add64(mul64((unsigned long long)c, T), U), rhs)) ++c;
+    // P(i): i*T + U < a*N holds for i < result and fails from result on
+    while (c > 0 && !lt96(add96(mul_u64_u32(T, (unsigned int)(c - 1)), U), rhs)) --c;
+    while (c < N && lt96(add96(mul_u64_u32(T, (unsigned int)c), U), rhs)) ++c;
     return c;
 }
 
@@ -230,6 +236,44 @@ __device__ __forceinline__ unsigned long long block_sum_before(const unsigned lo
     unsigned long long total;
     block_excl_scan_u64(v, scratch, &total);
     return total;
+}
+
+// Exclusive scan of one 64-bit value per thread, offset by sums[0 .. t) (the per-tile sums a
+// previous kernel completed): returns sums[0..t) + (exclusive prefix of v); *total gets the
+// block's sum of v.  One barrier round for both.
+__device__ __forceinline__ unsigned long long block_scan_after(unsigned long long v, const unsigned long long* sums,
+                                                               int t, unsigned long long* scratch16,
+                                                               unsigned long long* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long part = 0ull;
+    for (int i = threadIdx.x; i < t; i += blockDim.x) part += sums[i];
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+        part += __shfl_xor_sync(0xffffffffu, part, o);
+    }
+    if (lane == 31) scratch16[warp] = x;
+    if (lane == 0) scratch16[8 + warp] = part;
+    __syncthreads();
+    unsigned long long wpre = 0ull, tot = 0ull, before = 0ull;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+        const unsigned long long s = scratch16[w];
+        if (w < warp) wpre += s;
+        tot += s;
+        before += scratch16[8 + w];
+    }
+    __syncthreads();
+    *total = tot;
+    return before + wpre + x - v;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
 // Per-block accumulation of exact integer sums into a window of consecutive global

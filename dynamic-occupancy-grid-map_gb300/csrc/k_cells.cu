@@ -289,7 +289,7 @@ __device__ __forceinline__ void add_joint_range(TileAgg& agg, unsigned long long
 }
 
 __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
-    __shared__ unsigned long long red[kThreads / 32];
+    __shared__ unsigned long long red[2 * (kThreads / 32)];
     __shared__ int iscan[kThreads / 32];
     __shared__ TileAgg agg;
     __shared__ int s_first;
@@ -300,7 +300,6 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
         const int lt = t - bt->prefix[gi][kStBirth];
         const int base = lt * kCellTile;
         const unsigned long long T = g.fs->qb_total;
-        const unsigned long long E = block_sum_before(g.cell_sum, lt, red);
         unsigned long long q[kCellIpt];
         float rb[kCellIpt];
         unsigned long long v = 0ull;
@@ -312,7 +311,7 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
             v += q[j];
         }
         unsigned long long tile_sum;
-        unsigned long long acc = E + block_excl_scan_u64(v, red, &tile_sum);
+        unsigned long long acc = block_scan_after(v, g.cell_sum, lt, red, &tile_sum);
         int lo_c = alloc_boundary(acc, T, g.B);
         if (threadIdx.x == 0) {
             g.nb_tile_start[lt] = lo_c;
@@ -327,7 +326,7 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
             acc += q[j];
-            bnd[j + 1] = alloc_boundary(acc, T, g.B);
+            bnd[j + 1] = q[j] ? alloc_boundary(acc, T, g.B) : bnd[j];
             nflag += (bnd[j + 1] > bnd[j]) ? 1 : 0;
         }
         int ntile;
@@ -357,12 +356,12 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
                 add_joint_range(agg, g.res_sum, N + bnd[j] + nA, N + bnd[j + 1], qU);
             }
         }
-        unsigned long long tile_jq;
-        block_excl_scan_u64(jq, red, &tile_jq);  // (its barriers also order the shared adds)
+        jq = warp_sum_u64(jq);
+        if ((threadIdx.x & 31) == 0 && jq) atomicAdd(&g.fs->joint_total, jq);
+        __syncthreads();  // every shared add is done
         agg_flush(agg, g.res_sum, g.tiles[kStResample]);
         if (threadIdx.x == 0) {
             g.nb_count[lt] = ntile;
-            if (tile_jq) atomicAdd(&g.fs->joint_total, tile_jq);
             if (lt == 0) g.fs->n_birth = (T > 0ull) ? g.B : 0;
             if (lt == g.tiles[kStBirth] - 1) g.nb_tile_start[lt + 1] = (T > 0ull) ? g.B : 0;
         }

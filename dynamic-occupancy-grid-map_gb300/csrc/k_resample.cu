@@ -16,15 +16,21 @@ struct ResSmem {
     float4 st[kResTile];
     uint32_t kw[kResTile];
     union {
-        float w[kResTile];   // phase 1: weight of each item
-        int hi[kResTile];    // phase 2: end of each item's output slots
+        float w[kResTile];   // weight of each item
     } u;
-    int ent_first[kResTile + 1];   // newborn cells whose slots meet this tile: first slot,
-    int2 ent_cell[kResTile + 1];   // and {cell, associated slots}
-    unsigned long long red[kThreads / 32];
+    union {
+        struct {                       // phase 1: newborn cells whose slots meet this tile
+            int first[kResTile + 1];   // first slot
+            int2 cell[kResTile + 1];   // {cell, associated slots}
+        } ent;
+        int3 heavy[kResTile];          // phase 2: items with many copies {item, first, end slot}
+    } x;
+    unsigned long long red[2 * (kThreads / 32)];
     int nent;
     int ct_lo;
+    int nheavy;
 };
+constexpr int kOwnCopies = 8;        // an item writes up to this many copies itself
 
 // Collects (warp 0) the newborn cells whose slot ranges meet [s0, s1), in slot order.
 // Cell tile ct owns slots [start[ct], start[ct+1]).
@@ -59,8 +65,8 @@ __device__ void gather_newborn_cells(const GridDesc& g, int s0, int s1, ResSmem&
             if (take) {
                 const int i = base + __popc(m & ((1u << lane) - 1u));
                 if (i <= kResTile) {
-                    sm.ent_first[i] = c.first;
-                    sm.ent_cell[i] = make_int2(c.cell, c.nu_A);
+                    sm.x.ent.first[i] = c.first;
+                    sm.x.ent.cell[i] = make_int2(c.cell, c.nu_A);
                 }
             }
             __syncwarp();
@@ -114,11 +120,11 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
                 int lo = 0, hi = sm.nent - 1;
                 while (lo < hi) {  // last entry with first <= b
                     const int m = (lo + hi + 1) >> 1;
-                    if (sm.ent_first[m] <= b) lo = m; else hi = m - 1;
+                    if (sm.x.ent.first[m] <= b) lo = m; else hi = m - 1;
                 }
-                const int2 c = sm.ent_cell[lo];
+                const int2 c = sm.x.ent.cell[lo];
                 const int k = min(max(c.x, 0), g.C - 1);
-                const bool assoc = (b - sm.ent_first[lo]) < c.y;
+                const bool assoc = (b - sm.x.ent.first[lo]) < c.y;
                 float2 z;
                 if (g.rp_birth) {
                     z = g.rp_birth[b];
@@ -153,26 +159,41 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
             v += q[r];
         }
         unsigned long long tile_sum;
-        const unsigned long long pre = block_excl_scan_u64(v, sm.red, &tile_sum);
-        const unsigned long long tile_excl = block_sum_before(g.res_sum, lt, sm.red);
-        unsigned long long acc = tile_excl + pre;
+        unsigned long long acc = block_scan_after(v, g.res_sum, lt, sm.red, &tile_sum);
+        if (threadIdx.x == 0) sm.nheavy = 0;
+        // output slots [lo, hi) of each of this thread's items; the first item's lo is the
+        // comb count of everything before it
+        int lo_s = (base + threadIdx.x * kResIpt == 0) ? 0 : comb_count(acc, T, U, N);
+        __syncthreads();
 #pragma unroll
         for (int r = 0; r < kResIpt; ++r) {
+            const int j = threadIdx.x * kResIpt + r;
             acc += q[r];
-            sm.u.hi[threadIdx.x * kResIpt + r] = comb_count(acc, T, U, N);
+            const int hi_s = comb_count(acc, T, U, N);
+            if (hi_s - lo_s <= kOwnCopies) {
+                const float4 st = sm.st[j];
+                const uint32_t kw = sm.kw[j];
+                for (int s = lo_s; s < hi_s; ++s) {
+                    g.P_state[s] = st;
+                    g.P_key[s] = kw;
+                    if (g.dbg_src) g.dbg_src[s] = base + j;
+                }
+            } else {
+                const int h = atomicAdd(&sm.nheavy, 1);
+                sm.x.heavy[h] = make_int3(j, lo_s, hi_s);
+            }
+            lo_s = hi_s;
         }
         __syncthreads();
-        const int lo = (base == 0) ? 0 : comb_count(tile_excl, T, U, N);
-        const int hi = sm.u.hi[kResTile - 1];
-        for (int s = lo + threadIdx.x; s < hi; s += kThreads) {
-            int a = 0, b = kResTile - 1;  // first item with hi > s
-            while (a < b) {
-                const int m = (a + b) >> 1;
-                if (sm.u.hi[m] > s) b = m; else a = m + 1;
+        for (int h = 0; h < sm.nheavy; ++h) {
+            const int3 e = sm.x.heavy[h];
+            const float4 st = sm.st[e.x];
+            const uint32_t kw = sm.kw[e.x];
+            for (int s = e.y + threadIdx.x; s < e.z; s += kThreads) {
+                g.P_state[s] = st;
+                g.P_key[s] = kw;
+                if (g.dbg_src) g.dbg_src[s] = base + e.x;
             }
-            g.P_state[s] = sm.st[a];
-            g.P_key[s] = sm.kw[a];
-            if (g.dbg_src) g.dbg_src[s] = base + a;
         }
         if (lt == 0 && threadIdx.x == 0) {
             const float jf = ldexpf(__ull2float_rn(T), -g.q_shift);
