@@ -29,6 +29,7 @@ struct ResSmem {
     int nent;
     int ct_lo;
     int nheavy;
+    int claim;
 };
 constexpr int kOwnCopies = 8;        // an item writes up to this many copies itself
 
@@ -80,7 +81,12 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ResSmem& sm = *reinterpret_cast<ResSmem*>(smem_raw);
     const int total = batch_total(bt, kStResample);
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    // tiles are taken dynamically from the end: the newborn tiles (last in the joint order,
+    // with the heaviest copy counts) start first and the light tiles fill in around them
+    for (;;) {
+        const int c = claim_tile(bt, kStResample, &sm.claim);
+        if (c >= total) break;
+        const int t = total - 1 - c;
         const int gi = grid_of_tile(bt, kStResample, t);
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][kStResample];
