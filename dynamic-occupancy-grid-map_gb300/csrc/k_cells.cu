@@ -77,7 +77,7 @@ __device__ __forceinline__ SegRun seg_item(uint32_t kw, float4 st, bool head, in
 // loads; thread i reduces items [i*kSegIpt, (i+1)*kSegIpt) in order, then a block-wide
 // segmented scan joins the threads.  The combine order depends only on positions, so the
 // sums are deterministic.
-__global__ void __launch_bounds__(kThreads) k_segments(Batch* bt) {
+__global__ void __launch_bounds__(kThreads) k_segments(Batch* __restrict__ bt) {
     __shared__ uint32_t skey[kSegTile + 2];
     __shared__ float2 svel[kSegTile];
     __shared__ SegRun wagg[kThreads / 32];
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(kThreads) k_segments(Batch* bt) {
 // ---------------------------------------------------------------------------------------
 // Fused per-cell update.
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_cells(Batch* bt) {
+__global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
     __shared__ unsigned long long red[kThreads / 32];
     __shared__ unsigned long long red2[kThreads / 32];
     const int total = batch_total(bt, kStCell);
@@ -288,7 +288,7 @@ __device__ __forceinline__ void add_joint_range(TileAgg& agg, unsigned long long
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_newborn(Batch* bt) {
+__global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
     __shared__ unsigned long long red[2 * (kThreads / 32)];
     __shared__ int iscan[kThreads / 32];
     __shared__ TileAgg agg;

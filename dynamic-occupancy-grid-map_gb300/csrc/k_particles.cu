@@ -7,7 +7,7 @@ namespace dogm_gb300 {
 // ---------------------------------------------------------------------------------------
 // Frame begin: zero the per-frame scratch of every grid in the batch.
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* bt) {
+__global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt) {
     const int stride = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     for (int gi = 0; gi < bt->n_grids; ++gi) {
@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* bt) {
 // weight w_res, so the predicted weight is p_S * w_res, or 0 out of the grid (bit 30).
 // mode 0: full frame (shift + digit histograms); mode 1: stage call (no histograms).
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_predict(Batch* bt, int mode) {
+__global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, int mode) {
     __shared__ uint32_t h0[kSortMaxBins];
     __shared__ uint32_t h1[kSortMaxBins];
     const int total = batch_total(bt, kStPredict);
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* bt, int mode) {
 // allocation is an exact fixed-point scan instead of a float scan scaled by N / total.
 // An all-zero measurement spreads the particles uniformly (the reference divides by 0).
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_init_scan(Batch* bt) {
+__global__ void __launch_bounds__(kThreads) k_init_scan(Batch* __restrict__ bt) {
     __shared__ unsigned long long red[kThreads / 32];
     const int total = batch_total(bt, kStInitScan);
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kThreads) k_init_scan(Batch* bt) {
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_init_expand(Batch* bt) {
+__global__ void __launch_bounds__(kThreads) k_init_expand(Batch* __restrict__ bt) {
     __shared__ unsigned long long red[kThreads / 32];
     __shared__ int bnd[kCellTile + 1];  // bnd[0] = first slot of the tile, bnd[1+c] = end of cell c
     const int total = batch_total(bt, kStInitExpand);

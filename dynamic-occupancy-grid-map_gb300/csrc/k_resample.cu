@@ -12,18 +12,22 @@
 
 namespace dogm_gb300 {
 
+// A heavy item (more copies than an item writes itself) expanded by the whole block.
+struct HeavyItem {
+    float4 st;
+    uint32_t kw;
+    int first, end, item;
+};
+constexpr int kOwnCopies = 8;        // an item writes up to this many copies itself
+constexpr int kMaxHeavy = 768;       // heavy items per tile expanded cooperatively (more: by their thread)
+
 struct ResSmem {
-    float4 st[kResTile];
-    uint32_t kw[kResTile];
-    union {
-        float w[kResTile];   // weight of each item
-    } u;
     union {
         struct {                       // phase 1: newborn cells whose slots meet this tile
             int first[kResTile + 1];   // first slot
             int2 cell[kResTile + 1];   // {cell, associated slots}
         } ent;
-        int3 heavy[kResTile];          // phase 2: items with many copies {item, first, end slot}
+        HeavyItem heavy[kMaxHeavy];    // phase 2: items with many copies
     } x;
     unsigned long long red[2 * (kThreads / 32)];
     int nent;
@@ -31,14 +35,15 @@ struct ResSmem {
     int nheavy;
     int claim;
 };
-constexpr int kOwnCopies = 8;        // an item writes up to this many copies itself
 
 // Collects (warp 0) the newborn cells whose slot ranges meet [s0, s1), in slot order.
 // Cell tile ct owns slots [start[ct], start[ct+1]).
 __device__ void gather_newborn_cells(const GridDesc& g, int s0, int s1, ResSmem& sm) {
     const int lane = threadIdx.x & 31;
     const int CT = g.tiles[kStBirth];
-    const int* start = g.nb_tile_start;
+    const int* __restrict__ start = g.nb_tile_start;
+    const int* __restrict__ count = g.nb_count;
+    const NewbornCell* __restrict__ lists = g.nb_list;
     if (lane == 0) {
         int a = 0, b = CT - 1;  // largest ct with start[ct] <= s0
         while (a < b) {
@@ -49,35 +54,46 @@ __device__ void gather_newborn_cells(const GridDesc& g, int s0, int s1, ResSmem&
         sm.nent = 0;
     }
     __syncwarp();
-    for (int ct = sm.ct_lo; ct < CT; ++ct) {
-        if (start[ct] >= s1) break;
-        const int cnt = g.nb_count[ct];
-        const NewbornCell* list = g.nb_list + (size_t)ct * kCellTile;
-        for (int e0 = 0; e0 < cnt; e0 += 32) {
-            const int e = e0 + lane;
-            NewbornCell c;
-            bool take = false;
-            if (e < cnt) {
-                c = list[e];
-                take = c.first < s1 && c.first + c.n > s0;
-            }
-            const unsigned m = __ballot_sync(0xffffffffu, take);
-            const int base = sm.nent;
-            if (take) {
-                const int i = base + __popc(m & ((1u << lane) - 1u));
-                if (i <= kResTile) {
-                    sm.x.ent.first[i] = c.first;
-                    sm.x.ent.cell[i] = make_int2(c.cell, c.nu_A);
+    // cell tiles ct_lo, ct_lo+1, ... while they start before s1; 32 tiles examined at once
+    for (int c0 = sm.ct_lo; c0 < CT; c0 += 32) {
+        const int ct = c0 + lane;
+        const bool in = ct < CT && start[ct] < s1;
+        const int cnt = in ? count[ct] : 0;
+        unsigned todo = __ballot_sync(0xffffffffu, cnt > 0);
+        const bool more = __all_sync(0xffffffffu, in || ct >= CT) && (c0 + 32 < CT);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int tct = c0 + src;
+            const int tcnt = __shfl_sync(0xffffffffu, cnt, src);
+            const NewbornCell* list = lists + (size_t)tct * kCellTile;
+            for (int e0 = 0; e0 < tcnt; e0 += 32) {
+                const int e = e0 + lane;
+                NewbornCell c;
+                bool take = false;
+                if (e < tcnt) {
+                    c = list[e];
+                    take = c.first < s1 && c.first + c.n > s0;
                 }
+                const unsigned m = __ballot_sync(0xffffffffu, take);
+                const int base = sm.nent;
+                if (take) {
+                    const int i = base + __popc(m & ((1u << lane) - 1u));
+                    if (i <= kResTile) {
+                        sm.x.ent.first[i] = c.first;
+                        sm.x.ent.cell[i] = make_int2(c.cell, c.nu_A);
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) sm.nent = min(base + __popc(m), kResTile + 1);
+                __syncwarp();
             }
-            __syncwarp();
-            if (lane == 0) sm.nent = min(base + __popc(m), kResTile + 1);
-            __syncwarp();
         }
+        if (!more) break;
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
+__global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ResSmem& sm = *reinterpret_cast<ResSmem*>(smem_raw);
     const int total = batch_total(bt, kStResample);
@@ -91,14 +107,22 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][kStResample];
         const int base = lt * kResTile;
-        const int N = g.N;
+        const int N = g.N, C = g.C, gs = g.gs, S = g.q_shift;
         const int M = N + g.fs->n_birth;
         const unsigned long long T = g.fs->joint_total;
+        const uint32_t* __restrict__ S_key = g.S_key;
+        const float4* __restrict__ S_state = g.S_state;
+        const float* __restrict__ w_cell = g.w_cell;
+        const dogm_grid_cell* __restrict__ cells = g.cells;
+        float4* __restrict__ P_state = g.P_state;
+        uint32_t* __restrict__ P_key = g.P_key;
+        int* __restrict__ dbg_src = g.dbg_src;
         const int s0 = max(base, N) - N, s1 = min(base + kResTile, M) - N;  // newborn slots here
         if (threadIdx.x < 32) {
             if (s0 < s1) gather_newborn_cells(g, s0, s1, sm);
             else if (threadIdx.x == 0) sm.nent = 0;
         }
+        if (threadIdx.x == 0) sm.nheavy = 0;
         __syncthreads();
         unsigned long long r64;
         if (g.rp_resample) {
@@ -108,18 +132,23 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
             r64 = ((unsigned long long)r.x << 32) | r.y;
         }
         const unsigned long long U = __umul64hi(r64, T);  // floor(u * T), u = r64 / 2^64
-        const float fgs = (float)g.gs;
 
-        // phase 1 (striped, coalesced): stage every joint item of the tile
-        for (int j = threadIdx.x; j < kResTile; j += kThreads) {
-            const int p = base + j;
+        // this thread's kResIpt consecutive joint items, in registers
+        float4 st[kResIpt];
+        uint32_t kw[kResIpt];
+        float wq[kResIpt];
+        unsigned long long v = 0ull;
+        const int j0 = threadIdx.x * kResIpt;
+#pragma unroll
+        for (int r = 0; r < kResIpt; ++r) {
+            const int p = base + j0 + r;
             float w = 0.0f;
-            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-            uint32_t kw = 0u;
+            st[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+            kw[r] = 0u;
             if (p < N) {
-                kw = g.S_key[p];
-                s = g.S_state[p];
-                w = (kw & kOutBit) ? 0.0f : g.w_cell[kw & kCellMask];
+                kw[r] = S_key[p];
+                st[r] = S_state[p];
+                w = (kw[r] & kOutBit) ? 0.0f : w_cell[kw[r] & kCellMask];
             } else if (p < M) {
                 // newborn slot b: its cell from the compact list (init_new_particles.cu:157-195)
                 const int b = p - N;
@@ -128,9 +157,9 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
                     const int m = (lo + hi + 1) >> 1;
                     if (sm.x.ent.first[m] <= b) lo = m; else hi = m - 1;
                 }
-                const int2 c = sm.x.ent.cell[lo];
-                const int k = min(max(c.x, 0), g.C - 1);
-                const bool assoc = (b - sm.x.ent.first[lo]) < c.y;
+                const int2 ce = sm.x.ent.cell[lo];
+                const int k = min(max(ce.x, 0), C - 1);
+                const bool assoc = (b - sm.x.ent.first[lo]) < ce.y;
                 float2 z;
                 if (g.rp_birth) {
                     z = g.rp_birth[b];
@@ -138,71 +167,62 @@ __global__ void __launch_bounds__(kThreads) k_resample(Batch* bt) {
                     const U4 rr = draw_block(g, (uint32_t)b, g.frame, kDrawBirth);
                     z = box_muller(rr.x, rr.y);
                 }
-                s.x = __fadd_rn((float)(k % g.gs), 0.5f);
-                s.y = __fadd_rn(__fdiv_rn((float)k, fgs), 0.5f);  // float division, as the reference
-                s.z = __fmaf_rn(z.x, g.sigma_birth, 0.0f);
-                s.w = __fmaf_rn(z.y, g.sigma_birth, 0.0f);
-                kw = (uint32_t)k | (assoc ? kAssocBit : 0u);
-                w = assoc ? g.cells[k].w_A : g.cells[k].w_UA;
+                st[r].x = __fadd_rn((float)(k % gs), 0.5f);
+                st[r].y = __fadd_rn(__fdiv_rn((float)k, (float)gs), 0.5f);  // float division, as the reference
+                st[r].z = __fmaf_rn(z.x, g.sigma_birth, 0.0f);
+                st[r].w = __fmaf_rn(z.y, g.sigma_birth, 0.0f);
+                kw[r] = (uint32_t)k | (assoc ? kAssocBit : 0u);
+                w = assoc ? cells[k].w_A : cells[k].w_UA;
                 if (g.dbg_perm) {  // debug export of the newborns
-                    g.B_state[b] = s;
-                    g.B_key[b] = kw;
+                    g.B_state[b] = st[r];
+                    g.B_key[b] = kw[r];
                     g.B_w[b] = w;
                 }
             }
-            sm.st[j] = s;
-            sm.kw[j] = kw & ~kOutBit;
-            sm.u.w[j] = (p < M) ? w : 0.0f;
-        }
-        __syncthreads();
-
-        // phase 2 (blocked): exact prefix of the quantised weights, output slot ranges
-        unsigned long long q[kResIpt];
-        unsigned long long v = 0ull;
-#pragma unroll
-        for (int r = 0; r < kResIpt; ++r) {
-            q[r] = quantize(sm.u.w[threadIdx.x * kResIpt + r], g.q_shift);
-            v += q[r];
+            kw[r] &= ~kOutBit;
+            wq[r] = (p < M) ? w : 0.0f;
+            v += quantize(wq[r], S);
         }
         unsigned long long tile_sum;
         unsigned long long acc = block_scan_after(v, g.res_sum, lt, sm.red, &tile_sum);
-        if (threadIdx.x == 0) sm.nheavy = 0;
-        // output slots [lo, hi) of each of this thread's items; the first item's lo is the
-        // comb count of everything before it
-        int lo_s = (base + threadIdx.x * kResIpt == 0) ? 0 : comb_count(acc, T, U, N);
-        __syncthreads();
+        // phase 1 is over (the scan's barriers passed): the entry list may be overwritten
+        int lo_s = (base + j0 == 0) ? 0 : comb_count(acc, T, U, N);
 #pragma unroll
         for (int r = 0; r < kResIpt; ++r) {
-            const int j = threadIdx.x * kResIpt + r;
-            acc += q[r];
+            acc += quantize(wq[r], S);
             const int hi_s = comb_count(acc, T, U, N);
-            if (hi_s - lo_s <= kOwnCopies) {
-                const float4 st = sm.st[j];
-                const uint32_t kw = sm.kw[j];
-                for (int s = lo_s; s < hi_s; ++s) {
-                    g.P_state[s] = st;
-                    g.P_key[s] = kw;
-                    if (g.dbg_src) g.dbg_src[s] = base + j;
-                }
-            } else {
+            bool own = hi_s - lo_s <= kOwnCopies;
+            if (!own) {
                 const int h = atomicAdd(&sm.nheavy, 1);
-                sm.x.heavy[h] = make_int3(j, lo_s, hi_s);
+                if (h < kMaxHeavy) {
+                    HeavyItem e;
+                    e.st = st[r]; e.kw = kw[r]; e.first = lo_s; e.end = hi_s; e.item = base + j0 + r;
+                    sm.x.heavy[h] = e;
+                } else {
+                    own = true;  // list full: this thread writes the copies itself
+                }
+            }
+            if (own) {
+                for (int s = lo_s; s < hi_s; ++s) {
+                    P_state[s] = st[r];
+                    P_key[s] = kw[r];
+                    if (dbg_src) dbg_src[s] = base + j0 + r;
+                }
             }
             lo_s = hi_s;
         }
         __syncthreads();
-        for (int h = 0; h < sm.nheavy; ++h) {
-            const int3 e = sm.x.heavy[h];
-            const float4 st = sm.st[e.x];
-            const uint32_t kw = sm.kw[e.x];
-            for (int s = e.y + threadIdx.x; s < e.z; s += kThreads) {
-                g.P_state[s] = st;
-                g.P_key[s] = kw;
-                if (g.dbg_src) g.dbg_src[s] = base + e.x;
+        const int nh = min(sm.nheavy, kMaxHeavy);
+        for (int h = 0; h < nh; ++h) {
+            const HeavyItem e = sm.x.heavy[h];
+            for (int s = e.first + threadIdx.x; s < e.end; s += kThreads) {
+                P_state[s] = e.st;
+                P_key[s] = e.kw;
+                if (dbg_src) dbg_src[s] = e.item;
             }
         }
         if (lt == 0 && threadIdx.x == 0) {
-            const float jf = ldexpf(__ull2float_rn(T), -g.q_shift);
+            const float jf = ldexpf(__ull2float_rn(T), -S);
             g.fs->w_res = __fdiv_rn(jf, (float)N);
         }
         __syncthreads();
@@ -215,7 +235,7 @@ cudaError_t prepare_kernels() {
 
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg) {
     const int smem = (int)sizeof(ResSmem);
-    k_resample<<<cfg.num_sms * 3, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_resample<<<cfg.num_sms * 6, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 

@@ -17,7 +17,7 @@ namespace dogm_gb300 {
 // ---------------------------------------------------------------------------------------
 constexpr int kScanWarps = 32;
 
-__global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* bt, int pass) {
+__global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict__ bt, int pass) {
     __shared__ uint32_t chunk[kScanWarps][33];
     __shared__ uint32_t red[kScanWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -78,7 +78,7 @@ struct SortSmem {
 };
 
 template <bool FINAL>
-__global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* bt) {
+__global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* __restrict__ bt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SortSmem& sm = *reinterpret_cast<SortSmem*>(smem_raw);
     const int stage = FINAL ? kStSort1 : kStSort0;
