@@ -47,11 +47,6 @@ enum Stage : int {
     kStInitExpand, kNumStages
 };
 
-// One cell that receives newborns this frame (compact per cell tile).
-struct NewbornCell {
-    int cell, first, n, nu_A;   // cell index, first newborn slot, slots, associated slots
-    float w_A, w_UA;
-};
 
 // Per-grid state that lives on the device across frames.
 struct FrameState {
@@ -94,7 +89,7 @@ struct GridDesc {
     float4* P_state; uint32_t* P_key;
     uint32_t* T_key; uint32_t* T_idx;
     float4* S_state; uint32_t* S_key;
-    float4* B_state; uint32_t* B_key; float* B_w;
+    float4* B_state; uint32_t* B_key; float* B_w;  // newborns: key words always, state/weight for debug export
     // cells
     dogm_grid_cell* cells;
     const dogm_measurement_cell* meas_src;
@@ -113,9 +108,6 @@ struct GridDesc {
     unsigned long long* cell_sum;  // per cell tile: quantised newborn mass (first half) and
                                    // first-frame occupied mass (second half)
     unsigned long long* res_sum;   // per resample tile: quantised joint weight (exact atomics)
-    NewbornCell* nb_list;   // per cell tile, kCellTile entries: the cells that get newborns
-    int* nb_count;          // per cell tile: entries used in nb_list
-    int* nb_tile_start;     // per cell tile (+1 at the end): first newborn slot of the tile
     FrameState* fs;
     unsigned int* status_out;  // the batch-level status word
     // replay inputs (NULL: Philox) and debug outputs (NULL: off)

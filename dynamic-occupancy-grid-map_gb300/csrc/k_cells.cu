@@ -9,8 +9,9 @@
 //               (statistical_moments.cu:78-106), the ego shift of the free mass
 //               (ego_motion_compensation.cu:25-43) and the measurement copy (dogm.cu:205-208).
 //  k_newborn  : newborn allocation over an exact scan of the newborn masses
-//               (init_new_particles.cu:126-155, dogm.cu:323-348); the newborn particles
-//               themselves are created where they are consumed, in the resample kernel.
+//               (init_new_particles.cu:126-155, dogm.cu:323-348): records w_A / w_UA and
+//               the key word of every newborn slot; the newborn particles themselves are
+//               created where they are consumed, in the resample kernel.
 #include "dogm_device.cuh"
 
 namespace dogm_gb300 {
@@ -274,9 +275,9 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
 // Newborn allocation.  Cell k owns newborn slots [floor(Q[k-1] B / Q), floor(Q[k] B / Q))
 // of the exact prefix Q of quantised newborn masses; nu_A = round(n p_A) of them are
 // associated (the reference marks nu_A + 1, racing with the next cell:
-// init_new_particles.cu:145-153).  Writes w_A / w_UA into the records, a compact list of
-// the tile's newborn cells (the resample kernel creates the newborns from it) and the
-// newborns' quantised weights into the resample tiles that will hold them.
+// init_new_particles.cu:145-153).  Writes w_A / w_UA into the records, the key word of each
+// newborn slot, and the newborns' quantised weights into the resample tiles that will hold
+// them.
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ void add_joint_range(TileAgg& agg, unsigned long long* res_sum, long long a, long long b,
                                                 unsigned long long q) {
@@ -290,9 +291,9 @@ __device__ __forceinline__ void add_joint_range(TileAgg& agg, unsigned long long
 
 __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
     __shared__ unsigned long long red[2 * (kThreads / 32)];
-    __shared__ int iscan[kThreads / 32];
     __shared__ TileAgg agg;
-    __shared__ int s_first;
+    __shared__ int s_bnd[kCellTile + 1];  // s_bnd[c]: first slot of cell c of the tile
+    __shared__ int s_nuA[kCellTile];
     const int total = batch_total(bt, kStBirth);
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStBirth, t);
@@ -313,24 +314,18 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
         unsigned long long tile_sum;
         unsigned long long acc = block_scan_after(v, g.cell_sum, lt, red, &tile_sum);
         int lo_c = alloc_boundary(acc, T, g.B);
-        if (threadIdx.x == 0) {
-            g.nb_tile_start[lt] = lo_c;
-            s_first = lo_c;
-        }
+        if (threadIdx.x == 0) s_bnd[0] = lo_c;
         __syncthreads();
-        agg_reset(agg, ((long long)g.N + s_first) / kResTile);
-        __syncthreads();
+        agg_reset(agg, ((long long)g.N + s_bnd[0]) / kResTile);
         int bnd[kCellIpt + 1];
         bnd[0] = lo_c;
-        int nflag = 0;
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
             acc += q[j];
             bnd[j + 1] = q[j] ? alloc_boundary(acc, T, g.B) : bnd[j];
-            nflag += (bnd[j + 1] > bnd[j]) ? 1 : 0;
+            s_bnd[threadIdx.x * kCellIpt + j + 1] = bnd[j + 1];
         }
-        int ntile;
-        int pos = block_excl_scan_i32(nflag, iscan, &ntile);
+        __syncthreads();
         unsigned long long jq = 0ull;
         const long long N = g.N;
 #pragma unroll
@@ -345,10 +340,7 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
                 const float wUA = nuUA > 0 ? __fdiv_rn(__fmul_rn(__fsub_rn(1.0f, pA), rb[j]), (float)nuUA) : 0.0f;
                 g.cells[k].w_A = wA;
                 g.cells[k].w_UA = wUA;
-                NewbornCell e;
-                e.cell = k; e.first = bnd[j]; e.n = nnew; e.nu_A = nuA; e.w_A = wA; e.w_UA = wUA;
-                g.nb_list[(size_t)lt * kCellTile + pos] = e;
-                ++pos;
+                s_nuA[threadIdx.x * kCellIpt + j] = nuA;
                 const int nA = min(max(nuA, 0), nnew);
                 const unsigned long long qA = quantize(wA, g.q_shift), qU = quantize(wUA, g.q_shift);
                 jq += (unsigned long long)nA * qA + (unsigned long long)(nnew - nA) * qU;
@@ -358,13 +350,21 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
         }
         jq = warp_sum_u64(jq);
         if ((threadIdx.x & 31) == 0 && jq) atomicAdd(&g.fs->joint_total, jq);
-        __syncthreads();  // every shared add is done
+        __syncthreads();  // every shared add and s_nuA entry is done
         agg_flush(agg, g.res_sum, g.tiles[kStResample]);
-        if (threadIdx.x == 0) {
-            g.nb_count[lt] = ntile;
-            if (lt == 0) g.fs->n_birth = (T > 0ull) ? g.B : 0;
-            if (lt == g.tiles[kStBirth] - 1) g.nb_tile_start[lt + 1] = (T > 0ull) ? g.B : 0;
+        // key word of every newborn slot of the tile: cell | associated bit (the slot's cell
+        // is the first c with s_bnd[c + 1] > s); the resample pass creates the particles
+        const int ncell = min(kCellTile, g.C - base);
+        const int slo = s_bnd[0], shi = s_bnd[ncell];
+        for (int sl = slo + threadIdx.x; sl < shi; sl += kThreads) {
+            int a = 0, b = ncell - 1;
+            while (a < b) {
+                const int m = (a + b) >> 1;
+                if (s_bnd[m + 1] > sl) b = m; else a = m + 1;
+            }
+            g.B_key[sl] = (uint32_t)(base + a) | ((sl - s_bnd[a]) < s_nuA[a] ? kAssocBit : 0u);
         }
+        if (threadIdx.x == 0 && lt == 0) g.fs->n_birth = (T > 0ull) ? g.B : 0;
         __syncthreads();
     }
 }

@@ -1,6 +1,6 @@
 // Resampling: one pass over the joint particle array [persistent (sorted) | newborn].
-// The newborns are created here from the compact per-tile lists the newborn kernel wrote
-// (the reference initialises them in initNewParticlesKernel2, init_new_particles.cu:157-195).
+// The newborns are created here from the slot key words the newborn kernel wrote (the
+// reference initialises them in initNewParticlesKernel2, init_new_particles.cu:157-195).
 // Replaces the joint concatenation, float scan, random draws, float sort, lower_bound and
 // gather of dogm.cu:386-423 / resampling.cu:17-68.  Joint weights are quantised to
 // 2^-q_shift and scanned exactly (integer, order-independent; a tile's prefix is the sum of the
@@ -22,76 +22,11 @@ constexpr int kOwnCopies = 8;        // an item writes up to this many copies it
 constexpr int kMaxHeavy = 768;       // heavy items per tile expanded cooperatively (more: by their thread)
 
 struct ResSmem {
-    union {
-        struct {                       // phase 1: newborn cells whose slots meet this tile
-            int first[kResTile + 1];   // first slot
-            int2 cell[kResTile + 1];   // {cell, associated slots}
-        } ent;
-        HeavyItem heavy[kMaxHeavy];    // phase 2: items with many copies
-    } x;
+    HeavyItem heavy[kMaxHeavy];    // items with many copies
     unsigned long long red[2 * (kThreads / 32)];
-    int nent;
-    int ct_lo;
     int nheavy;
     int claim;
 };
-
-// Collects (warp 0) the newborn cells whose slot ranges meet [s0, s1), in slot order.
-// Cell tile ct owns slots [start[ct], start[ct+1]).
-__device__ void gather_newborn_cells(const GridDesc& g, int s0, int s1, ResSmem& sm) {
-    const int lane = threadIdx.x & 31;
-    const int CT = g.tiles[kStBirth];
-    const int* __restrict__ start = g.nb_tile_start;
-    const int* __restrict__ count = g.nb_count;
-    const NewbornCell* __restrict__ lists = g.nb_list;
-    if (lane == 0) {
-        int a = 0, b = CT - 1;  // largest ct with start[ct] <= s0
-        while (a < b) {
-            const int m = (a + b + 1) >> 1;
-            if (start[m] <= s0) a = m; else b = m - 1;
-        }
-        sm.ct_lo = a;
-        sm.nent = 0;
-    }
-    __syncwarp();
-    // cell tiles ct_lo, ct_lo+1, ... while they start before s1; 32 tiles examined at once
-    for (int c0 = sm.ct_lo; c0 < CT; c0 += 32) {
-        const int ct = c0 + lane;
-        const bool in = ct < CT && start[ct] < s1;
-        const int cnt = in ? count[ct] : 0;
-        unsigned todo = __ballot_sync(0xffffffffu, cnt > 0);
-        const bool more = __all_sync(0xffffffffu, in || ct >= CT) && (c0 + 32 < CT);
-        while (todo) {
-            const int src = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const int tct = c0 + src;
-            const int tcnt = __shfl_sync(0xffffffffu, cnt, src);
-            const NewbornCell* list = lists + (size_t)tct * kCellTile;
-            for (int e0 = 0; e0 < tcnt; e0 += 32) {
-                const int e = e0 + lane;
-                NewbornCell c;
-                bool take = false;
-                if (e < tcnt) {
-                    c = list[e];
-                    take = c.first < s1 && c.first + c.n > s0;
-                }
-                const unsigned m = __ballot_sync(0xffffffffu, take);
-                const int base = sm.nent;
-                if (take) {
-                    const int i = base + __popc(m & ((1u << lane) - 1u));
-                    if (i <= kResTile) {
-                        sm.x.ent.first[i] = c.first;
-                        sm.x.ent.cell[i] = make_int2(c.cell, c.nu_A);
-                    }
-                }
-                __syncwarp();
-                if (lane == 0) sm.nent = min(base + __popc(m), kResTile + 1);
-                __syncwarp();
-            }
-        }
-        if (!more) break;
-    }
-}
 
 __global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -117,13 +52,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt
         float4* __restrict__ P_state = g.P_state;
         uint32_t* __restrict__ P_key = g.P_key;
         int* __restrict__ dbg_src = g.dbg_src;
-        const int s0 = max(base, N) - N, s1 = min(base + kResTile, M) - N;  // newborn slots here
-        if (threadIdx.x < 32) {
-            if (s0 < s1) gather_newborn_cells(g, s0, s1, sm);
-            else if (threadIdx.x == 0) sm.nent = 0;
-        }
         if (threadIdx.x == 0) sm.nheavy = 0;
-        __syncthreads();
         unsigned long long r64;
         if (g.rp_resample) {
             r64 = *g.rp_resample;
@@ -150,16 +79,12 @@ __global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt
                 st[r] = S_state[p];
                 w = (kw[r] & kOutBit) ? 0.0f : w_cell[kw[r] & kCellMask];
             } else if (p < M) {
-                // newborn slot b: its cell from the compact list (init_new_particles.cu:157-195)
+                // newborn slot b (initNewParticlesKernel2, init_new_particles.cu:157-195): cell
+                // and associated flag from the key word the newborn kernel wrote
                 const int b = p - N;
-                int lo = 0, hi = sm.nent - 1;
-                while (lo < hi) {  // last entry with first <= b
-                    const int m = (lo + hi + 1) >> 1;
-                    if (sm.x.ent.first[m] <= b) lo = m; else hi = m - 1;
-                }
-                const int2 ce = sm.x.ent.cell[lo];
-                const int k = min(max(ce.x, 0), C - 1);
-                const bool assoc = (b - sm.x.ent.first[lo]) < ce.y;
+                const uint32_t bk = g.B_key[b];
+                const int k = min((int)(bk & kCellMask), C - 1);
+                const bool assoc = (bk & kAssocBit) != 0u;
                 float2 z;
                 if (g.rp_birth) {
                     z = g.rp_birth[b];
@@ -175,7 +100,6 @@ __global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt
                 w = assoc ? cells[k].w_A : cells[k].w_UA;
                 if (g.dbg_perm) {  // debug export of the newborns
                     g.B_state[b] = st[r];
-                    g.B_key[b] = kw[r];
                     g.B_w[b] = w;
                 }
             }
@@ -185,7 +109,6 @@ __global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt
         }
         unsigned long long tile_sum;
         unsigned long long acc = block_scan_after(v, g.res_sum, lt, sm.red, &tile_sum);
-        // phase 1 is over (the scan's barriers passed): the entry list may be overwritten
         int lo_s = (base + j0 == 0) ? 0 : comb_count(acc, T, U, N);
 #pragma unroll
         for (int r = 0; r < kResIpt; ++r) {
@@ -197,7 +120,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt
                 if (h < kMaxHeavy) {
                     HeavyItem e;
                     e.st = st[r]; e.kw = kw[r]; e.first = lo_s; e.end = hi_s; e.item = base + j0 + r;
-                    sm.x.heavy[h] = e;
+                    sm.heavy[h] = e;
                 } else {
                     own = true;  // list full: this thread writes the copies itself
                 }
@@ -214,7 +137,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt
         __syncthreads();
         const int nh = min(sm.nheavy, kMaxHeavy);
         for (int h = 0; h < nh; ++h) {
-            const HeavyItem e = sm.x.heavy[h];
+            const HeavyItem e = sm.heavy[h];
             for (int s = e.first + threadIdx.x; s < e.end; s += kThreads) {
                 P_state[s] = e.st;
                 P_key[s] = e.kw;
@@ -235,7 +158,7 @@ cudaError_t prepare_kernels() {
 
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg) {
     const int smem = (int)sizeof(ResSmem);
-    k_resample<<<cfg.num_sms * 6, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_resample<<<cfg.num_sms * 3, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 

@@ -422,7 +422,6 @@ size_t dogm_state_bytes(const dogm_params* p) {
     b += C * (sizeof(dogm_grid_cell) + sizeof(dogm_measurement_cell) + 2 * 4 + 32 + 4 + 4) + C / 8;
     b += 2 * kSortMaxBins * 4 + (size_t)2 * s.sort_tiles * kSortMaxBins * 4;
     b += (size_t)s.seg_tiles * 2 * sizeof(SegSums) + (size_t)s.cell_tiles * 16 + (size_t)s.res_tiles * 8;
-    b += (size_t)s.cell_tiles * (kCellTile * sizeof(NewbornCell) + 8);
     b += sizeof(Batch);
     return b;
 }
@@ -480,9 +479,6 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     ALLOC(g.seg_head, s.seg_tiles); ALLOC(g.seg_tail, s.seg_tiles);
     ALLOC(g.cell_sum, 2 * (size_t)s.cell_tiles);
     ALLOC(g.res_sum, s.res_tiles);
-    ALLOC(g.nb_list, (size_t)s.cell_tiles * kCellTile);
-    ALLOC(g.nb_count, s.cell_tiles);
-    ALLOC(g.nb_tile_start, (size_t)s.cell_tiles + 1);
     ALLOC(g.fs, 1);
 #undef ALLOC
     // measurement cells start as in initGridCellsKernel (init.cu:65-80): no evidence,
