@@ -103,6 +103,19 @@ __device__ __forceinline__ int alloc_boundary(unsigned long long Q, unsigned lon
     return b;
 }
 
+// The same with a precomputed scale sc = fl(M / fl(T)): when the float estimate Q * sc is
+// farther from an integer than its error bound (4 roundings, relative 2.4e-7 < 3e-7), its
+// floor is exact and the 96-bit check is skipped; otherwise the exact path decides.
+__device__ __forceinline__ int alloc_boundary_fast(unsigned long long Q, unsigned long long T, int M, float sc) {
+    if (T == 0ull) return 0;
+    if (Q >= T) return M;
+    const float f = __fmul_rn(__ull2float_rn(Q), sc);
+    const float err = __fmaf_rn(f, 3e-7f, 1e-30f);
+    const float lo = floorf(__fsub_rn(f, err)), hi = floorf(__fadd_rn(f, err));
+    if (lo == hi && lo >= 0.0f && lo <= (float)M) return (int)lo;
+    return alloc_boundary(Q, T, M);
+}
+
 // Systematic resampling comb: slot i takes the joint particle j with
 // A[j-1]*N <= i*T + U < A[j]*N (A = inclusive exact prefix, T = total, U in [0,T)).
 // comb_count(a) = #{ i in [0,N) : i*T + U < a*N }.  T == 0 sends every slot to particle 0.

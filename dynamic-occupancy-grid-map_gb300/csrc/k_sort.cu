@@ -16,6 +16,7 @@ namespace dogm_gb300 {
 // Work item = (grid, group of 32 digits); 32 warps split the tiles into contiguous chunks.
 // ---------------------------------------------------------------------------------------
 constexpr int kScanWarps = 32;
+constexpr int kScanBatch = 8;
 
 __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict__ bt, int pass) {
     __shared__ uint32_t chunk[kScanWarps][33];
@@ -45,26 +46,40 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict
             if (lane >= o) lanepre += y;
         }
         base += lanepre - own;
-        // sweep 1: chunk sums
+        // each warp owns a contiguous chunk of tiles; its counts are loaded once, in batches
+        // of kScanBatch independent loads, summed, then rewritten as offsets
         uint32_t* H = g.hsort + (size_t)pass * g.sort_tiles * kSortMaxBins;
         const int T = g.sort_tiles;
         const int per = (T + kScanWarps - 1) / kScanWarps;
         const int t0 = warp * per, t1 = min(T, t0 + per);
         uint32_t s = 0;
-        if (b < nb)
-            for (int tt = t0; tt < t1; ++tt) s += H[(size_t)tt * kSortMaxBins + b];
+        if (b < nb) {
+            for (int tb = t0; tb < t1; tb += kScanBatch) {
+                uint32_t v[kScanBatch];
+#pragma unroll
+                for (int i = 0; i < kScanBatch; ++i)
+                    v[i] = (tb + i < t1) ? H[(size_t)(tb + i) * kSortMaxBins + b] : 0u;
+#pragma unroll
+                for (int i = 0; i < kScanBatch; ++i) s += v[i];
+            }
+        }
         chunk[warp][lane] = s;
         __syncthreads();
         uint32_t pre = base;
         for (int w = 0; w < warp; ++w) pre += chunk[w][lane];
-        // sweep 2: exclusive offsets in place
-        if (b < nb)
-            for (int tt = t0; tt < t1; ++tt) {
-                uint32_t* p = H + (size_t)tt * kSortMaxBins + b;
-                const uint32_t v = *p;
-                *p = pre;
-                pre += v;
+        if (b < nb) {
+            for (int tb = t0; tb < t1; tb += kScanBatch) {
+                uint32_t v[kScanBatch];
+#pragma unroll
+                for (int i = 0; i < kScanBatch; ++i)
+                    v[i] = (tb + i < t1) ? H[(size_t)(tb + i) * kSortMaxBins + b] : 0u;
+#pragma unroll
+                for (int i = 0; i < kScanBatch; ++i) {
+                    if (tb + i < t1) H[(size_t)(tb + i) * kSortMaxBins + b] = pre;
+                    pre += v[i];
+                }
             }
+        }
         __syncthreads();
     }
 }
@@ -181,7 +196,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* __restrict__ b
 }
 
 cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
-    k_sort_scan<<<cfg.num_sms, kScanWarps * 32, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), pass);
+    k_sort_scan<<<cfg.num_sms * 2, kScanWarps * 32, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), pass);
     return cudaGetLastError();
 }
 
