@@ -168,7 +168,6 @@ __global__ void __launch_bounds__(kThreads) k_segments(Batch* __restrict__ bt) {
 __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
     __shared__ unsigned long long red[kThreads / 32];
     __shared__ unsigned long long red2[kThreads / 32];
-    __shared__ float4 srec[kThreads * 4];  // one round of 256 records, written out coalesced
     const int total = batch_total(bt, kStCell);
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStCell, t);
@@ -257,7 +256,7 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
                         cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vxy)), __fmul_rn(mx, my));
                     }
                 }
-                float4* rec = srec + threadIdx.x * 4;
+                float4* rec = reinterpret_cast<float4*>(g.cells + k);
                 rec[0] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
                 rec[1] = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
                 rec[2] = make_float4(muUA, 0.0f, 0.0f, mx);
@@ -281,11 +280,6 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
                     }
                 }
             }
-            __syncthreads();
-            // the round's records, 512 contiguous bytes per warp store
-            float4* dst = reinterpret_cast<float4*>(g.cells + base + r * kThreads);
-            for (int i = threadIdx.x; i < ncell_r * 4; i += kThreads) dst[i] = srec[i];
-            __syncthreads();
         }
         unsigned long long tile_qb, tile_jq;
         block_excl_scan_u64(qb, red, &tile_qb);
@@ -380,17 +374,18 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
         if ((threadIdx.x & 31) == 0 && jq) atomicAdd(&g.fs->joint_total, jq);
         __syncthreads();  // every shared add and s_nuA entry is done
         agg_flush(agg, g.res_sum, g.tiles[kStResample]);
-        // key word of every newborn slot of the tile: cell | associated bit (the slot's cell
-        // is the first c with s_bnd[c + 1] > s); the resample pass creates the particles
+        // key word of every newborn slot of the tile: cell | associated bit.  Cells go to the
+        // warps round-robin and a warp fills a cell's slots 32 at a time, so a cell with
+        // thousands of newborns costs its warp a few dozen stores.
         const int ncell = min(kCellTile, g.C - base);
-        const int slo = s_bnd[0], shi = s_bnd[ncell];
-        for (int sl = slo + threadIdx.x; sl < shi; sl += kThreads) {
-            int a = 0, b = ncell - 1;
-            while (a < b) {
-                const int m = (a + b) >> 1;
-                if (s_bnd[m + 1] > sl) b = m; else a = m + 1;
-            }
-            g.B_key[sl] = (uint32_t)(base + a) | ((sl - s_bnd[a]) < s_nuA[a] ? kAssocBit : 0u);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t* __restrict__ B_key = g.B_key;
+        for (int c = warp; c < ncell; c += kThreads / 32) {
+            const int lo = s_bnd[c], hi = s_bnd[c + 1];
+            if (hi <= lo) continue;
+            const uint32_t key = (uint32_t)(base + c);
+            const int nA = s_nuA[c];
+            for (int sl = lo + lane; sl < hi; sl += 32) B_key[sl] = key | ((sl - lo) < nA ? kAssocBit : 0u);
         }
         if (threadIdx.x == 0 && lt == 0) g.fs->n_birth = (T > 0ull) ? g.B : 0;
         __syncthreads();
