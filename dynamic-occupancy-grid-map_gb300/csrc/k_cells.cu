@@ -174,110 +174,89 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][kStCell];
         const int base = lt * kCellTile;
-        const int C = g.C, gs = g.gs, S = g.q_shift;
-        const float alpha = g.alpha, p_B = g.p_B;
-        const dogm_measurement_cell* __restrict__ meas_src = g.meas_src;
-        const float* __restrict__ free_old = g.free_old;
-        const uint32_t* __restrict__ occ_bits = g.occ_bits;
         const float c_pred = __fmul_rn(g.p_S, g.fs->w_res);  // predicted weight of an in-grid particle
-        // inputs of this thread's cells first (independent loads in flight together)
-        float4 mz[kCellIpt];
-        float fp[kCellIpt];
-        bool occ[kCellIpt];
-#pragma unroll
-        for (int r = 0; r < kCellIpt; ++r) {
-            const int k = base + r * kThreads + threadIdx.x;
-            occ[r] = false;
-            fp[r] = 0.0f;
-            mz[r] = make_float4(0.f, 0.f, 1.f, 1.f);
-            if (k < C) {
-                occ[r] = (occ_bits[k >> 5] >> (k & 31)) & 1u;
-                mz[r] = reinterpret_cast<const float4*>(meas_src)[k];
-                if (g.shifted) {
-                    const int x = k % gs, y = k / gs;
-                    const int sx = x + g.shift_x, sy = y + g.shift_y;
-                    const bool ok = sx > 0 && sx < gs && sy > 0 && sy < gs;  // strict, as the reference
-                    fp[r] = ok ? free_old[sx + gs * sy] : 0.0f;
-                } else {
-                    fp[r] = free_old[k];
-                }
-            }
-        }
         unsigned long long qb = 0ull, jq = 0ull;
         for (int r = 0; r < kCellIpt; ++r) {
             const int k = base + r * kThreads + threadIdx.x;
-            const int ncell_r = min(kThreads, C - (base + r * kThreads));
-            if (ncell_r <= 0) break;
-            if (k < C) {
-                int start = -1, end = -1;
-                SegSums s;
-                s.n_in = 0; s.vx = s.vy = s.vxx = s.vyy = s.vxy = 0.0f;
-                if (occ[r]) {
-                    const int4 si = g.seg_i[k];
-                    start = si.x;
-                    end = si.y;
-                    const int ts = start / kSegTile, te = end / kSegTile;
-                    if (ts == te) {
-                        const float4 sf = g.seg_f[k];
-                        s.n_in = si.z;
-                        s.vxy = __int_as_float(si.w);
-                        s.vx = sf.x; s.vy = sf.y; s.vxx = sf.z; s.vyy = sf.w;
-                    } else {
-                        s = g.seg_tail[ts];
-                        for (int tt = ts + 1; tt <= te; ++tt) {
-                            const SegSums h = g.seg_head[tt];
-                            s.n_in += h.n_in;
-                            s.vx = __fadd_rn(s.vx, h.vx);
-                            s.vy = __fadd_rn(s.vy, h.vy);
-                            s.vxx = __fadd_rn(s.vxx, h.vxx);
-                            s.vyy = __fadd_rn(s.vyy, h.vyy);
-                            s.vxy = __fadd_rn(s.vxy, h.vxy);
-                        }
+            if (k >= g.C) break;
+            const int x = k % g.gs, y = k / g.gs;
+            const bool occupied = (g.occ_bits[k >> 5] >> (k & 31)) & 1u;
+            int start = -1, end = -1;
+            SegSums s;
+            s.n_in = 0; s.vx = s.vy = s.vxx = s.vyy = s.vxy = 0.0f;
+            if (occupied) {
+                const int4 si = g.seg_i[k];
+                start = si.x;
+                end = si.y;
+                const int ts = start / kSegTile, te = end / kSegTile;
+                if (ts == te) {
+                    const float4 sf = g.seg_f[k];
+                    s.n_in = si.z;
+                    s.vxy = __int_as_float(si.w);
+                    s.vx = sf.x; s.vy = sf.y; s.vxx = sf.z; s.vyy = sf.w;
+                } else {
+                    s = g.seg_tail[ts];
+                    for (int tt = ts + 1; tt <= te; ++tt) {
+                        const SegSums h = g.seg_head[tt];
+                        s.n_in += h.n_in;
+                        s.vx = __fadd_rn(s.vx, h.vx);
+                        s.vy = __fadd_rn(s.vy, h.vy);
+                        s.vxx = __fadd_rn(s.vxx, h.vxx);
+                        s.vyy = __fadd_rn(s.vyy, h.vyy);
+                        s.vxy = __fadd_rn(s.vxy, h.vxy);
                     }
                 }
-                const float4 m = mz[r];  // {free, occ, likelihood, p_A}
-                if (g.copy_meas) reinterpret_cast<float4*>(g.meas_own)[k] = m;
-                const CellOut o = cell_masses(s.n_in, c_pred, fp[r], alpha, p_B, m.x, m.y);
-                float muA = 0.0f, muUA = 0.0f, wp = 0.0f;
-                float mx = 0.0f, my = 0.0f, vx = 0.0f, vy = 0.0f, cxy = 0.0f;
-                if (occ[r]) {
-                    const float wu = __fmul_rn(m.z, o.w_norm);
-                    const float swu = __fmul_rn((float)s.n_in, wu);
-                    muA = swu > 0.0f ? __fdiv_rn(o.rho_p, swu) : 0.0f;
-                    muUA = o.m_occ_pred > 0.0f ? __fdiv_rn(o.rho_p, o.m_occ_pred) : 0.0f;
-                    wp = __fadd_rn(__fmul_rn(__fmul_rn(m.w, muA), wu),
-                                   __fmul_rn(__fmul_rn(__fsub_rn(1.0f, m.w), muUA), o.w_norm));
-                    if (o.rho_p > 0.0f) {
-                        const float inv = __fdiv_rn(1.0f, o.rho_p);
-                        mx = __fmul_rn(inv, __fmul_rn(wp, s.vx));
-                        my = __fmul_rn(inv, __fmul_rn(wp, s.vy));
-                        vx = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vxx)), __fmul_rn(mx, mx));
-                        vy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vyy)), __fmul_rn(my, my));
-                        cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vxy)), __fmul_rn(mx, my));
-                    }
+            }
+            float free_prev;
+            if (g.shifted) {
+                const int sx = x + g.shift_x, sy = y + g.shift_y;
+                const bool ok = sx > 0 && sx < g.gs && sy > 0 && sy < g.gs;  // strict, as the reference
+                free_prev = ok ? g.free_old[sx + g.gs * sy] : 0.0f;
+            } else {
+                free_prev = g.free_old[k];
+            }
+            const dogm_measurement_cell m = g.meas_src[k];
+            if (g.copy_meas) g.meas_own[k] = m;
+            const CellOut o = cell_masses(s.n_in, c_pred, free_prev, g.alpha, g.p_B, m.free_mass, m.occ_mass);
+            float muA = 0.0f, muUA = 0.0f, wp = 0.0f;
+            float mx = 0.0f, my = 0.0f, vx = 0.0f, vy = 0.0f, cxy = 0.0f;
+            if (occupied) {
+                const float wu = __fmul_rn(m.likelihood, o.w_norm);
+                const float swu = __fmul_rn((float)s.n_in, wu);
+                muA = swu > 0.0f ? __fdiv_rn(o.rho_p, swu) : 0.0f;
+                muUA = o.m_occ_pred > 0.0f ? __fdiv_rn(o.rho_p, o.m_occ_pred) : 0.0f;
+                wp = __fadd_rn(__fmul_rn(__fmul_rn(m.p_A, muA), wu),
+                               __fmul_rn(__fmul_rn(__fsub_rn(1.0f, m.p_A), muUA), o.w_norm));
+                if (o.rho_p > 0.0f) {
+                    const float inv = __fdiv_rn(1.0f, o.rho_p);
+                    mx = __fmul_rn(inv, __fmul_rn(wp, s.vx));
+                    my = __fmul_rn(inv, __fmul_rn(wp, s.vy));
+                    vx = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vxx)), __fmul_rn(mx, mx));
+                    vy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vyy)), __fmul_rn(my, my));
+                    cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vxy)), __fmul_rn(mx, my));
                 }
-                float4* rec = reinterpret_cast<float4*>(g.cells + k);
-                rec[0] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
-                rec[1] = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
-                rec[2] = make_float4(muUA, 0.0f, 0.0f, mx);
-                rec[3] = make_float4(my, vx, vy, cxy);
-                g.free_new[k] = o.free_up;
-                g.rho_b[k] = o.rho_b;
-                g.w_cell[k] = wp;
-                qb += quantize(o.rho_b, S);
-                // this cell's persistent particles sit at sorted positions [start, end]; their
-                // quantised weights go to the resample tiles that hold them (exact integer adds)
-                const unsigned long long qw = quantize(wp, S);
-                if (s.n_in > 0 && qw > 0ull) {
-                    jq += (unsigned long long)s.n_in * qw;
-                    const int ts = start / kResTile, te = end / kResTile;
-                    if (ts == te) {
-                        atomicAdd(&g.res_sum[ts], (unsigned long long)s.n_in * qw);
-                    } else {
-                        atomicAdd(&g.res_sum[ts], (unsigned long long)g.seg_tail[ts].n_in * qw);
-                        for (int tt = ts + 1; tt <= te; ++tt)
-                            atomicAdd(&g.res_sum[tt], (unsigned long long)g.seg_head[tt].n_in * qw);
-                    }
+            }
+            float4* rec = reinterpret_cast<float4*>(g.cells + k);
+            rec[0] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
+            rec[1] = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
+            rec[2] = make_float4(muUA, 0.0f, 0.0f, mx);
+            rec[3] = make_float4(my, vx, vy, cxy);
+            g.free_new[k] = o.free_up;
+            g.rho_b[k] = o.rho_b;
+            g.w_cell[k] = wp;
+            qb += quantize(o.rho_b, g.q_shift);
+            // this cell's persistent particles sit at sorted positions [start, end]; their
+            // quantised weights go to the resample tiles that hold them (exact integer adds)
+            const unsigned long long qw = quantize(wp, g.q_shift);
+            if (s.n_in > 0 && qw > 0ull) {
+                jq += (unsigned long long)s.n_in * qw;
+                const int ts = start / kResTile, te = end / kResTile;
+                if (ts == te) {
+                    atomicAdd(&g.res_sum[ts], (unsigned long long)s.n_in * qw);
+                } else {
+                    atomicAdd(&g.res_sum[ts], (unsigned long long)g.seg_tail[ts].n_in * qw);
+                    for (int tt = ts + 1; tt <= te; ++tt)
+                        atomicAdd(&g.res_sum[tt], (unsigned long long)g.seg_head[tt].n_in * qw);
                 }
             }
         }
@@ -310,11 +289,15 @@ __device__ __forceinline__ void add_joint_range(TileAgg& agg, unsigned long long
     }
 }
 
+constexpr int kOwnSlots = 16;  // newborn slots a thread fills for its own cell
+
 __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
     __shared__ unsigned long long red[2 * (kThreads / 32)];
     __shared__ TileAgg agg;
     __shared__ int s_bnd[kCellTile + 1];  // s_bnd[c]: first slot of cell c of the tile
     __shared__ int s_nuA[kCellTile];
+    __shared__ int s_heavy[kCellTile];
+    __shared__ int s_nheavy;
     const int total = batch_total(bt, kStBirth);
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStBirth, t);
@@ -336,7 +319,10 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
         unsigned long long acc = block_scan_after(v, g.cell_sum, lt, red, &tile_sum);
         const float sc = T ? __fdiv_rn((float)g.B, __ull2float_rn(T)) : 0.0f;
         int lo_c = alloc_boundary_fast(acc, T, g.B, sc);
-        if (threadIdx.x == 0) s_bnd[0] = lo_c;
+        if (threadIdx.x == 0) {
+            s_bnd[0] = lo_c;
+            s_nheavy = 0;
+        }
         __syncthreads();
         agg_reset(agg, ((long long)g.N + s_bnd[0]) / kResTile);
         int bnd[kCellIpt + 1];
@@ -374,18 +360,28 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
         if ((threadIdx.x & 31) == 0 && jq) atomicAdd(&g.fs->joint_total, jq);
         __syncthreads();  // every shared add and s_nuA entry is done
         agg_flush(agg, g.res_sum, g.tiles[kStResample]);
-        // key word of every newborn slot of the tile: cell | associated bit.  Cells go to the
-        // warps round-robin and a warp fills a cell's slots 32 at a time, so a cell with
-        // thousands of newborns costs its warp a few dozen stores.
-        const int ncell = min(kCellTile, g.C - base);
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        // key word of every newborn slot of the tile: cell | associated bit.  A cell with few
+        // newborns is filled by its own thread; the block fills the heavy cells together.
         uint32_t* __restrict__ B_key = g.B_key;
-        for (int c = warp; c < ncell; c += kThreads / 32) {
+#pragma unroll
+        for (int j = 0; j < kCellIpt; ++j) {
+            const int c = threadIdx.x * kCellIpt + j;
+            const int lo = bnd[j], hi = bnd[j + 1];
+            if (hi - lo > 0 && hi - lo <= kOwnSlots) {
+                const uint32_t key = (uint32_t)(base + c);
+                const int nA = s_nuA[c];
+                for (int sl = lo; sl < hi; ++sl) B_key[sl] = key | ((sl - lo) < nA ? kAssocBit : 0u);
+            } else if (hi - lo > kOwnSlots) {
+                s_heavy[atomicAdd(&s_nheavy, 1)] = c;
+            }
+        }
+        __syncthreads();
+        for (int h = 0; h < s_nheavy; ++h) {
+            const int c = s_heavy[h];
             const int lo = s_bnd[c], hi = s_bnd[c + 1];
-            if (hi <= lo) continue;
             const uint32_t key = (uint32_t)(base + c);
             const int nA = s_nuA[c];
-            for (int sl = lo + lane; sl < hi; sl += 32) B_key[sl] = key | ((sl - lo) < nA ? kAssocBit : 0u);
+            for (int sl = lo + threadIdx.x; sl < hi; sl += kThreads) B_key[sl] = key | ((sl - lo) < nA ? kAssocBit : 0u);
         }
         if (threadIdx.x == 0 && lt == 0) g.fs->n_birth = (T > 0ull) ? g.B : 0;
         __syncthreads();
