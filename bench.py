@@ -111,7 +111,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "10"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -156,6 +156,16 @@ def make_frames(count: int, seed: int = 0):
     return scene, cfg, [sc.frame(k) for k in range(count)]
 
 
+def pingpong(n: int, pool: int) -> int:
+    """Frame index of step n when cycling a pool forth and back (0..P-1, P-2..1, 0, ...):
+    the ego drives back and forth, so every step still moves the grid."""
+    if pool <= 1:
+        return 0
+    period = 2 * pool - 2
+    m = n % period
+    return m if m < pool else period - m
+
+
 def cpu_baseline(frames, cfg, n_frames: int, threads: int = 0) -> dict:
     """The reference's pipeline on the host cores over a bounded sample of the workload."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
@@ -172,7 +182,7 @@ def cpu_baseline(frames, cfg, n_frames: int, threads: int = 0) -> dict:
     ref.update(m, x, y, yaw, 0.1)  # first measurement: initialisation, not timed
     times = []
     for k in range(1, n_frames + 1):
-        m, x, y, yaw = frames[k % len(frames)]
+        m, x, y, yaw = frames[pingpong(k, len(frames))]
         t0 = time.perf_counter()
         ref.update(m, x, y, yaw, 0.1)
         times.append((time.perf_counter() - t0) * 1e3)
@@ -192,10 +202,12 @@ def run_gb300(args, rank: int, world: int):
     dogm.load()
     K, W = args.steps, args.warmup
     P = 5  # profiled updates
-    # frames: [0, W] warm-up, then K timed, K end-to-end, P profiled (the trajectory continues)
+    # steps: [0, W] warm-up, then K timed, K end-to-end, P profiled; measurement grids come
+    # from a pool of distinct frames cycled forth and back (pingpong)
     t0_, e0_, p0_ = W + 1, W + 1 + K, W + 1 + 2 * K
-    n_frames = W + 1 + 2 * K + P
-    scene, cfg, frames = make_frames(n_frames, seed=rank)
+    pool = min(W + 1 + 2 * K + P, args.pool)
+    scene, cfg, frames = make_frames(pool, seed=rank)
+    fr = lambda n: pingpong(n, pool)
     p = dogm.make_params(**scene.params_dict(cfg))
     N, B = p.particle_count, p.new_born_particle_count
     g = dogm.DOGM(p, seed=123456, stream_id=rank, sync_each_update=False)
@@ -211,8 +223,8 @@ def run_gb300(args, rank: int, world: int):
         dbufs.append(d)
     # first measurement (initialisation) + warm-up (graph capture for both mirrors)
     for k in range(W + 1):
-        m, x, y, yaw = frames[k]
-        g.update_grid(dbufs[k].ptr, x, y, yaw, 0.1, device=True)
+        m, x, y, yaw = frames[fr(k)]
+        g.update_grid(dbufs[fr(k)].ptr, x, y, yaw, 0.1, device=True)
     g.synchronize()
 
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if world > 1 else 0)
@@ -221,8 +233,8 @@ def run_gb300(args, rank: int, world: int):
     e0, e1 = ev.new(), ev.new()
     ev.record(e0)
     for k in range(t0_, t0_ + K):
-        m, x, y, yaw = frames[k]
-        g.update_grid(dbufs[k].ptr, x, y, yaw, 0.1, device=True)
+        m, x, y, yaw = frames[fr(k)]
+        g.update_grid(dbufs[fr(k)].ptr, x, y, yaw, 0.1, device=True)
     ev.record(e1)
     total_ms = ev.elapsed(e0, e1)
     g.synchronize()
@@ -231,23 +243,26 @@ def run_gb300(args, rank: int, world: int):
     total_ms = reduce_max(total_ms, world)
 
     # end to end through the C ABI with host buffers (pinned), grid read back every step
-    pins = []
+    pins = {}
     for k in range(K):
-        pa = dogm.PinnedArray((C_, 4), np.float32)
-        pa.array[:] = frames[e0_ + k][0]
-        pins.append(pa)
+        i = fr(e0_ + k)
+        if i not in pins:
+            pa = dogm.PinnedArray((C_, 4), np.float32)
+            pa.array[:] = frames[i][0]
+            pins[i] = pa
     out = dogm.PinnedArray((C_,), dogm.GRID_CELL_DTYPE)
     g.synchronize()
     barrier(world)
     e2, e3 = ev.new(), ev.new()
     ev.record(e2)
     for k in range(K):
-        _, x, y, yaw = frames[e0_ + k]
-        g.update_grid(pins[k].array, x, y, yaw, 0.1, device=False)
+        i = fr(e0_ + k)
+        _, x, y, yaw = frames[i]
+        g.update_grid(pins[i].array, x, y, yaw, 0.1, device=False)
         g.get_grid_cells(out.array)
     ev.record(e3)
     e2e_ms = reduce_max(ev.elapsed(e2, e3), world)
-    for pa in pins:
+    for pa in pins.values():
         pa.free()
     out.free()
 
@@ -255,8 +270,8 @@ def run_gb300(args, rank: int, world: int):
     g.profile_enable(True)
     stage_runs = []
     for k in range(p0_, p0_ + P):
-        m, x, y, yaw = frames[k]
-        g.update_grid(dbufs[k].ptr, x, y, yaw, 0.1, device=True)
+        m, x, y, yaw = frames[fr(k)]
+        g.update_grid(dbufs[fr(k)].ptr, x, y, yaw, 0.1, device=True)
         g.synchronize()
         stage_runs.append(g.stage_times())
     g.profile_enable(False)
@@ -328,7 +343,7 @@ def run_reference(args, rank: int, world: int):
     if rank != 0:
         return None
     K, W = args.steps, args.warmup
-    _, cfg, frames = make_frames(min(K + W + 1, 12), seed=0)
+    _, cfg, frames = make_frames(min(K + W + 1, 24), seed=0)
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import importlib
     import pyoracle
@@ -340,11 +355,11 @@ def run_reference(args, rank: int, world: int):
     p = dogm.make_params(**importlib.import_module(PKG + ".scene").params_dict(cfg))
     ref = pyoracle.ReferencePipeline(p, threads=0)
     for k in range(W + 1):
-        m, x, y, yaw = frames[k % len(frames)]
+        m, x, y, yaw = frames[pingpong(k, len(frames))]
         ref.update(m, x, y, yaw, 0.1)
     t0 = time.perf_counter()
     for k in range(K):
-        m, x, y, yaw = frames[(W + 1 + k) % len(frames)]
+        m, x, y, yaw = frames[pingpong(W + 1 + k, len(frames))]
         ref.update(m, x, y, yaw, 0.1)
     ms = (time.perf_counter() - t0) * 1e3 / K
     sample = "%d full updates of the %s workload (1.44e6 cells, 2e6 + 2e5 particles)" % (K, WORKLOAD)
@@ -379,10 +394,11 @@ def reduce_max(v: float, world: int) -> float:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--pool", type=int, default=40, help="distinct measurement frames resident on the device")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-frames", type=int, default=3)
+    ap.add_argument("--cpu-frames", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
