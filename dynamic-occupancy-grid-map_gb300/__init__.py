@@ -38,7 +38,7 @@ ABI_SYMBOLS = [
     "dogm_get_grid_cells", "dogm_get_grid_cells_device", "dogm_get_measurement_cells", "dogm_get_particles",
     "dogm_get_grid_size", "dogm_get_resolution", "dogm_get_position_x", "dogm_get_position_y", "dogm_get_yaw",
     "dogm_get_iteration", "dogm_get_particle_count", "dogm_get_new_born_particle_count", "dogm_particle_prediction",
-    "dogm_update_pose", "dogm_initialize_particles", "dogm_set_measurement_cells", "dogm_set_particles",
+    "dogm_update_pose", "dogm_update_pose_noalloc", "dogm_initialize_particles", "dogm_set_measurement_cells", "dogm_set_particles",
     "dogm_set_replay", "dogm_clear_replay", "dogm_generate_draws", "dogm_debug_enable", "dogm_debug_export",
     "dogm_lower_bound_f32", "dogm_host_alloc", "dogm_host_free", "dogm_device_alloc", "dogm_device_free",
     "dogm_memcpy", "dogm_state_bytes", "dogm_last_launch_count", "dogm_last_error", "dogm_status_string",
@@ -88,6 +88,7 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_get_position_y": ([vp], f), "dogm_get_yaw": ([vp], f), "dogm_get_iteration": ([vp], i),
         "dogm_get_particle_count": ([vp], i), "dogm_get_new_born_particle_count": ([vp], i),
         "dogm_particle_prediction": ([vp, f], i), "dogm_update_pose": ([vp, f, f, f], i),
+        "dogm_update_pose_noalloc": ([vp, f, f, f], i),
         "dogm_initialize_particles": ([vp], i), "dogm_set_measurement_cells": ([vp, vp, sz], i),
         "dogm_set_particles": ([vp, vp, vp, vp, f, sz], i), "dogm_set_replay": ([vp, vp, vp, vp, vp], i),
         "dogm_clear_replay": ([vp], i), "dogm_generate_draws": ([vp, i, vp, vp, vp, vp], i),
@@ -287,6 +288,10 @@ class DOGM:
 
     def update_pose(self, x: float, y: float, yaw: float) -> None:
         check(load().dogm_update_pose(self.h, x, y, yaw), "dogm_update_pose")
+
+    def update_pose_noalloc(self, x: float, y: float, yaw: float) -> None:
+        """update_pose without device allocation (grids of at most 262,144 cells)."""
+        check(load().dogm_update_pose_noalloc(self.h, x, y, yaw), "dogm_update_pose_noalloc")
 
     def initialize_particles(self) -> None:
         check(load().dogm_initialize_particles(self.h), "dogm_initialize_particles")

@@ -149,6 +149,11 @@ cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_shift_stage(const GridDesc& g, int x_move, int y_move, const LaunchCfg& cfg);
+// Allocation-free shift stage: the copy of the previous cell records goes to a fixed device
+// array of kShiftScratchBytes (16 MiB = 262,144 cells, e.g. a 512 x 512 grid).
+constexpr size_t kShiftScratchBytes = size_t(16) << 20;
+cudaError_t shift_scratch_setup();  // once per device, with that device current
+cudaError_t launch_shift_stage_noalloc(const GridDesc& g, int x_move, int y_move, const LaunchCfg& cfg);
 cudaError_t launch_draws(const GridDesc& g, int iteration, float2* init_u, float4* predict_z, float2* birth_z,
                          unsigned long long* resample_r, const LaunchCfg& cfg);
 cudaError_t launch_lower_bound(const float* accum, int n_accum, const float* q, int n_q, int* out, int clamp_last,

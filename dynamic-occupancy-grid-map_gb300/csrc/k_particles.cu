@@ -1,5 +1,8 @@
 // Particle-side kernels: frame begin, prediction (with the fused ego shift), first-frame
 // particle initialisation, the stand-alone shift stage and Philox draw export.
+#include <map>
+#include <mutex>
+
 #include "dogm_device.cuh"
 
 namespace dogm_gb300 {
@@ -311,6 +314,62 @@ cudaError_t launch_shift_stage(const GridDesc& g, int x_move, int y_move, const 
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return cudaFreeAsync(old_cells, cfg.stream);
+}
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free shift stage.
+//
+// Some callers may not allocate device memory once they are running: a real-time loop whose
+// device memory is fixed at start-up, or a process whose free device memory is held by
+// another allocator (a framework's caching allocator, a fixed arena), where the temporary
+// cudaMallocAsync of launch_shift_stage can stall or fail in mid-run.  This variant copies
+// the previous cell records into a fixed device array compiled into the library instead.
+//
+// The array is one per device (per CUDA context) and every call shares it; it keeps the
+// contents of the last call.  Nothing in it has to start at zero: the copy overwrites the
+// first C records before k_shift_cells reads them, and nothing past them is read.  Calls
+// whose work overlaps on the GPU (two host threads shifting two grids at once) race on the
+// array, so such callers must serialise them.
+// ---------------------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_shift_scratch[kShiftScratchBytes];
+
+namespace {
+std::mutex g_shift_scratch_mu;
+std::map<int, void*> g_shift_scratch_ptr;  // device ordinal -> device address of g_shift_scratch
+}  // namespace
+
+cudaError_t shift_scratch_setup() {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(g_shift_scratch_mu);
+    if (g_shift_scratch_ptr.count(dev)) return cudaSuccess;
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_shift_scratch);
+    if (e != cudaSuccess) return e;
+    g_shift_scratch_ptr[dev] = p;
+    return cudaSuccess;
+}
+
+cudaError_t launch_shift_stage_noalloc(const GridDesc& g, int x_move, int y_move, const LaunchCfg& cfg) {
+    const size_t bytes = sizeof(dogm_grid_cell) * (size_t)g.C;
+    if (bytes > kShiftScratchBytes) return cudaErrorInvalidValue;  // the caller checks first
+    cudaError_t e = shift_scratch_setup();
+    if (e != cudaSuccess) return e;
+    int dev = -1;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    dogm_grid_cell* old_cells;
+    {
+        std::lock_guard<std::mutex> lock(g_shift_scratch_mu);
+        old_cells = static_cast<dogm_grid_cell*>(g_shift_scratch_ptr[dev]);
+    }
+    k_shift_particles<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(g.P_state, g.N, (float)x_move, (float)y_move);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    e = cudaMemcpyAsync(old_cells, g.cells, bytes, cudaMemcpyDeviceToDevice, cfg.stream);
+    if (e != cudaSuccess) return e;
+    k_shift_cells<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(g.cells, old_cells, g.free_new, g.free_old, g.gs,
+                                                                 x_move, y_move);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_draws(const GridDesc& g, int iteration, float2* init_u, float4* predict_z, float2* birth_z,

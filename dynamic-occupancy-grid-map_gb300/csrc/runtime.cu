@@ -711,6 +711,31 @@ dogm_status dogm_update_pose(dogm_handle* h, float new_x, float new_y, float new
     return DOGM_OK;
 }
 
+// dogm_update_pose without device allocation: the shift's copy of the previous cell records
+// goes to the library's fixed shift array (launch_shift_stage_noalloc) instead of a temporary
+// buffer.  A grid too large for the array is refused before the pose changes.
+dogm_status dogm_update_pose_noalloc(dogm_handle* h, float new_x, float new_y, float new_yaw) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    const size_t need = sizeof(dogm_grid_cell) * (size_t)h->C;
+    if (need > kShiftScratchBytes)
+        return fail(DOGM_ERR_INVALID_ARGUMENT,
+                    "dogm_update_pose_noalloc: a grid of " + std::to_string(h->C) + " cells needs " +
+                        std::to_string(need) + " B of shift scratch, more than the fixed " +
+                        std::to_string(kShiftScratchBytes) + " B (" +
+                        std::to_string(kShiftScratchBytes / sizeof(dogm_grid_cell)) +
+                        " cells); use dogm_update_pose for this grid");
+    DeviceGuard dg(h->device);
+    DOGM_CUDA(shift_scratch_setup());
+    int shifted, xm, ym;
+    pose_update(h, new_x, new_y, new_yaw, &shifted, &xm, &ym);
+    if (!shifted) return DOGM_OK;
+    LaunchCfg cfg{h->ctx.num_sms, h->ctx.stream};
+    DOGM_CUDA(launch_shift_stage_noalloc(h->desc, xm, ym, cfg));
+    DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+    std::swap(h->desc.free_old, h->desc.free_new);
+    return DOGM_OK;
+}
+
 dogm_status dogm_initialize_particles(dogm_handle* h) {
     if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
     DeviceGuard dg(h->device);

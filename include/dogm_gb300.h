@@ -153,6 +153,19 @@ dogm_status dogm_particle_prediction(dogm_handle* h, float dt);
  * when the pose moved by more than one cell, the particle and grid shift. */
 dogm_status dogm_update_pose(dogm_handle* h, float new_x, float new_y, float new_yaw);
 
+/* dogm_update_pose that allocates no device memory; it has no counterpart in the reference.
+ * Same arguments, results and errors as dogm_update_pose.  It is for callers that may not
+ * allocate device memory while they run -- a real-time loop whose device memory is fixed at
+ * start-up, or a process whose free device memory belongs to another allocator -- because
+ * dogm_update_pose takes a temporary buffer for the copy of the previous cell records.  Here
+ * that copy goes to a fixed 16 MiB device array built into the library, one per device, so
+ * grids of at most 262,144 cells (for example 512 x 512) are accepted; a larger grid returns
+ * DOGM_ERR_INVALID_ARGUMENT and leaves the handle unchanged.  The first call on a device looks
+ * up the array's address: make that first call before any stream capture.  All calls on a
+ * device share the one array, so calls whose work overlaps on the GPU (several host threads at
+ * once) race on it and must be serialised by the caller. */
+dogm_status dogm_update_pose_noalloc(dogm_handle* h, float new_x, float new_y, float new_yaw);
+
 /* Replaces DOGM::initializeParticles (dogm/src/dogm.cu:217-241) from the resident
  * measurement grid (set by a previous update, or by dogm_set_measurement_cells). */
 dogm_status dogm_initialize_particles(dogm_handle* h);
