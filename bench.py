@@ -52,8 +52,8 @@ def stage_bytes(N: int, B: int, C_: int, n_occ: int, n_birth_cells: int, sort_ti
         "sort_pass0": 12 * N + 4 * sort_tiles * nb0,  # key R 4, (key, index) W 8; offsets R
         "sort_scan1": 8 * sort_tiles * nb1,
         "sort_pass1": 44 * N,                    # (key, index) R 8, state gather R 16, state+key W 20
-        "segments": 20 * N + 32 * n_occ,         # key 4 + state 16 R; 32 B per occupied cell W
-        "cells": 112 * C_ + 32 * n_occ,          # meas 16 + free 4 R; record 64 + free 4 + rho_b 4 + w 4 + meas copy 16 W
+        "cells": 20 * N + 112 * C_,              # key 4 + state 16 R; meas 16 + free 4 R;
+                                                 # record 64 + free 4 + rho_b 4 + w 4 + meas copy 16 W
         "newborn": 4 * C_ + 32 * n_birth_cells,   # newborn mass R; w_A/w_UA + newborn-cell list W
         "resample": 24 * N + 20 * N,             # key 4 + state 16 + weight 4 R; state+key 20 W
                                                  # (newborns are created in registers)

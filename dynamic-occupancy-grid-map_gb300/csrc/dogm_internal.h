@@ -20,7 +20,7 @@ constexpr int kSortIpt = 16;         // keys per thread in a sort pass
 constexpr int kSortTile = kThreads * kSortIpt;
 constexpr int kSortMaxBits = 11;     // radix digit width <= 11 -> <= 2048 bins
 constexpr int kSortMaxBins = 1 << kSortMaxBits;
-constexpr int kSegIpt = 8;           // sorted particles per thread in the segmented reduction
+constexpr int kSegIpt = 4;           // sorted particles per thread in a chunk of the cell pass
 constexpr int kSegTile = kThreads * kSegIpt;
 constexpr int kCellIpt = 4;          // cells per thread in the cell passes
 constexpr int kCellTile = kThreads * kCellIpt;
@@ -28,9 +28,12 @@ constexpr int kResIpt = 8;           // joint particles per thread in resampling
 constexpr int kResTile = kThreads * kResIpt;
 
 static_assert(kPredictTile == kSortTile, "predict writes the pass-0 digit counts of the sort tiles");
-static_assert(kSegTile == kResTile, "cells add persistent weights into resample tiles by sorted position");
 
 constexpr int kMaxKeyBits = 22;      // grid_size <= 2048 -> cells < 2^22 -> 2 radix passes
+constexpr int kCellTileBits = 10;
+constexpr int kMaxCellTiles = (1 << kMaxKeyBits) >> kCellTileBits;
+static_assert(kCellTile == (1 << kCellTileBits), "cell tiles are indexed by cell >> kCellTileBits");
+static_assert(kResTile % 32 == 0, "32 aligned sorted positions lie in one resample tile");
 constexpr int kMaxParticles = (1 << 24) - 1;  // keys, counts and slot indices stay below 2^24
 
 // Particle key word: bits 0..29 cell index, bit 30 "out of grid" (weight 0), bit 31 associated.
@@ -43,7 +46,7 @@ enum DrawStage : uint32_t { kDrawInit = 1, kDrawPredict = 2, kDrawBirth = 3, kDr
 
 // Stages that claim tiles from a work counter (look-back ordering) or iterate statically.
 enum Stage : int {
-    kStPredict = 0, kStScan0, kStSort0, kStScan1, kStSort1, kStSeg, kStCell, kStBirth, kStResample, kStInitScan,
+    kStPredict = 0, kStScan0, kStSort0, kStScan1, kStSort1, kStCell, kStBirth, kStResample, kStInitScan,
     kStInitExpand, kNumStages
 };
 
@@ -62,12 +65,6 @@ struct FrameState {
 };
 constexpr uint32_t kStatusTimeout = 1u;  // a bounded wait gave up
 constexpr uint32_t kStatusBounds = 2u;   // an index check refused a write
-
-// Partial sums of one particle segment (one cell): in-grid count and velocity moments.
-struct SegSums {
-    int n_in;
-    float vx, vy, vxx, vyy, vxy;
-};
 
 struct GridDesc {
     // sizes
@@ -95,16 +92,14 @@ struct GridDesc {
     const dogm_measurement_cell* meas_src;
     dogm_measurement_cell* meas_own;
     float* free_old; float* free_new;   // free mass of the previous / this frame (ping-pong)
-    int4* seg_i;            // per cell: {start, end, n_in, float_bits(sum vxy)}
-    float4* seg_f;          // per cell: {sum vx, sum vy, sum vxx, sum vyy}
     float* rho_b;           // per cell newborn mass of this frame
     float* w_cell;          // per cell weight of an in-grid persistent particle after reweighting
-    uint32_t* occ_bits;     // per cell occupancy bit of this frame
     // scratch
     uint32_t* hist;         // 2 x kSortMaxBins digit histograms
     uint32_t* hsort;        // 2 x sort_tiles x kSortMaxBins: per-tile digit counts, then offsets
-    SegSums* seg_head;      // per segmented-reduction tile: partial of the segment entering it
-    SegSums* seg_tail;      // per tile: partial of the segment leaving it
+    uint32_t* ctile_cnt;    // per cell tile: particles whose cell lies in it (counted by predict)
+    uint32_t* ctile_start;  // per cell tile + 1: first sorted position of the tile (exclusive scan)
+    uint32_t* ctile_order;  // cell tiles in claim order: tiles with many particles first
     unsigned long long* cell_sum;  // per cell tile: quantised newborn mass (first half) and
                                    // first-frame occupied mass (second half)
     unsigned long long* res_sum;   // per resample tile: quantised joint weight (exact atomics)
@@ -138,13 +133,13 @@ struct LaunchCfg {
 };
 
 cudaError_t prepare_kernels();  // per device, before the first launch
+cudaError_t prepare_cells();
 cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCfg& cfg);
 cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg);
 cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg);
 cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cfg);
-cudaError_t launch_segments(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg);
@@ -160,8 +155,8 @@ cudaError_t launch_lower_bound(const float* accum, int n_accum, const float* q, 
                                cudaStream_t s);
 
 // Kernel launches per update (for the launch-count claim): frame-begin, predict, 2 x (digit
-// scan, sort pass), segments, cells, newborn, resample.
-constexpr int kLaunchesPerFrame = 10;
+// scan, sort pass), cells, newborn, resample.
+constexpr int kLaunchesPerFrame = 9;
 constexpr int kLaunchesInit = 2;
 
 }  // namespace dogm_gb300

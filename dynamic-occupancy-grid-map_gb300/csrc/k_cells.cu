@@ -1,35 +1,40 @@
 // Cell-side kernels.
-//  k_segments : one pass over the sorted particles; per cell (segment) the in-grid count
-//               and the velocity sums sum(v), sum(v^2), sum(vx*vy).  Replaces
-//               particleToGridKernel (particle_to_grid.cu:22-40), the weight-array copy and
-//               the five statistical-moment prefix scans (dogm.cu:350-384).
-//  k_cells    : one pass over all cells; fuses the predicted/free mass, the Dempster-Shafer
-//               measurement update and newborn split (mass_update.cu:57-89), the persistent
-//               reweighting (update_persistent_particles.cu:49-87), the moments
-//               (statistical_moments.cu:78-106), the ego shift of the free mass
-//               (ego_motion_compensation.cu:25-43) and the measurement copy (dogm.cu:205-208).
+//  k_cells    : one pass over all cells and the sorted particles in them; fuses the
+//               particle-to-cell segmented reduction, the mass update, reweighting,
+//               moments, ego shift of the free mass and the measurement copy.
 //  k_newborn  : newborn allocation over an exact scan of the newborn masses
 //               (init_new_particles.cu:126-155, dogm.cu:323-348): records w_A / w_UA and
 //               the key word of every newborn slot; the newborn particles themselves are
 //               created where they are consumed, in the resample kernel.
+#include <cstddef>
+
 #include "dogm_device.cuh"
 
 namespace dogm_gb300 {
 
 // ---------------------------------------------------------------------------------------
-// Segmented reduction over sorted particles.
+// Open runs of the segmented reduction: the sums that flow from one thread's particles into
+// the next thread's.  Bit 31 of fn marks a run that starts (has a segment head) inside the
+// span it summarises; bits 0..30 count in-grid particles.
 // ---------------------------------------------------------------------------------------
-struct SegRun {
-    int head;      // sorted position of the segment head inside this tile, -1 if it began earlier
-    int n;
+struct Run {
+    uint32_t fn;
     float vx, vy, vxx, vyy, vxy;
 };
+constexpr uint32_t kRunHead = 1u << 31;
 
-__device__ __forceinline__ SegRun seg_combine(const SegRun& a, const SegRun& b) {
-    if (b.head >= 0) return b;
-    SegRun r;
-    r.head = a.head;
-    r.n = a.n + b.n;
+__device__ __forceinline__ Run run_empty(uint32_t flag) {
+    Run r;
+    r.fn = flag;
+    r.vx = r.vy = r.vxx = r.vyy = r.vxy = 0.0f;
+    return r;
+}
+
+// a followed by b
+__device__ __forceinline__ Run run_combine(const Run& a, const Run& b) {
+    if (b.fn & kRunHead) return b;
+    Run r;
+    r.fn = a.fn + b.fn;
     r.vx = __fadd_rn(a.vx, b.vx);
     r.vy = __fadd_rn(a.vy, b.vy);
     r.vxx = __fadd_rn(a.vxx, b.vxx);
@@ -38,10 +43,19 @@ __device__ __forceinline__ SegRun seg_combine(const SegRun& a, const SegRun& b) 
     return r;
 }
 
-__device__ __forceinline__ SegRun seg_shfl_up(const SegRun& a, int o) {
-    SegRun r;
-    r.head = __shfl_up_sync(0xffffffffu, a.head, o);
-    r.n = __shfl_up_sync(0xffffffffu, a.n, o);
+__device__ __forceinline__ void run_add(Run& r, uint32_t kw, float2 v) {
+    if (kw & kOutBit) return;
+    r.fn += 1u;
+    r.vx = __fadd_rn(r.vx, v.x);
+    r.vy = __fadd_rn(r.vy, v.y);
+    r.vxx = __fadd_rn(r.vxx, __fmul_rn(v.x, v.x));
+    r.vyy = __fadd_rn(r.vyy, __fmul_rn(v.y, v.y));
+    r.vxy = __fadd_rn(r.vxy, __fmul_rn(v.x, v.y));
+}
+
+__device__ __forceinline__ Run run_shfl_up(const Run& a, int o) {
+    Run r;
+    r.fn = __shfl_up_sync(0xffffffffu, a.fn, o);
     r.vx = __shfl_up_sync(0xffffffffu, a.vx, o);
     r.vy = __shfl_up_sync(0xffffffffu, a.vy, o);
     r.vxx = __shfl_up_sync(0xffffffffu, a.vxx, o);
@@ -50,190 +64,226 @@ __device__ __forceinline__ SegRun seg_shfl_up(const SegRun& a, int o) {
     return r;
 }
 
-__device__ __forceinline__ SegSums to_sums(const SegRun& r) {
-    SegSums s;
-    s.n_in = r.n;
-    s.vx = r.vx; s.vy = r.vy; s.vxx = r.vxx; s.vyy = r.vyy; s.vxy = r.vxy;
-    return s;
-}
+// ---------------------------------------------------------------------------------------
+// Fused per-cell update over one tile of kCellTile cells and the sorted particles that lie
+// in it, positions [ctile_start[t], ctile_start[t + 1]).
+//   A  segmented reduction of those particles into per-cell shared sums (sorted range,
+//      in-grid count, sum(v), sum(v^2), sum(vx*vy)).  Each thread walks kSegIpt consecutive
+//      particles: a cell whose particles start and end inside the thread is written
+//      directly; the run still open at the thread's end flows through a block scan to the
+//      thread holding the cell's last particle, which writes it.  Plain stores only (every
+//      slot has one writer), and the add order depends only on positions, so the sums are
+//      deterministic.  Replaces particleToGridKernel (particle_to_grid.cu:22-40), the
+//      weight-array copy and the five statistical-moment prefix scans (dogm.cu:350-384).
+//   B  per cell: predicted and free mass, Dempster-Shafer update and newborn split
+//      (mass_update.cu:57-89), persistent reweighting (update_persistent_particles.cu:49-87),
+//      moments (statistical_moments.cu:78-106), ego shift of the free mass
+//      (ego_motion_compensation.cu:25-43) and the measurement copy (dogm.cu:205-208).
+//      The quantised weight of each cell's persistent particles goes to the resample
+//      tiles that hold them.
+// ---------------------------------------------------------------------------------------
+struct CellSmem {
+    dogm_measurement_cell meas[kCellTile];  // prefetched (cp.async) while A runs
+    float free_prev[kCellTile];             // previous free mass, ego shift applied
+    int start[kCellTile];   // sorted position of the first particle (-1: none)
+    int end[kCellTile];     // sorted position of the last particle
+    int n_in[kCellTile];    // in-grid particles
+    float vx[kCellTile], vy[kCellTile], vxx[kCellTile], vyy[kCellTile], vxy[kCellTile];
+    Run wagg[kThreads / 32];
+    Run carry;              // run open at the end of the previous chunk
+    unsigned long long red[kThreads / 32], red2[kThreads / 32];
+    int tile;
+};
+static_assert(offsetof(CellSmem, meas) % 16 == 0, "16-byte cp.async destination");
 
-__device__ __forceinline__ SegRun seg_item(uint32_t kw, float4 st, bool head, int pos) {
-    SegRun it;
-    it.head = head ? pos : -1;
-    if (kw & kOutBit) {
-        it.n = 0;
-        it.vx = it.vy = it.vxx = it.vyy = it.vxy = 0.0f;
-    } else {
-        it.n = 1;
-        it.vx = st.z;
-        it.vy = st.w;
-        it.vxx = __fmul_rn(st.z, st.z);
-        it.vyy = __fmul_rn(st.w, st.w);
-        it.vxy = __fmul_rn(st.z, st.w);
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// The quantised weights of a cell's in-grid persistent particles (sorted positions
+// [start, end]) added to the resample tiles that hold them.  Out-of-grid particles (weight
+// 0) lie only in border cells; only for those is a split across tiles counted from the keys.
+__device__ __forceinline__ void add_persistent(const GridDesc& g, int start, int end, int n_in,
+                                               unsigned long long qw) {
+    const int ts = start / kResTile, te = end / kResTile;
+    if (ts == te) {
+        atomicAdd(&g.res_sum[ts], (unsigned long long)n_in * qw);
+        return;
     }
-    return it;
-}
-
-// One tile = kSegTile consecutive sorted particles, staged in shared memory with coalesced
-// loads; thread i reduces items [i*kSegIpt, (i+1)*kSegIpt) in order, then a block-wide
-// segmented scan joins the threads.  The combine order depends only on positions, so the
-// sums are deterministic.
-__global__ void __launch_bounds__(kThreads) k_segments(Batch* __restrict__ bt) {
-    __shared__ uint32_t skey[kSegTile + 2];
-    __shared__ float2 svel[kSegTile];
-    __shared__ SegRun wagg[kThreads / 32];
-    const int total = batch_total(bt, kStSeg);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
-        const int gi = grid_of_tile(bt, kStSeg, t);
-        const GridDesc& g = bt->g[gi];
-        const int lt = t - bt->prefix[gi][kStSeg];
-        const int base = lt * kSegTile;
-        const int n = min(kSegTile, g.N - base);
-        for (int i = threadIdx.x; i < n; i += kThreads) {
-            skey[1 + i] = g.S_key[base + i];
-            const float4 st = g.S_state[base + i];
-            svel[i] = make_float2(st.z, st.w);
+    const bool all_in = n_in == end - start + 1;
+    for (int rt = ts; rt <= te; ++rt) {
+        const int lo = max(start, rt * kResTile), hi = min(end + 1, (rt + 1) * kResTile);
+        int cnt = hi - lo;
+        if (!all_in) {
+            cnt = 0;
+            for (int i = lo; i < hi; ++i) cnt += (g.S_key[i] & kOutBit) ? 0 : 1;
         }
-        if (threadIdx.x == 0) {
-            skey[0] = base > 0 ? (g.S_key[base - 1] & kCellMask) : 0xffffffffu;
-            skey[n + 1] = (base + n < g.N) ? (g.S_key[base + n] & kCellMask) : 0xffffffffu;
-        }
-        __syncthreads();
-
-        const int j0 = threadIdx.x * kSegIpt;
-        SegRun agg;
-        agg.head = -1; agg.n = 0; agg.vx = agg.vy = agg.vxx = agg.vyy = agg.vxy = 0.0f;
-        for (int r = 0; r < kSegIpt; ++r) {
-            const int j = j0 + r;
-            if (j >= n) break;
-            const uint32_t kw = skey[1 + j];
-            const uint32_t prev = (j == 0) ? skey[0] : (skey[j] & kCellMask);
-            const float2 v = svel[j];
-            agg = seg_combine(agg, seg_item(kw, make_float4(0.f, 0.f, v.x, v.y), (kw & kCellMask) != prev, base + j));
-        }
-        // block-wide exclusive segmented scan of the thread aggregates
-        SegRun inc = agg;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const SegRun other = seg_shfl_up(inc, o);
-            if (lane >= o) inc = seg_combine(other, inc);
-        }
-        if (lane == 31) wagg[warp] = inc;
-        SegRun excl = seg_shfl_up(inc, 1);
-        __syncthreads();
-        SegRun wpre;
-        wpre.head = -1; wpre.n = 0; wpre.vx = wpre.vy = wpre.vxx = wpre.vyy = wpre.vxy = 0.0f;
-        for (int w = 0; w < warp; ++w) wpre = seg_combine(wpre, wagg[w]);
-        excl = (lane == 0) ? wpre : seg_combine(wpre, excl);
-
-        // re-walk and emit at segment tails
-        SegRun run = excl;
-        for (int r = 0; r < kSegIpt; ++r) {
-            const int j = j0 + r;
-            if (j >= n) break;
-            const uint32_t kw = skey[1 + j];
-            const uint32_t c = kw & kCellMask;
-            const uint32_t prev = (j == 0) ? skey[0] : (skey[j] & kCellMask);
-            const uint32_t next = (j == n - 1) ? skey[n + 1] : (skey[2 + j] & kCellMask);
-            const float2 v = svel[j];
-            run = seg_combine(run, seg_item(kw, make_float4(0.f, 0.f, v.x, v.y), c != prev, base + j));
-            const int pos = base + j;
-            if (c != next) {
-                if (run.head >= 0) {
-                    g.seg_i[c] = make_int4(run.head, pos, run.n, __float_as_int(run.vxy));
-                    g.seg_f[c] = make_float4(run.vx, run.vy, run.vxx, run.vyy);
-                    atomicOr(&g.occ_bits[c >> 5], 1u << (c & 31));
-                } else {
-                    g.seg_head[lt] = to_sums(run);
-                    g.seg_i[c].y = pos;
-                }
-            } else if (j == n - 1) {
-                if (run.head >= 0) {
-                    g.seg_tail[lt] = to_sums(run);
-                    g.seg_i[c].x = run.head;
-                    atomicOr(&g.occ_bits[c >> 5], 1u << (c & 31));
-                } else {
-                    g.seg_head[lt] = to_sums(run);
-                }
-            }
-        }
-        __syncthreads();
+        if (cnt) atomicAdd(&g.res_sum[rt], (unsigned long long)cnt * qw);
     }
 }
 
-// ---------------------------------------------------------------------------------------
-// Fused per-cell update.
-// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void put_cell(CellSmem& sm, const GridDesc& g, uint32_t cl, int last, const Run& r) {
+    if (cl >= (uint32_t)kCellTile) {  // only inconsistent tile counts get here
+        flag_status(g, kStatusBounds);
+        return;
+    }
+    sm.end[cl] = last;
+    sm.n_in[cl] = (int)(r.fn & ~kRunHead);
+    sm.vx[cl] = r.vx;
+    sm.vy[cl] = r.vy;
+    sm.vxx[cl] = r.vxx;
+    sm.vyy[cl] = r.vyy;
+    sm.vxy[cl] = r.vxy;
+}
+
 __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
-    __shared__ unsigned long long red[kThreads / 32];
-    __shared__ unsigned long long red2[kThreads / 32];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    CellSmem& sm = *reinterpret_cast<CellSmem*>(smem_raw);
     const int total = batch_total(bt, kStCell);
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (;;) {
+        const int t = claim_tile(bt, kStCell, &sm.tile);
+        if (t >= total) break;
         const int gi = grid_of_tile(bt, kStCell, t);
         const GridDesc& g = bt->g[gi];
-        const int lt = t - bt->prefix[gi][kStCell];
+        const int lt = (int)g.ctile_order[t - bt->prefix[gi][kStCell]];  // full tiles first
         const int base = lt * kCellTile;
-        const float c_pred = __fmul_rn(g.p_S, g.fs->w_res);  // predicted weight of an in-grid particle
-        unsigned long long qb = 0ull, jq = 0ull;
+        const int p0 = (int)g.ctile_start[lt], p1 = (int)g.ctile_start[lt + 1];
+        // prefetch the measurement and the (shifted) previous free mass of this thread's cells
+        const bool meas16 = (reinterpret_cast<uintptr_t>(g.meas_src) & 15u) == 0u;
         for (int r = 0; r < kCellIpt; ++r) {
-            const int k = base + r * kThreads + threadIdx.x;
+            const int cl = r * kThreads + threadIdx.x;
+            const int k = base + cl;
             if (k >= g.C) break;
-            const int x = k % g.gs, y = k / g.gs;
-            const bool occupied = (g.occ_bits[k >> 5] >> (k & 31)) & 1u;
-            int start = -1, end = -1;
-            SegSums s;
-            s.n_in = 0; s.vx = s.vy = s.vxx = s.vyy = s.vxy = 0.0f;
-            if (occupied) {
-                const int4 si = g.seg_i[k];
-                start = si.x;
-                end = si.y;
-                const int ts = start / kSegTile, te = end / kSegTile;
-                if (ts == te) {
-                    const float4 sf = g.seg_f[k];
-                    s.n_in = si.z;
-                    s.vxy = __int_as_float(si.w);
-                    s.vx = sf.x; s.vy = sf.y; s.vxx = sf.z; s.vyy = sf.w;
-                } else {
-                    s = g.seg_tail[ts];
-                    for (int tt = ts + 1; tt <= te; ++tt) {
-                        const SegSums h = g.seg_head[tt];
-                        s.n_in += h.n_in;
-                        s.vx = __fadd_rn(s.vx, h.vx);
-                        s.vy = __fadd_rn(s.vy, h.vy);
-                        s.vxx = __fadd_rn(s.vxx, h.vxx);
-                        s.vyy = __fadd_rn(s.vyy, h.vyy);
-                        s.vxy = __fadd_rn(s.vxy, h.vxy);
+            if (meas16) {
+                cp_async16(&sm.meas[cl], g.meas_src + k);
+            } else {
+                for (int w = 0; w < 4; ++w)
+                    cp_async4(reinterpret_cast<float*>(&sm.meas[cl]) + w, reinterpret_cast<const float*>(g.meas_src + k) + w);
+            }
+            int src = k;
+            if (g.shifted) {
+                const int sx = k % g.gs + g.shift_x, sy = k / g.gs + g.shift_y;
+                const bool ok = sx > 0 && sx < g.gs && sy > 0 && sy < g.gs;  // strict, as the reference
+                src = ok ? sx + g.gs * sy : -1;
+            }
+            if (src >= 0) cp_async4(&sm.free_prev[cl], g.free_old + src);
+            else sm.free_prev[cl] = 0.0f;
+        }
+        for (int c = threadIdx.x; c < kCellTile; c += kThreads) sm.start[c] = -1;
+        if (threadIdx.x == 0) sm.carry = run_empty(0u);
+        __syncthreads();
+
+        // ---- A: segmented reduction of the tile's particles ------------------------------
+        for (int cb = p0; cb < p1; cb += kSegTile) {
+            const Run carry = sm.carry;  // read before thread 0 rewrites it below
+            const int i0 = cb + threadIdx.x * kSegIpt;
+            uint32_t kw[kSegIpt];
+            float2 v[kSegIpt];
+#pragma unroll
+            for (int r = 0; r < kSegIpt; ++r) {
+                const int i = i0 + r;
+                kw[r] = 0xffffffffu;
+                v[r] = make_float2(0.0f, 0.0f);
+                if (i < p1) {
+                    kw[r] = g.S_key[i];
+                    const float4 st = g.S_state[i];
+                    v[r] = make_float2(st.z, st.w);
+                }
+            }
+            // cells of the particles either side of the thread's span (sentinel outside the tile)
+            const uint32_t kSent = 0xffffffffu;
+            const uint32_t before = (i0 > p0 && i0 <= p1) ? (g.S_key[i0 - 1] & kCellMask) : kSent;
+            const uint32_t after = (i0 + kSegIpt < p1) ? (g.S_key[i0 + kSegIpt] & kCellMask) : kSent;
+            Run cur = run_empty(0u);   // run open at the current particle
+            Run first = run_empty(0u); // the thread's first run, when it continues an earlier one
+            uint32_t first_cell = kSent;
+            int first_last = -1;
+            bool last_tail = false;
+#pragma unroll
+            for (int r = 0; r < kSegIpt; ++r) {
+                const int i = i0 + r;
+                if (i < p1) {
+                    const uint32_t c = kw[r] & kCellMask;
+                    const uint32_t prev = r == 0 ? before : (kw[r - 1] & kCellMask);
+                    const uint32_t next = (r + 1 < kSegIpt && i + 1 < p1) ? (kw[r + 1] & kCellMask) : after;
+                    if (c != prev) {  // segment head
+                        cur = run_empty(kRunHead);
+                        const uint32_t cl = c - (uint32_t)base;
+                        if (cl < (uint32_t)kCellTile) sm.start[cl] = i;
+                    }
+                    run_add(cur, kw[r], v[r]);
+                    last_tail = c != next;
+                    if (last_tail) {  // segment tail
+                        if (cur.fn & kRunHead) {
+                            put_cell(sm, g, c - (uint32_t)base, i, cur);
+                        } else {
+                            first = cur;
+                            first_cell = c;
+                            first_last = i;
+                        }
+                        cur = run_empty(kRunHead);
                     }
                 }
             }
-            float free_prev;
-            if (g.shifted) {
-                const int sx = x + g.shift_x, sy = y + g.shift_y;
-                const bool ok = sx > 0 && sx < g.gs && sy > 0 && sy < g.gs;  // strict, as the reference
-                free_prev = ok ? g.free_old[sx + g.gs * sy] : 0.0f;
-            } else {
-                free_prev = g.free_old[k];
+            // the run this thread passes on: empty after a tail, else the open run
+            const Run out = last_tail ? run_empty(kRunHead) : cur;
+            Run inc = out;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const Run other = run_shfl_up(inc, o);
+                if (lane >= o) inc = run_combine(other, inc);
             }
-            const dogm_measurement_cell m = g.meas_src[k];
+            if (lane == 31) sm.wagg[warp] = inc;
+            Run excl = run_shfl_up(inc, 1);
+            __syncthreads();
+            Run pre = carry;
+            for (int w = 0; w < warp; ++w) pre = run_combine(pre, sm.wagg[w]);
+            if (lane > 0) pre = run_combine(pre, excl);
+            if (first_last >= 0) put_cell(sm, g, first_cell - (uint32_t)base, first_last, run_combine(pre, first));
+            if (threadIdx.x == kThreads - 1) sm.carry = run_combine(pre, out);
+            __syncthreads();
+        }
+
+        // ---- B: per-cell update ----------------------------------------------------------
+        const float c_pred = __fmul_rn(g.p_S, g.fs->w_res);  // predicted weight of an in-grid particle
+        unsigned long long qb = 0ull, jq = 0ull;
+        cp_async_wait_all();  // this thread's own prefetches (B reads only its own cells' slots)
+        for (int r = 0; r < kCellIpt; ++r) {
+            const int cl = r * kThreads + threadIdx.x;
+            const int k = base + cl;
+            if (k >= g.C) break;
+            const bool occupied = sm.start[cl] >= 0;  // end, count and sums are set only then
+            const int start = occupied ? sm.start[cl] : -1, end = occupied ? sm.end[cl] : -1;
+            const int n_in = occupied ? sm.n_in[cl] : 0;
+            const float free_prev = sm.free_prev[cl];
+            const dogm_measurement_cell m = sm.meas[cl];
             if (g.copy_meas) g.meas_own[k] = m;
-            const CellOut o = cell_masses(s.n_in, c_pred, free_prev, g.alpha, g.p_B, m.free_mass, m.occ_mass);
+            const CellOut o = cell_masses(n_in, c_pred, free_prev, g.alpha, g.p_B, m.free_mass, m.occ_mass);
             float muA = 0.0f, muUA = 0.0f, wp = 0.0f;
             float mx = 0.0f, my = 0.0f, vx = 0.0f, vy = 0.0f, cxy = 0.0f;
             if (occupied) {
                 const float wu = __fmul_rn(m.likelihood, o.w_norm);
-                const float swu = __fmul_rn((float)s.n_in, wu);
+                const float swu = __fmul_rn((float)n_in, wu);
                 muA = swu > 0.0f ? __fdiv_rn(o.rho_p, swu) : 0.0f;
                 muUA = o.m_occ_pred > 0.0f ? __fdiv_rn(o.rho_p, o.m_occ_pred) : 0.0f;
                 wp = __fadd_rn(__fmul_rn(__fmul_rn(m.p_A, muA), wu),
                                __fmul_rn(__fmul_rn(__fsub_rn(1.0f, m.p_A), muUA), o.w_norm));
                 if (o.rho_p > 0.0f) {
                     const float inv = __fdiv_rn(1.0f, o.rho_p);
-                    mx = __fmul_rn(inv, __fmul_rn(wp, s.vx));
-                    my = __fmul_rn(inv, __fmul_rn(wp, s.vy));
-                    vx = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vxx)), __fmul_rn(mx, mx));
-                    vy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vyy)), __fmul_rn(my, my));
-                    cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, s.vxy)), __fmul_rn(mx, my));
+                    mx = __fmul_rn(inv, __fmul_rn(wp, sm.vx[cl]));
+                    my = __fmul_rn(inv, __fmul_rn(wp, sm.vy[cl]));
+                    vx = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.vxx[cl])), __fmul_rn(mx, mx));
+                    vy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.vyy[cl])), __fmul_rn(my, my));
+                    cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.vxy[cl])), __fmul_rn(mx, my));
                 }
             }
             float4* rec = reinterpret_cast<float4*>(g.cells + k);
@@ -245,24 +295,15 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
             g.rho_b[k] = o.rho_b;
             g.w_cell[k] = wp;
             qb += quantize(o.rho_b, g.q_shift);
-            // this cell's persistent particles sit at sorted positions [start, end]; their
-            // quantised weights go to the resample tiles that hold them (exact integer adds)
-            const unsigned long long qw = quantize(wp, g.q_shift);
-            if (s.n_in > 0 && qw > 0ull) {
-                jq += (unsigned long long)s.n_in * qw;
-                const int ts = start / kResTile, te = end / kResTile;
-                if (ts == te) {
-                    atomicAdd(&g.res_sum[ts], (unsigned long long)s.n_in * qw);
-                } else {
-                    atomicAdd(&g.res_sum[ts], (unsigned long long)g.seg_tail[ts].n_in * qw);
-                    for (int tt = ts + 1; tt <= te; ++tt)
-                        atomicAdd(&g.res_sum[tt], (unsigned long long)g.seg_head[tt].n_in * qw);
-                }
+            const unsigned long long qw = n_in > 0 ? quantize(wp, g.q_shift) : 0ull;
+            if (qw) {
+                jq += (unsigned long long)n_in * qw;
+                add_persistent(g, start, end, n_in, qw);
             }
         }
         unsigned long long tile_qb, tile_jq;
-        block_excl_scan_u64(qb, red, &tile_qb);
-        block_excl_scan_u64(jq, red2, &tile_jq);
+        block_excl_scan_u64(qb, sm.red, &tile_qb);
+        block_excl_scan_u64(jq, sm.red2, &tile_jq);
         if (threadIdx.x == 0) {
             g.cell_sum[lt] = tile_qb;
             atomicAdd(&g.fs->qb_total, tile_qb);
@@ -388,13 +429,12 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
     }
 }
 
-cudaError_t launch_segments(const Batch* d_batch, const LaunchCfg& cfg) {
-    k_segments<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
-    return cudaGetLastError();
+cudaError_t prepare_cells() {
+    return cudaFuncSetAttribute(k_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CellSmem));
 }
 
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg) {
-    k_cells<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_cells<<<cfg.num_sms * 4, kThreads, sizeof(CellSmem), cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 

@@ -16,8 +16,7 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
     for (int gi = 0; gi < bt->n_grids; ++gi) {
         const GridDesc& g = bt->g[gi];
         for (int i = tid; i < 2 * kSortMaxBins; i += stride) g.hist[i] = 0u;
-        const int words = (g.C + 31) >> 5;
-        for (int i = tid; i < words; i += stride) g.occ_bits[i] = 0u;
+        for (int i = tid; i < g.tiles[kStCell]; i += stride) g.ctile_cnt[i] = 0u;
         for (int i = tid; i < 2 * g.tiles[kStCell]; i += stride) g.cell_sum[i] = 0ull;
         for (int i = tid; i < g.tiles[kStResample]; i += stride) g.res_sum[i] = 0ull;
         // pass-1 digit counts are accumulated by pass 0 (the pass-0 counts are written whole)
@@ -46,6 +45,7 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
 __global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, int mode) {
     __shared__ uint32_t h0[kSortMaxBins];
     __shared__ uint32_t h1[kSortMaxBins];
+    __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (ranges of the cell pass)
     const int total = batch_total(bt, kStPredict);
     const int lane = threadIdx.x & 31;
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, in
         if (mode == 0) {
             for (int i = threadIdx.x; i < nb0; i += kThreads) h0[i] = 0u;
             for (int i = threadIdx.x; i < nb1; i += kThreads) h1[i] = 0u;
+            for (int i = threadIdx.x; i < g.tiles[kStCell]; i += kThreads) h2[i] = 0u;
             __syncthreads();
         }
         const float gsm1 = (float)(g.gs - 1);
@@ -106,6 +107,7 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, in
                     const uint32_t cnt = __popc(peers);
                     atomicAdd(&h0[key & (nb0 - 1)], cnt);
                     atomicAdd(&h1[key >> g.d0_bits], cnt);
+                    atomicAdd(&h2[key >> kCellTileBits], cnt);
                 }
             }
         }
@@ -119,6 +121,8 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, in
             }
             for (int i = threadIdx.x; i < nb1; i += kThreads)
                 if (h1[i]) atomicAdd(&g.hist[kSortMaxBins + i], h1[i]);
+            for (int i = threadIdx.x; i < g.tiles[kStCell]; i += kThreads)
+                if (h2[i]) atomicAdd(&g.ctile_cnt[i], h2[i]);
             __syncthreads();
         }
     }

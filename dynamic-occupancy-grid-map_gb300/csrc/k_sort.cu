@@ -17,6 +17,68 @@ namespace dogm_gb300 {
 // ---------------------------------------------------------------------------------------
 constexpr int kScanWarps = 32;
 constexpr int kScanBatch = 8;
+constexpr int kCtilePer = kMaxCellTiles / (kScanWarps * 32);
+static_assert(kCtilePer * kScanWarps * 32 == kMaxCellTiles, "one block scans every cell-tile count");
+
+// Exclusive scan of the per-cell-tile particle counts that predict took: ctile_start[i] is
+// the first sorted position of cell tile i, ctile_start[n] = N.  Also the claim order of the
+// cell pass: tiles holding more than kFullTile particles first (they take longest), then the
+// rest, each group in index order.  Run by one block as the last work item of the pass-1
+// digit scan (after predict, before the cell pass).
+constexpr uint32_t kFullTile = 2 * kSegTile;
+
+__device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* red2) {
+    const int n = g.tiles[kStCell];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int i0 = threadIdx.x * kCtilePer;
+    uint32_t v[kCtilePer], s = 0u, cls = 0u;  // cls: full tiles << 16 | other tiles
+#pragma unroll
+    for (int j = 0; j < kCtilePer; ++j) {
+        v[j] = (i0 + j < n) ? g.ctile_cnt[i0 + j] : 0u;
+        s += v[j];
+        if (i0 + j < n) cls += v[j] > kFullTile ? (1u << 16) : 1u;
+    }
+    uint32_t x = s, y = cls;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xffffffffu, x, o);
+        const uint32_t b = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o) {
+            x += a;
+            y += b;
+        }
+    }
+    if (lane == 31) {
+        red[warp] = x;
+        red2[warp] = y;
+    }
+    __syncthreads();
+    uint32_t e = x - s, ec = y - cls, tc = 0u;
+    for (int w = 0; w < kScanWarps; ++w) {
+        if (w < warp) {
+            e += red[w];
+            ec += red2[w];
+        }
+        tc += red2[w];
+    }
+    const uint32_t n_full = tc >> 16;
+#pragma unroll
+    for (int j = 0; j < kCtilePer; ++j) {
+        if (i0 + j < n) {
+            g.ctile_start[i0 + j] = e;
+            if (v[j] > kFullTile) {
+                g.ctile_order[ec >> 16] = (uint32_t)(i0 + j);
+                ec += 1u << 16;
+            } else {
+                g.ctile_order[n_full + (ec & 0xffffu)] = (uint32_t)(i0 + j);
+                ec += 1u;
+            }
+        }
+        e += v[j];
+    }
+    if (i0 < n && n <= i0 + kCtilePer) g.ctile_start[n] = e;
+    __syncthreads();
+}
 
 __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict__ bt, int pass) {
     __shared__ uint32_t chunk[kScanWarps][33];
@@ -28,6 +90,10 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict
         const int gi = grid_of_tile(bt, stage, t);
         const GridDesc& g = bt->g[gi];
         const int group = t - bt->prefix[gi][stage];
+        if (pass == 1 && group == g.tiles[kStScan1] - 1) {  // block-uniform
+            ctile_scan(g, red, &chunk[0][0]);
+            continue;
+        }
         const int nb = 1 << (pass ? g.d1_bits : g.d0_bits);
         const int b = group * 32 + lane;
         const uint32_t* hist = g.hist + pass * kSortMaxBins;

@@ -38,9 +38,9 @@ int bitlen(unsigned long long v) {
 
 int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-constexpr int kStages = 10;
-const char* const kStageNames[kStages] = {"frame_begin", "predict",  "sort_scan0", "sort_pass0", "sort_scan1",
-                                          "sort_pass1",  "segments", "cells",      "newborn",    "resample"};
+constexpr int kStages = 9;
+const char* const kStageNames[kStages] = {"frame_begin", "predict", "sort_scan0", "sort_pass0", "sort_scan1",
+                                          "sort_pass1",  "cells",   "newborn",    "resample"};
 
 // One launch context: a device copy of a Batch, two pinned host mirrors (the host fills one
 // while the device may still read the other, so frame k+1 is queued while frame k runs) and
@@ -141,7 +141,7 @@ dogm_status dalloc(dogm_handle* h, T** p, size_t count) {
 }
 
 struct Sizes {
-    int gs, N, B, C, key_bits, sort_tiles, seg_tiles, cell_tiles, res_tiles, pred_tiles, scan0, scan1;
+    int gs, N, B, C, key_bits, sort_tiles, cell_tiles, res_tiles, pred_tiles, scan0, scan1;
 };
 
 dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
@@ -158,12 +158,11 @@ dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
     if (s.B < 0 || s.B > kMaxParticles) return fail(DOGM_ERR_UNSUPPORTED, "new_born_particle_count must be in [0, 2^24)");
     s.pred_tiles = div_up(s.N, kPredictTile);
     s.sort_tiles = div_up(s.N, kSortTile);
-    s.seg_tiles = div_up(s.N, kSegTile);
     s.cell_tiles = div_up(s.C, kCellTile);
     s.res_tiles = div_up((long long)s.N + s.B, kResTile);
     const int d0 = (s.key_bits + 1) / 2, d1 = s.key_bits - d0;
     s.scan0 = div_up(1 << d0, 32);  // digit groups of the column scans
-    s.scan1 = div_up(1 << d1, 32);
+    s.scan1 = div_up(1 << d1, 32) + 1;  // + the cell-tile start scan
     return DOGM_OK;
 }
 
@@ -174,7 +173,6 @@ void set_tiles(GridDesc& g, const Sizes& s) {
     g.tiles[kStSort0] = s.sort_tiles;
     g.tiles[kStScan1] = s.scan1;
     g.tiles[kStSort1] = s.sort_tiles;
-    g.tiles[kStSeg] = s.seg_tiles;
     g.tiles[kStCell] = s.cell_tiles;
     g.tiles[kStBirth] = s.cell_tiles;
     g.tiles[kStResample] = s.res_tiles;
@@ -278,10 +276,9 @@ cudaError_t frame_kernels(Ctx& c, bool with_init) {
     STAGE(3, launch_sort_pass(c.d_batch, 0, cfg));
     STAGE(4, launch_sort_scan(c.d_batch, 1, cfg));
     STAGE(5, launch_sort_pass(c.d_batch, 1, cfg));
-    STAGE(6, launch_segments(c.d_batch, cfg));
-    STAGE(7, launch_cells(c.d_batch, cfg));
-    STAGE(8, launch_newborn(c.d_batch, cfg));
-    STAGE(9, launch_resample(c.d_batch, cfg));
+    STAGE(6, launch_cells(c.d_batch, cfg));
+    STAGE(7, launch_newborn(c.d_batch, cfg));
+    STAGE(8, launch_resample(c.d_batch, cfg));
 #undef STAGE
     if (prof && (e = cudaEventRecord(c.ev[kStages], c.stream)) != cudaSuccess) return e;
     return cudaSuccess;
@@ -417,11 +414,10 @@ size_t dogm_state_bytes(const dogm_params* p) {
     size_t b = 0;
     b += N * (16 + 4) + N * (4 + 4) + N * (16 + 4);    // P, T, S particles
     b += B * (16 + 4 + 4);                            // newborns
-    // per cell: record 64, measurement copy 16, free mass 2 x 4, segment sums 32, newborn
-    // mass 4, cell weight 4, occupancy bit
-    b += C * (sizeof(dogm_grid_cell) + sizeof(dogm_measurement_cell) + 2 * 4 + 32 + 4 + 4) + C / 8;
+    // per cell: record 64, measurement copy 16, free mass 2 x 4, newborn mass 4, cell weight 4
+    b += C * (sizeof(dogm_grid_cell) + sizeof(dogm_measurement_cell) + 2 * 4 + 4 + 4);
     b += 2 * kSortMaxBins * 4 + (size_t)2 * s.sort_tiles * kSortMaxBins * 4;
-    b += (size_t)s.seg_tiles * 2 * sizeof(SegSums) + (size_t)s.cell_tiles * 16 + (size_t)s.res_tiles * 8;
+    b += (size_t)s.cell_tiles * (16 + 12) + 4 + (size_t)s.res_tiles * 8;
     b += sizeof(Batch);
     return b;
 }
@@ -440,7 +436,8 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     h->gs = s.gs; h->N = s.N; h->B = s.B; h->C = s.C;
     auto cleanup = [&](dogm_status s2) { dogm_destroy(h); return s2; };
     if ((st = ctx_init(h->ctx, h->device)) != DOGM_OK) return cleanup(st);
-    if (prepare_kernels() != cudaSuccess) return cleanup(fail(DOGM_ERR_CUDA, "kernel attribute setup failed"));
+    if (prepare_kernels() != cudaSuccess || prepare_cells() != cudaSuccess)
+        return cleanup(fail(DOGM_ERR_CUDA, "kernel attribute setup failed"));
 
     GridDesc& g = h->desc;
     g.N = s.N; g.B = s.B; g.C = s.C; g.gs = s.gs;
@@ -471,12 +468,11 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     float* fa = nullptr; float* fb = nullptr;
     ALLOC(fa, s.C); ALLOC(fb, s.C);
     g.free_old = fa; g.free_new = fb;
-    ALLOC(g.seg_i, s.C); ALLOC(g.seg_f, s.C);
     ALLOC(g.rho_b, s.C); ALLOC(g.w_cell, s.C);
-    ALLOC(g.occ_bits, (s.C + 31) / 32);
     ALLOC(g.hist, 2 * kSortMaxBins);
     ALLOC(g.hsort, (size_t)2 * s.sort_tiles * kSortMaxBins);
-    ALLOC(g.seg_head, s.seg_tiles); ALLOC(g.seg_tail, s.seg_tiles);
+    ALLOC(g.ctile_cnt, s.cell_tiles); ALLOC(g.ctile_start, (size_t)s.cell_tiles + 1);
+    ALLOC(g.ctile_order, s.cell_tiles);
     ALLOC(g.cell_sum, 2 * (size_t)s.cell_tiles);
     ALLOC(g.res_sum, s.res_tiles);
     ALLOC(g.fs, 1);
