@@ -6,29 +6,52 @@
 // 2^-q_shift and scanned exactly (integer, order-independent; a tile's prefix is the sum of the
 // per-tile sums that the cell and newborn kernels accumulated), and
 // systematic resampling assigns output slot i to the joint particle j with
-// A[j-1]*N <= i*T + U < A[j]*N, so each particle writes its own copies directly.
+// A[j-1]*N <= i*T + U < A[j]*N.  A tile's items are staged in shared memory; their first
+// output slots come from the blocked exact scan, and the copies are written with
+// consecutive items on consecutive lanes, so the stores of a warp are contiguous.
 // The new common weight is T / N (dogm.cu:417).
 #include "dogm_device.cuh"
 
 namespace dogm_gb300 {
 
-// A heavy item (more copies than an item writes itself) expanded by the whole block.
-struct HeavyItem {
-    float4 st;
-    uint32_t kw;
-    int first, end, item;
+// Copy counts per item: comb_count(a) = #{ i in [0,N) : i*T + U < a*N }, starting from a
+// float estimate (inv_T = 1/T rounded) that the exact 96-bit checks then correct.
+__device__ __forceinline__ int comb_count_est(unsigned long long a, unsigned long long T, unsigned long long U, int N,
+                                              float inv_T) {
+    if (T == 0ull || a >= T) return N;
+    const U96 rhs = mul_u64_u32(a, (unsigned int)N);
+    const float f = __fmul_rn(__fsub_rn(__fmul_rn(__ull2float_rn(a), (float)N), __ull2float_rn(U)), inv_T);
+    int c = (int)ceilf(f);
+    c = c < 0 ? 0 : (c > N ? N : c);
+    // P(i): i*T + U < a*N holds for i < result and fails from result on
+    while (c > 0 && !lt96(add96(mul_u64_u32(T, (unsigned int)(c - 1)), U), rhs)) --c;
+    while (c < N && lt96(add96(mul_u64_u32(T, (unsigned int)c), U), rhs)) ++c;
+    return c;
+}
+
+// Shared words of a tile indexed with one pad word per 32, so that both the blocked
+// (thread t: items 8t..8t+7) and the warp-striped (item r*256 + t) accesses are free of
+// bank conflicts.
+__device__ __forceinline__ int pad_idx(int j) { return j + (j >> 5); }
+constexpr int kResPadded = kResTile + 1 + ((kResTile + 1) >> 5) + 1;
+
+struct HeavyRef {
+    int item, first, end;  // a joint item with more copies than one thread writes
 };
-constexpr int kOwnCopies = 8;        // an item writes up to this many copies itself
-constexpr int kMaxHeavy = 768;       // heavy items per tile expanded cooperatively (more: by their thread)
+constexpr int kOwnCopies = 8;
+constexpr int kMaxHeavy = 256;
 
 struct ResSmem {
-    HeavyItem heavy[kMaxHeavy];    // items with many copies
+    float4 st[kResTile];         // states of the tile's joint items
+    uint32_t kw[kResTile];       // their key words
+    uint32_t lw[kResPadded];     // weight (float bits), then first output slot of each item (+ end)
+    HeavyRef heavy[kMaxHeavy];
     unsigned long long red[2 * (kThreads / 32)];
     int nheavy;
     int claim;
 };
 
-__global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt) {
+__global__ void __launch_bounds__(kThreads, 4) k_resample(Batch* __restrict__ bt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ResSmem& sm = *reinterpret_cast<ResSmem*>(smem_raw);
     const int total = batch_total(bt, kStResample);
@@ -45,39 +68,20 @@ __global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt
         const int N = g.N, C = g.C, gs = g.gs, S = g.q_shift;
         const int M = N + g.fs->n_birth;
         const unsigned long long T = g.fs->joint_total;
-        const uint32_t* __restrict__ S_key = g.S_key;
-        const float4* __restrict__ S_state = g.S_state;
-        const float* __restrict__ w_cell = g.w_cell;
-        const dogm_grid_cell* __restrict__ cells = g.cells;
-        float4* __restrict__ P_state = g.P_state;
-        uint32_t* __restrict__ P_key = g.P_key;
-        int* __restrict__ dbg_src = g.dbg_src;
         if (threadIdx.x == 0) sm.nheavy = 0;
-        unsigned long long r64;
-        if (g.rp_resample) {
-            r64 = *g.rp_resample;
-        } else {
-            const U4 r = draw_block(g, 0u, g.frame, kDrawResample);
-            r64 = ((unsigned long long)r.x << 32) | r.y;
-        }
-        const unsigned long long U = __umul64hi(r64, T);  // floor(u * T), u = r64 / 2^64
 
-        // this thread's kResIpt consecutive joint items, in registers
-        float4 st[kResIpt];
-        uint32_t kw[kResIpt];
-        float wq[kResIpt];
-        unsigned long long v = 0ull;
-        const int j0 = threadIdx.x * kResIpt;
-#pragma unroll
+        // ---- 1: the tile's joint items, loaded warp-striped into shared memory -----------
+#pragma unroll 2
         for (int r = 0; r < kResIpt; ++r) {
-            const int p = base + j0 + r;
+            const int j = r * kThreads + threadIdx.x;
+            const int p = base + j;
+            float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
+            uint32_t kw = 0u;
             float w = 0.0f;
-            st[r] = make_float4(0.f, 0.f, 0.f, 0.f);
-            kw[r] = 0u;
             if (p < N) {
-                kw[r] = S_key[p];
-                st[r] = S_state[p];
-                w = (kw[r] & kOutBit) ? 0.0f : w_cell[kw[r] & kCellMask];
+                kw = g.S_key[p];
+                st = g.S_state[p];
+                w = (kw & kOutBit) ? 0.0f : g.w_cell[kw & kCellMask];
             } else if (p < M) {
                 // newborn slot b (initNewParticlesKernel2, init_new_particles.cu:157-195): cell
                 // and associated flag from the key word the newborn kernel wrote
@@ -92,56 +96,89 @@ __global__ void __launch_bounds__(kThreads, 3) k_resample(Batch* __restrict__ bt
                     const U4 rr = draw_block(g, (uint32_t)b, g.frame, kDrawBirth);
                     z = box_muller(rr.x, rr.y);
                 }
-                st[r].x = __fadd_rn((float)(k % gs), 0.5f);
-                st[r].y = __fadd_rn(__fdiv_rn((float)k, (float)gs), 0.5f);  // float division, as the reference
-                st[r].z = __fmaf_rn(z.x, g.sigma_birth, 0.0f);
-                st[r].w = __fmaf_rn(z.y, g.sigma_birth, 0.0f);
-                kw[r] = (uint32_t)k | (assoc ? kAssocBit : 0u);
-                w = assoc ? cells[k].w_A : cells[k].w_UA;
+                st.x = __fadd_rn((float)(k % gs), 0.5f);
+                st.y = __fadd_rn(__fdiv_rn((float)k, (float)gs), 0.5f);  // float division, as the reference
+                st.z = __fmaf_rn(z.x, g.sigma_birth, 0.0f);
+                st.w = __fmaf_rn(z.y, g.sigma_birth, 0.0f);
+                kw = (uint32_t)k | (assoc ? kAssocBit : 0u);
+                w = assoc ? g.cells[k].w_A : g.cells[k].w_UA;
                 if (g.dbg_perm) {  // debug export of the newborns
-                    g.B_state[b] = st[r];
+                    g.B_state[b] = st;
                     g.B_w[b] = w;
                 }
             }
-            kw[r] &= ~kOutBit;
-            wq[r] = (p < M) ? w : 0.0f;
-            v += quantize(wq[r], S);
+            sm.st[j] = st;
+            sm.kw[j] = kw & ~kOutBit;
+            sm.lw[pad_idx(j)] = __float_as_uint(w);
+        }
+        __syncthreads();
+
+        // ---- 2: exact scan (blocked) -> first output slot of every item -----------------
+        unsigned long long r64;
+        if (g.rp_resample) {
+            r64 = *g.rp_resample;
+        } else {
+            const U4 r = draw_block(g, 0u, g.frame, kDrawResample);
+            r64 = ((unsigned long long)r.x << 32) | r.y;
+        }
+        const unsigned long long U = __umul64hi(r64, T);  // floor(u * T), u = r64 / 2^64
+        const float inv_T = T ? __frcp_rn(__ull2float_rn(T)) : 0.0f;
+        const int j0 = threadIdx.x * kResIpt;
+        unsigned long long q[kResIpt];
+        unsigned long long v = 0ull;
+#pragma unroll
+        for (int r = 0; r < kResIpt; ++r) {
+            q[r] = quantize(__uint_as_float(sm.lw[pad_idx(j0 + r)]), S);
+            v += q[r];
         }
         unsigned long long tile_sum;
         unsigned long long acc = block_scan_after(v, g.res_sum, lt, sm.red, &tile_sum);
-        int lo_s = (base + j0 == 0) ? 0 : comb_count(acc, T, U, N);
+        int lo_s = (base + j0 == 0) ? 0 : comb_count_est(acc, T, U, N, inv_T);
 #pragma unroll
         for (int r = 0; r < kResIpt; ++r) {
-            acc += quantize(wq[r], S);
-            const int hi_s = comb_count(acc, T, U, N);
-            bool own = hi_s - lo_s <= kOwnCopies;
-            if (!own) {
-                const int h = atomicAdd(&sm.nheavy, 1);
-                if (h < kMaxHeavy) {
-                    HeavyItem e;
-                    e.st = st[r]; e.kw = kw[r]; e.first = lo_s; e.end = hi_s; e.item = base + j0 + r;
-                    sm.heavy[h] = e;
-                } else {
-                    own = true;  // list full: this thread writes the copies itself
+            sm.lw[pad_idx(j0 + r)] = (uint32_t)lo_s;  // this thread read the slot above
+            acc += q[r];
+            if (q[r]) lo_s = comb_count_est(acc, T, U, N, inv_T);
+        }
+        if (threadIdx.x == kThreads - 1) sm.lw[pad_idx(kResTile)] = (uint32_t)lo_s;
+        __syncthreads();
+
+        // ---- 3: copies, consecutive items on consecutive lanes (coalesced stores) --------
+        float4* __restrict__ P_state = g.P_state;
+        uint32_t* __restrict__ P_key = g.P_key;
+        int* __restrict__ dbg_src = g.dbg_src;
+#pragma unroll 2
+        for (int r = 0; r < kResIpt; ++r) {
+            const int j = r * kThreads + threadIdx.x;
+            const int first = (int)sm.lw[pad_idx(j)], end = (int)sm.lw[pad_idx(j + 1)];
+            if (end > first) {
+                bool own = end - first <= kOwnCopies;
+                if (!own) {
+                    const int h = atomicAdd(&sm.nheavy, 1);
+                    if (h < kMaxHeavy) sm.heavy[h] = HeavyRef{j, first, end};
+                    else own = true;  // list full: this thread writes the copies itself
+                }
+                if (own) {
+                    const float4 st = sm.st[j];
+                    const uint32_t kw = sm.kw[j];
+                    for (int s = first; s < end; ++s) {
+                        P_state[s] = st;
+                        P_key[s] = kw;
+                        if (dbg_src) dbg_src[s] = base + j;
+                    }
                 }
             }
-            if (own) {
-                for (int s = lo_s; s < hi_s; ++s) {
-                    P_state[s] = st[r];
-                    P_key[s] = kw[r];
-                    if (dbg_src) dbg_src[s] = base + j0 + r;
-                }
-            }
-            lo_s = hi_s;
         }
         __syncthreads();
         const int nh = min(sm.nheavy, kMaxHeavy);
         for (int h = 0; h < nh; ++h) {
-            const HeavyItem e = sm.heavy[h];
+            const HeavyRef e = sm.heavy[h];
+            const float4 st = sm.st[e.item];
+            const uint32_t kw = sm.kw[e.item];
             for (int s = e.first + threadIdx.x; s < e.end; s += kThreads) {
-                P_state[s] = e.st;
-                P_key[s] = e.kw;
-                if (dbg_src) dbg_src[s] = e.item;
+                P_state[s] = st;
+                P_key[s] = kw;
+                if (dbg_src) dbg_src[s] = base + e.item;
             }
         }
         if (lt == 0 && threadIdx.x == 0) {
@@ -158,7 +195,7 @@ cudaError_t prepare_kernels() {
 
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg) {
     const int smem = (int)sizeof(ResSmem);
-    k_resample<<<cfg.num_sms * 3, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_resample<<<cfg.num_sms * 4, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 
