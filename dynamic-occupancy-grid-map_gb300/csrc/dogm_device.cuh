@@ -172,6 +172,22 @@ __device__ __forceinline__ CellOut cell_masses(int n_in, float c, float free_pre
 }
 
 // ---------------------------------------------------------------------------------------
+// Asynchronous global -> shared copies (cp.async): a thread's copies land while it works on
+// something else; cp_async_wait_all() makes that thread's own copies visible to it.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// ---------------------------------------------------------------------------------------
 // Batches: tile claiming and grid lookup.
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ int batch_total(const Batch* bt, int stage) { return bt->prefix[bt->n_grids][stage]; }
@@ -259,7 +275,15 @@ __device__ __forceinline__ unsigned long long block_scan_after(unsigned long lon
                                                                unsigned long long* total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long part = 0ull;
-    for (int i = threadIdx.x; i < t; i += blockDim.x) part += sums[i];
+    for (int i0 = 0; i0 < t; i0 += 4 * kThreads) {  // four independent loads in flight per thread
+        unsigned long long a[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u * kThreads + (int)threadIdx.x;
+            a[u] = i < t ? sums[i] : 0ull;
+        }
+        part += (a[0] + a[1]) + (a[2] + a[3]);
+    }
     unsigned long long x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {

@@ -96,18 +96,6 @@ struct CellSmem {
 };
 static_assert(offsetof(CellSmem, meas) % 16 == 0, "16-byte cp.async destination");
 
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
-                 "l"(gmem)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
-                 "l"(gmem)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
 // The quantised weights of a cell's in-grid persistent particles (sorted positions
 // [start, end]) added to the resample tiles that hold them.  Out-of-grid particles (weight
 // 0) lie only in border cells; only for those is a split across tiles counted from the keys.

@@ -70,19 +70,35 @@ __global__ void __launch_bounds__(kThreads, 4) k_resample(Batch* __restrict__ bt
         const unsigned long long T = g.fs->joint_total;
         if (threadIdx.x == 0) sm.nheavy = 0;
 
-        // ---- 1: the tile's joint items, loaded warp-striped into shared memory -----------
-#pragma unroll 2
+        // ---- 1: the tile's joint items, warp-striped into shared memory -------------------
+        // persistent items: asynchronous copies, then one batch of cell-weight gathers
+#pragma unroll
+        for (int r = 0; r < kResIpt; ++r) {
+            const int p = base + r * kThreads + (int)threadIdx.x;
+            if (p < N) {
+                cp_async16(&sm.st[p - base], g.S_state + p);
+                cp_async4(&sm.kw[p - base], g.S_key + p);
+            }
+        }
+        cp_async_wait_all();
+#pragma unroll
+        for (int r = 0; r < kResIpt; ++r) {
+            const int j = r * kThreads + threadIdx.x;
+            if (base + j < N) {
+                const uint32_t kw = sm.kw[j];
+                sm.lw[pad_idx(j)] = __float_as_uint((kw & kOutBit) ? 0.0f : g.w_cell[kw & kCellMask]);
+                sm.kw[j] = kw & ~kOutBit;
+            }
+        }
+        // newborn items, created here, and the empty tail of the last tile
         for (int r = 0; r < kResIpt; ++r) {
             const int j = r * kThreads + threadIdx.x;
             const int p = base + j;
+            if (p < N) continue;
             float4 st = make_float4(0.f, 0.f, 0.f, 0.f);
             uint32_t kw = 0u;
             float w = 0.0f;
-            if (p < N) {
-                kw = g.S_key[p];
-                st = g.S_state[p];
-                w = (kw & kOutBit) ? 0.0f : g.w_cell[kw & kCellMask];
-            } else if (p < M) {
+            if (p < M) {
                 // newborn slot b (initNewParticlesKernel2, init_new_particles.cu:157-195): cell
                 // and associated flag from the key word the newborn kernel wrote
                 const int b = p - N;
@@ -108,7 +124,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_resample(Batch* __restrict__ bt
                 }
             }
             sm.st[j] = st;
-            sm.kw[j] = kw & ~kOutBit;
+            sm.kw[j] = kw;
             sm.lw[pad_idx(j)] = __float_as_uint(w);
         }
         __syncthreads();
@@ -133,12 +149,29 @@ __global__ void __launch_bounds__(kThreads, 4) k_resample(Batch* __restrict__ bt
         }
         unsigned long long tile_sum;
         unsigned long long acc = block_scan_after(v, g.res_sum, lt, sm.red, &tile_sum);
+        // first slot of the thread's first item; later boundaries walk the comb tooth by tooth
+        // (tooth = lo_s*T + U, exact 96-bit), or jump for an item with many copies
         int lo_s = (base + j0 == 0) ? 0 : comb_count_est(acc, T, U, N, inv_T);
+        U96 tooth = add96(mul_u64_u32(T, (unsigned int)lo_s), U);
 #pragma unroll
         for (int r = 0; r < kResIpt; ++r) {
             sm.lw[pad_idx(j0 + r)] = (uint32_t)lo_s;  // this thread read the slot above
             acc += q[r];
-            if (q[r]) lo_s = comb_count_est(acc, T, U, N, inv_T);
+            if (T == 0ull) {
+                lo_s = N;  // no weight at all: every slot goes to the first item
+            } else if (q[r]) {
+                const float copies = __fmul_rn(__fmul_rn(__ull2float_rn(q[r]), (float)N), inv_T);
+                if (copies < 32.0f) {
+                    const U96 rhs = mul_u64_u32(acc, (unsigned int)N);
+                    while (lo_s < N && lt96(tooth, rhs)) {
+                        ++lo_s;
+                        tooth = add96(tooth, T);
+                    }
+                } else {
+                    lo_s = comb_count_est(acc, T, U, N, inv_T);
+                    tooth = add96(mul_u64_u32(T, (unsigned int)lo_s), U);
+                }
+            }
         }
         if (threadIdx.x == kThreads - 1) sm.lw[pad_idx(kResTile)] = (uint32_t)lo_s;
         __syncthreads();

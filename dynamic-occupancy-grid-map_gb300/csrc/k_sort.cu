@@ -156,10 +156,12 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict
 struct SortSmem {
     uint16_t whist[kThreads / 32][kSortMaxBins];  // per-warp digit counts, then warp offsets
     uint32_t gbase[kSortMaxBins];                  // global offset of each digit for this tile
+    uint16_t rank[kSortTile];                      // rank of each key among its warp's equal digits
 };
 
+// Four blocks per SM: a 2M-particle frame's 489 tiles run in one wave.
 template <bool FINAL>
-__global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* __restrict__ bt) {
+__global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ bt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SortSmem& sm = *reinterpret_cast<SortSmem*>(smem_raw);
     const int stage = FINAL ? kStSort1 : kStSort0;
@@ -177,33 +179,29 @@ __global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* __restrict__ b
         const int nb = 1 << bits;
         const uint32_t* O = g.hsort + (size_t)pass * g.sort_tiles * kSortMaxBins + (size_t)lt * kSortMaxBins;
         for (int i = threadIdx.x; i < nb; i += kThreads) sm.gbase[i] = O[i];
-        for (int i = threadIdx.x; i < (kThreads / 32) * nb; i += kThreads) sm.whist[i / nb][i % nb] = 0;
+        uint4* wz = reinterpret_cast<uint4*>(&sm.whist[0][0]);  // all warp counts, 16 bytes a store
+        for (int i = threadIdx.x; i < (int)(sizeof(sm.whist) / sizeof(uint4)); i += kThreads)
+            wz[i] = make_uint4(0u, 0u, 0u, 0u);
         __syncthreads();
 
         // load the tile warp-striped (item k of lane l: warp base + k*32 + l)
         const int base = lt * kSortTile + warp * (32 * kSortIpt);
-        uint32_t key[kSortIpt], val[kSortIpt];
-        uint16_t rank[kSortIpt];
+        uint16_t* rank = sm.rank + warp * (32 * kSortIpt) + lane;  // item k at rank[k * 32]
+        uint32_t key[kSortIpt];
 #pragma unroll
         for (int k = 0; k < kSortIpt; ++k) {
             const int pos = base + k * 32 + lane;
-            if (pos < g.N) {
-                key[k] = FINAL ? g.T_key[pos] : g.P_key[pos];
-                val[k] = FINAL ? g.T_idx[pos] : (uint32_t)pos;
-            } else {
-                key[k] = 0xffffffffu;
-                val[k] = 0xffffffffu;
-            }
+            key[k] = pos < g.N ? (FINAL ? g.T_key[pos] : g.P_key[pos]) : 0xffffffffu;
         }
         // stable rank within the warp: rounds in input order, peers by match_any
 #pragma unroll
         for (int k = 0; k < kSortIpt; ++k) {
-            const bool valid = val[k] != 0xffffffffu;
+            const bool valid = base + k * 32 + lane < g.N;
             const uint32_t d = valid ? (((key[k] & kCellMask) >> shift) & (uint32_t)(nb - 1)) : 0xffffffffu;
             const uint32_t peers = __match_any_sync(0xffffffffu, d);
             uint16_t before = 0;
             if (valid) before = sm.whist[warp][d];
-            rank[k] = (uint16_t)(before + __popc(peers & lt_mask));
+            rank[k * 32] = (uint16_t)(before + __popc(peers & lt_mask));
             __syncwarp();
             if (valid && lane == __ffs(peers) - 1) sm.whist[warp][d] = (uint16_t)(before + __popc(peers));
             __syncwarp();
@@ -227,11 +225,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* __restrict__ b
         const uint32_t nb1m = (1u << g.d1_bits) - 1u;
 #pragma unroll
         for (int k = 0; k < kSortIpt; ++k) {
-            const bool valid = val[k] != 0xffffffffu;
+            const int pos = base + k * 32 + lane;
+            const bool valid = pos < g.N;
             uint32_t out = 0xffffffffu;
             if (valid) {
                 const uint32_t d = ((key[k] & kCellMask) >> shift) & (uint32_t)(nb - 1);
-                out = sm.gbase[d] + sm.whist[warp][d] + rank[k];
+                out = sm.gbase[d] + sm.whist[warp][d] + rank[k * 32];
                 if (out >= (uint32_t)g.N) {  // only an inconsistent histogram can get here
                     flag_status(g, kStatusBounds);
                     out = 0xffffffffu;
@@ -239,15 +238,16 @@ __global__ void __launch_bounds__(kThreads, 2) k_sort_pass(Batch* __restrict__ b
             }
             if (FINAL) {
                 if (out != 0xffffffffu) {
+                    const uint32_t src = g.T_idx[pos];  // particle index carried by pass 0
                     g.S_key[out] = key[k];
-                    g.S_state[out] = g.P_state[val[k]];
-                    if (g.dbg_perm) g.dbg_perm[out] = (int)val[k];
+                    g.S_state[out] = g.P_state[src];
+                    if (g.dbg_perm) g.dbg_perm[out] = (int)src;
                 }
             } else {
                 uint32_t hk = 0xffffffffu;
                 if (out != 0xffffffffu) {
                     g.T_key[out] = key[k];
-                    g.T_idx[out] = val[k];
+                    g.T_idx[out] = (uint32_t)pos;
                     const uint32_t d1 = ((key[k] & kCellMask) >> shift1) & nb1m;
                     hk = ((out / (uint32_t)kSortTile) << kSortMaxBits) | d1;
                 }
@@ -267,12 +267,12 @@ cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cf
 }
 
 cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
-    const size_t smem = sizeof(SortSmem);  // < 48 KB: no opt-in attribute needed
+    const size_t smem = sizeof(SortSmem);  // 48 KB: no opt-in attribute needed
     Batch* b = const_cast<Batch*>(d_batch);
     if (pass == 0)
-        k_sort_pass<false><<<cfg.num_sms * 2, kThreads, smem, cfg.stream>>>(b);
+        k_sort_pass<false><<<cfg.num_sms * 4, kThreads, smem, cfg.stream>>>(b);
     else
-        k_sort_pass<true><<<cfg.num_sms * 2, kThreads, smem, cfg.stream>>>(b);
+        k_sort_pass<true><<<cfg.num_sms * 4, kThreads, smem, cfg.stream>>>(b);
     return cudaGetLastError();
 }
 
