@@ -201,7 +201,7 @@ def run_gb300(args, rank: int, world: int):
     b.build_cuda()
     dogm.load()
     K, W = args.steps, args.warmup
-    P = 5  # profiled updates
+    P = 24  # profiled updates (event pairs tick coarsely: the stage times are means)
     # steps: [0, W] warm-up, then K timed, K end-to-end, P profiled; measurement grids come
     # from a pool of distinct frames cycled forth and back (pingpong)
     t0_, e0_, p0_ = W + 1, W + 1 + K, W + 1 + 2 * K
@@ -275,7 +275,7 @@ def run_gb300(args, rank: int, world: int):
         g.synchronize()
         stage_runs.append(g.stage_times())
     g.profile_enable(False)
-    stages = {k: statistics.median(r[k] for r in stage_runs) for k in stage_runs[0]}
+    stages = {k: statistics.fmean(r[k] for r in stage_runs) for k in stage_runs[0]}
     cells = g.get_grid_cells()
     n_occ = int((cells["start_idx"] >= 0).sum())
     n_bcells = int(((cells["w_A"] > 0) | (cells["w_UA"] > 0)).sum())

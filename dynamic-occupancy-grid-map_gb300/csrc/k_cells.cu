@@ -308,26 +308,35 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
 // newborn slot, and the newborns' quantised weights into the resample tiles that will hold
 // them.
 // ---------------------------------------------------------------------------------------
-__device__ __forceinline__ void add_joint_range(TileAgg& agg, unsigned long long* res_sum, long long a, long long b,
+constexpr int kRunTiles = 4;  // resample tiles a thread accumulates in registers
+
+// q per slot over joint positions [a, b), added per resample tile: the first kRunTiles tiles
+// from rt0 in registers, any further ones straight to the global sums.
+__device__ __forceinline__ void add_joint_range(unsigned long long (&racc)[kRunTiles], long long rt0,
+                                                unsigned long long* res_sum, long long a, long long b,
                                                 unsigned long long q) {
     if (q == 0ull) return;
-    for (long long t = a / kResTile; t * kResTile < b; ++t) {
-        const long long lo = max(a, t * (long long)kResTile);
-        const long long hi = min(b, (t + 1) * (long long)kResTile);
-        if (hi > lo) agg_add(agg, res_sum, t, (unsigned long long)(hi - lo) * q);
+    for (long long rt = a / kResTile; rt * kResTile < b; ++rt) {
+        const long long lo = max(a, rt * (long long)kResTile);
+        const long long hi = min(b, (rt + 1) * (long long)kResTile);
+        if (hi <= lo) continue;
+        const unsigned long long v = (unsigned long long)(hi - lo) * q;
+        const long long o = rt - rt0;
+        if (o >= 0 && o < kRunTiles) {
+#pragma unroll
+            for (int i = 0; i < kRunTiles; ++i) racc[i] += (o == i) ? v : 0ull;
+        } else {
+            atomicAdd(&res_sum[rt], v);
+        }
     }
 }
 
-constexpr int kOwnSlots = 16;  // newborn slots a thread fills for its own cell
-
 __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
     __shared__ unsigned long long red[2 * (kThreads / 32)];
-    __shared__ TileAgg agg;
-    __shared__ int s_bnd[kCellTile + 1];  // s_bnd[c]: first slot of cell c of the tile
+    __shared__ int s_bnd[kCellTile + 1];  // s_bnd[c]: first slot of cell c of the tile; [kCellTile]: end
     __shared__ int s_nuA[kCellTile];
-    __shared__ int s_heavy[kCellTile];
-    __shared__ int s_nheavy;
     const int total = batch_total(bt, kStBirth);
+    const int lane = threadIdx.x & 31;
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStBirth, t);
         const GridDesc& g = bt->g[gi];
@@ -335,82 +344,70 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
         const int base = lt * kCellTile;
         const unsigned long long T = g.fs->qb_total;
         unsigned long long q[kCellIpt];
-        float rb[kCellIpt];
+        float rb[kCellIpt], pA[kCellIpt];
         unsigned long long v = 0ull;
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
             const int k = base + threadIdx.x * kCellIpt + j;
             rb[j] = (k < g.C) ? g.rho_b[k] : 0.0f;
             q[j] = (k < g.C) ? quantize(rb[j], g.q_shift) : 0ull;
+            pA[j] = q[j] ? g.meas_own[k].p_A : 0.0f;  // only a cell with mass can get newborns
             v += q[j];
         }
         unsigned long long tile_sum;
         unsigned long long acc = block_scan_after(v, g.cell_sum, lt, red, &tile_sum);
         const float sc = T ? __fdiv_rn((float)g.B, __ull2float_rn(T)) : 0.0f;
-        int lo_c = alloc_boundary_fast(acc, T, g.B, sc);
-        if (threadIdx.x == 0) {
-            s_bnd[0] = lo_c;
-            s_nheavy = 0;
-        }
-        __syncthreads();
-        agg_reset(agg, ((long long)g.N + s_bnd[0]) / kResTile);
         int bnd[kCellIpt + 1];
-        bnd[0] = lo_c;
+        bnd[0] = alloc_boundary_fast(acc, T, g.B, sc);
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
             acc += q[j];
             bnd[j + 1] = q[j] ? alloc_boundary_fast(acc, T, g.B, sc) : bnd[j];
-            s_bnd[threadIdx.x * kCellIpt + j + 1] = bnd[j + 1];
+            s_bnd[threadIdx.x * kCellIpt + j] = bnd[j];
         }
+        if (threadIdx.x == kThreads - 1) s_bnd[kCellTile] = bnd[kCellIpt];
         __syncthreads();
-        unsigned long long jq = 0ull;
+        const int lo_tile = s_bnd[0], hi_tile = s_bnd[kCellTile];
         const long long N = g.N;
+        const long long rt0 = (N + lo_tile) / kResTile;
+        unsigned long long racc[kRunTiles] = {0ull, 0ull, 0ull, 0ull};
+        unsigned long long jq = 0ull;
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
             const int k = base + threadIdx.x * kCellIpt + j;
             const int nnew = bnd[j + 1] - bnd[j];
             if (nnew > 0 && k < g.C) {
-                const float pA = g.meas_own[k].p_A;
-                const int nuA = (int)roundf(__fmul_rn((float)nnew, pA));
+                const int nuA = (int)roundf(__fmul_rn((float)nnew, pA[j]));
                 const int nuUA = nnew - nuA;
-                const float wA = nuA > 0 ? __fdiv_rn(__fmul_rn(pA, rb[j]), (float)nuA) : 0.0f;
-                const float wUA = nuUA > 0 ? __fdiv_rn(__fmul_rn(__fsub_rn(1.0f, pA), rb[j]), (float)nuUA) : 0.0f;
+                const float wA = nuA > 0 ? __fdiv_rn(__fmul_rn(pA[j], rb[j]), (float)nuA) : 0.0f;
+                const float wUA = nuUA > 0 ? __fdiv_rn(__fmul_rn(__fsub_rn(1.0f, pA[j]), rb[j]), (float)nuUA) : 0.0f;
                 g.cells[k].w_A = wA;
                 g.cells[k].w_UA = wUA;
                 s_nuA[threadIdx.x * kCellIpt + j] = nuA;
                 const int nA = min(max(nuA, 0), nnew);
                 const unsigned long long qA = quantize(wA, g.q_shift), qU = quantize(wUA, g.q_shift);
                 jq += (unsigned long long)nA * qA + (unsigned long long)(nnew - nA) * qU;
-                add_joint_range(agg, g.res_sum, N + bnd[j], N + bnd[j] + nA, qA);
-                add_joint_range(agg, g.res_sum, N + bnd[j] + nA, N + bnd[j + 1], qU);
+                add_joint_range(racc, rt0, g.res_sum, N + bnd[j], N + bnd[j] + nA, qA);
+                add_joint_range(racc, rt0, g.res_sum, N + bnd[j] + nA, N + bnd[j + 1], qU);
             }
+        }
+#pragma unroll
+        for (int i = 0; i < kRunTiles; ++i) {
+            const unsigned long long s = warp_sum_u64(racc[i]);
+            if (lane == 0 && s) atomicAdd(&g.res_sum[rt0 + i], s);
         }
         jq = warp_sum_u64(jq);
-        if ((threadIdx.x & 31) == 0 && jq) atomicAdd(&g.fs->joint_total, jq);
-        __syncthreads();  // every shared add and s_nuA entry is done
-        agg_flush(agg, g.res_sum, g.tiles[kStResample]);
-        // key word of every newborn slot of the tile: cell | associated bit.  A cell with few
-        // newborns is filled by its own thread; the block fills the heavy cells together.
-        uint32_t* __restrict__ B_key = g.B_key;
-#pragma unroll
-        for (int j = 0; j < kCellIpt; ++j) {
-            const int c = threadIdx.x * kCellIpt + j;
-            const int lo = bnd[j], hi = bnd[j + 1];
-            if (hi - lo > 0 && hi - lo <= kOwnSlots) {
-                const uint32_t key = (uint32_t)(base + c);
-                const int nA = s_nuA[c];
-                for (int sl = lo; sl < hi; ++sl) B_key[sl] = key | ((sl - lo) < nA ? kAssocBit : 0u);
-            } else if (hi - lo > kOwnSlots) {
-                s_heavy[atomicAdd(&s_nheavy, 1)] = c;
+        if (lane == 0 && jq) atomicAdd(&g.fs->joint_total, jq);
+        __syncthreads();  // every s_nuA entry is written
+        // key word of every newborn slot of the tile (cell | associated bit), slot by slot on
+        // consecutive threads; the owner cell is the last c with s_bnd[c] <= slot
+        for (int sl = lo_tile + threadIdx.x; sl < hi_tile; sl += kThreads) {
+            int lo = 0, hi = kCellTile - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_bnd[mid] <= sl) lo = mid; else hi = mid - 1;
             }
-        }
-        __syncthreads();
-        for (int h = 0; h < s_nheavy; ++h) {
-            const int c = s_heavy[h];
-            const int lo = s_bnd[c], hi = s_bnd[c + 1];
-            const uint32_t key = (uint32_t)(base + c);
-            const int nA = s_nuA[c];
-            for (int sl = lo + threadIdx.x; sl < hi; sl += kThreads) B_key[sl] = key | ((sl - lo) < nA ? kAssocBit : 0u);
+            g.B_key[sl] = (uint32_t)(base + lo) | ((sl - s_bnd[lo]) < s_nuA[lo] ? kAssocBit : 0u);
         }
         if (threadIdx.x == 0 && lt == 0) g.fs->n_birth = (T > 0ull) ? g.B : 0;
         __syncthreads();
