@@ -231,8 +231,9 @@ __device__ __forceinline__ void flag_status(const GridDesc& g, uint32_t bits) {
 }
 __device__ __forceinline__ void flag_timeout(const GridDesc& g) { flag_status(g, kStatusTimeout); }
 
-// Block-wide exclusive scan of one 64-bit value per thread (256 threads).  Returns the
+// Block-wide exclusive scan of one 64-bit value per thread (NT threads).  Returns the
 // exclusive prefix; *total receives the block sum.  scratch: >= 8 entries.
+template <int NT = kThreads>
 __device__ __forceinline__ unsigned long long block_excl_scan_u64(unsigned long long v, unsigned long long* scratch,
                                                                   unsigned long long* total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -246,7 +247,7 @@ __device__ __forceinline__ unsigned long long block_excl_scan_u64(unsigned long 
     __syncthreads();
     unsigned long long wpre = 0ull, tot = 0ull;
 #pragma unroll
-    for (int w = 0; w < kThreads / 32; ++w) {
+    for (int w = 0; w < NT / 32; ++w) {
         const unsigned long long s = scratch[w];
         if (w < warp) wpre += s;
         tot += s;

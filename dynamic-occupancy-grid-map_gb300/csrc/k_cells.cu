@@ -68,10 +68,10 @@ __device__ __forceinline__ Run run_shfl_up(const Run& a, int o) {
 // Fused per-cell update over one tile of kCellTile cells and the sorted particles that lie
 // in it, positions [ctile_start[t], ctile_start[t + 1]).
 //   A  segmented reduction of those particles into per-cell shared sums (sorted range,
-//      in-grid count, sum(v), sum(v^2), sum(vx*vy)).  Each thread walks kSegIpt consecutive
-//      particles: a cell whose particles start and end inside the thread is written
-//      directly; the run still open at the thread's end flows through a block scan to the
-//      thread holding the cell's last particle, which writes it.  Plain stores only (every
+//      in-grid count, sum(v), sum(v^2), sum(vx*vy)).  Each thread walks its own share of
+//      consecutive particles: a cell whose particles start and end inside the thread is
+//      written directly; the run still open at the thread's end flows through a block scan
+//      to the thread holding the cell's last particle, which writes it.  Plain stores only (every
 //      slot has one writer), and the add order depends only on positions, so the sums are
 //      deterministic.  Replaces particleToGridKernel (particle_to_grid.cu:22-40), the
 //      weight-array copy and the five statistical-moment prefix scans (dogm.cu:350-384).
@@ -82,6 +82,9 @@ __device__ __forceinline__ Run run_shfl_up(const Run& a, int o) {
 //      The quantised weight of each cell's persistent particles goes to the resample
 //      tiles that hold them.
 // ---------------------------------------------------------------------------------------
+constexpr int kCellThreads = 512;  // two cells per thread: a tile finishes in half the time
+static_assert(kCellTile % kCellThreads == 0, "whole cells per thread");
+
 struct CellSmem {
     dogm_measurement_cell meas[kCellTile];  // prefetched (cp.async) while A runs
     float free_prev[kCellTile];             // previous free mass, ego shift applied
@@ -89,9 +92,8 @@ struct CellSmem {
     int end[kCellTile];     // sorted position of the last particle
     int n_in[kCellTile];    // in-grid particles
     float vx[kCellTile], vy[kCellTile], vxx[kCellTile], vyy[kCellTile], vxy[kCellTile];
-    Run wagg[kThreads / 32];
-    Run carry;              // run open at the end of the previous chunk
-    unsigned long long red[kThreads / 32], red2[kThreads / 32];
+    Run wagg[kCellThreads / 32];
+    unsigned long long red[kCellThreads / 32], red2[kCellThreads / 32];
     int tile;
 };
 static_assert(offsetof(CellSmem, meas) % 16 == 0, "16-byte cp.async destination");
@@ -132,7 +134,7 @@ __device__ __forceinline__ void put_cell(CellSmem& sm, const GridDesc& g, uint32
     sm.vxy[cl] = r.vxy;
 }
 
-__global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
+__global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ bt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CellSmem& sm = *reinterpret_cast<CellSmem*>(smem_raw);
     const int total = batch_total(bt, kStCell);
@@ -147,8 +149,8 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
         const int p0 = (int)g.ctile_start[lt], p1 = (int)g.ctile_start[lt + 1];
         // prefetch the measurement and the (shifted) previous free mass of this thread's cells
         const bool meas16 = (reinterpret_cast<uintptr_t>(g.meas_src) & 15u) == 0u;
-        for (int r = 0; r < kCellIpt; ++r) {
-            const int cl = r * kThreads + threadIdx.x;
+        for (int r = 0; r < kCellTile / kCellThreads; ++r) {
+            const int cl = r * kCellThreads + threadIdx.x;
             const int k = base + cl;
             if (k >= g.C) break;
             if (meas16) {
@@ -166,59 +168,63 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
             if (src >= 0) cp_async4(&sm.free_prev[cl], g.free_old + src);
             else sm.free_prev[cl] = 0.0f;
         }
-        for (int c = threadIdx.x; c < kCellTile; c += kThreads) sm.start[c] = -1;
-        if (threadIdx.x == 0) sm.carry = run_empty(0u);
+        for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) sm.start[c] = -1;
         __syncthreads();
 
         // ---- A: segmented reduction of the tile's particles ------------------------------
-        for (int cb = p0; cb < p1; cb += kSegTile) {
-            const Run carry = sm.carry;  // read before thread 0 rewrites it below
-            const int i0 = cb + threadIdx.x * kSegIpt;
-            uint32_t kw[kSegIpt];
-            float2 v[kSegIpt];
-#pragma unroll
-            for (int r = 0; r < kSegIpt; ++r) {
-                const int i = i0 + r;
-                kw[r] = 0xffffffffu;
-                v[r] = make_float2(0.0f, 0.0f);
-                if (i < p1) {
-                    kw[r] = g.S_key[i];
-                    const float4 st = g.S_state[i];
-                    v[r] = make_float2(st.z, st.w);
-                }
-            }
-            // cells of the particles either side of the thread's span (sentinel outside the tile)
-            const uint32_t kSent = 0xffffffffu;
-            const uint32_t before = (i0 > p0 && i0 <= p1) ? (g.S_key[i0 - 1] & kCellMask) : kSent;
-            const uint32_t after = (i0 + kSegIpt < p1) ? (g.S_key[i0 + kSegIpt] & kCellMask) : kSent;
-            Run cur = run_empty(0u);   // run open at the current particle
-            Run first = run_empty(0u); // the thread's first run, when it continues an earlier one
+        // thread t walks its own consecutive share [i_beg, i_end) of the tile's particles, so
+        // a full tile costs one block scan however many particles it holds
+        const int np = p1 - p0;
+        if (np > 0) {  // block-uniform
+            const int per = (np + kCellThreads - 1) / kCellThreads;
+            const int i_beg = min(p1, p0 + (int)threadIdx.x * per), i_end = min(p1, i_beg + per);
+            const uint32_t kSent = 0xffffffffu;  // cell "outside the tile"
+            uint32_t prev = (i_beg > p0 && i_beg < p1) ? (g.S_key[i_beg - 1] & kCellMask) : kSent;
+            Run cur = run_empty(0u);    // run open at the current particle
+            Run first = run_empty(0u);  // the thread's first run, when it continues an earlier one
             uint32_t first_cell = kSent;
             int first_last = -1;
             bool last_tail = false;
+            for (int ib = i_beg; ib < i_end; ib += kSegIpt) {
+                uint32_t kw[kSegIpt];
+                float2 v[kSegIpt];
 #pragma unroll
-            for (int r = 0; r < kSegIpt; ++r) {
-                const int i = i0 + r;
-                if (i < p1) {
-                    const uint32_t c = kw[r] & kCellMask;
-                    const uint32_t prev = r == 0 ? before : (kw[r - 1] & kCellMask);
-                    const uint32_t next = (r + 1 < kSegIpt && i + 1 < p1) ? (kw[r + 1] & kCellMask) : after;
-                    if (c != prev) {  // segment head
-                        cur = run_empty(kRunHead);
-                        const uint32_t cl = c - (uint32_t)base;
-                        if (cl < (uint32_t)kCellTile) sm.start[cl] = i;
+                for (int r = 0; r < kSegIpt; ++r) {
+                    const int i = ib + r;
+                    kw[r] = kSent;
+                    v[r] = make_float2(0.0f, 0.0f);
+                    if (i < p1) kw[r] = g.S_key[i];
+                    if (i < i_end) {
+                        const float4 st = g.S_state[i];
+                        v[r] = make_float2(st.z, st.w);
                     }
-                    run_add(cur, kw[r], v[r]);
-                    last_tail = c != next;
-                    if (last_tail) {  // segment tail
-                        if (cur.fn & kRunHead) {
-                            put_cell(sm, g, c - (uint32_t)base, i, cur);
-                        } else {
-                            first = cur;
-                            first_cell = c;
-                            first_last = i;
+                }
+                const uint32_t after = (ib + kSegIpt < p1) ? (g.S_key[ib + kSegIpt] & kCellMask) : kSent;
+#pragma unroll
+                for (int r = 0; r < kSegIpt; ++r) {
+                    const int i = ib + r;
+                    if (i < i_end) {
+                        const uint32_t c = kw[r] & kCellMask;
+                        const uint32_t next = (r + 1 < kSegIpt) ? (kw[r + 1] == kSent ? kSent : (kw[r + 1] & kCellMask))
+                                                                : after;
+                        if (c != prev) {  // segment head
+                            cur = run_empty(kRunHead);
+                            const uint32_t cl = c - (uint32_t)base;
+                            if (cl < (uint32_t)kCellTile) sm.start[cl] = i;
                         }
-                        cur = run_empty(kRunHead);
+                        run_add(cur, kw[r], v[r]);
+                        last_tail = c != next;
+                        if (last_tail) {  // segment tail
+                            if (cur.fn & kRunHead) {
+                                put_cell(sm, g, c - (uint32_t)base, i, cur);
+                            } else {
+                                first = cur;
+                                first_cell = c;
+                                first_last = i;
+                            }
+                            cur = run_empty(kRunHead);
+                        }
+                        prev = c;
                     }
                 }
             }
@@ -233,11 +239,10 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
             if (lane == 31) sm.wagg[warp] = inc;
             Run excl = run_shfl_up(inc, 1);
             __syncthreads();
-            Run pre = carry;
+            Run pre = run_empty(0u);
             for (int w = 0; w < warp; ++w) pre = run_combine(pre, sm.wagg[w]);
             if (lane > 0) pre = run_combine(pre, excl);
             if (first_last >= 0) put_cell(sm, g, first_cell - (uint32_t)base, first_last, run_combine(pre, first));
-            if (threadIdx.x == kThreads - 1) sm.carry = run_combine(pre, out);
             __syncthreads();
         }
 
@@ -245,8 +250,8 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
         const float c_pred = __fmul_rn(g.p_S, g.fs->w_res);  // predicted weight of an in-grid particle
         unsigned long long qb = 0ull, jq = 0ull;
         cp_async_wait_all();  // this thread's own prefetches (B reads only its own cells' slots)
-        for (int r = 0; r < kCellIpt; ++r) {
-            const int cl = r * kThreads + threadIdx.x;
+        for (int r = 0; r < kCellTile / kCellThreads; ++r) {
+            const int cl = r * kCellThreads + threadIdx.x;
             const int k = base + cl;
             if (k >= g.C) break;
             const bool occupied = sm.start[cl] >= 0;  // end, count and sums are set only then
@@ -290,8 +295,8 @@ __global__ void __launch_bounds__(kThreads) k_cells(Batch* __restrict__ bt) {
             }
         }
         unsigned long long tile_qb, tile_jq;
-        block_excl_scan_u64(qb, sm.red, &tile_qb);
-        block_excl_scan_u64(jq, sm.red2, &tile_jq);
+        block_excl_scan_u64<kCellThreads>(qb, sm.red, &tile_qb);
+        block_excl_scan_u64<kCellThreads>(jq, sm.red2, &tile_jq);
         if (threadIdx.x == 0) {
             g.cell_sum[lt] = tile_qb;
             atomicAdd(&g.fs->qb_total, tile_qb);
@@ -419,7 +424,7 @@ cudaError_t prepare_cells() {
 }
 
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg) {
-    k_cells<<<cfg.num_sms * 4, kThreads, sizeof(CellSmem), cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_cells<<<cfg.num_sms * 2, kCellThreads, sizeof(CellSmem), cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 

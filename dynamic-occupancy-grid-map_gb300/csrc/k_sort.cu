@@ -22,61 +22,57 @@ static_assert(kCtilePer * kScanWarps * 32 == kMaxCellTiles, "one block scans eve
 
 // Exclusive scan of the per-cell-tile particle counts that predict took: ctile_start[i] is
 // the first sorted position of cell tile i, ctile_start[n] = N.  Also the claim order of the
-// cell pass: tiles holding more than kFullTile particles first (they take longest), then the
-// rest, each group in index order.  Run by one block as the last work item of the pass-1
-// digit scan (after predict, before the cell pass).
-constexpr uint32_t kFullTile = 2 * kSegTile;
-
-__device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* red2) {
+// cell pass: tiles by decreasing bit length of their particle count (the fullest, slowest
+// tiles start first; the last tiles claimed are the quickest), in any order within a class.
+// Run by one block as the last work item of the pass-1 digit scan (after predict, before
+// the cell pass).  scratch: >= 64 words.
+__device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) {
     const int n = g.tiles[kStCell];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int i0 = threadIdx.x * kCtilePer;
-    uint32_t v[kCtilePer], s = 0u, cls = 0u;  // cls: full tiles << 16 | other tiles
+    uint32_t* cls_count = scratch;       // 16 classes
+    uint32_t* cls_next = scratch + 32;
+    if (threadIdx.x < 16) cls_count[threadIdx.x] = 0u;
+    uint32_t v[kCtilePer], s = 0u;
 #pragma unroll
     for (int j = 0; j < kCtilePer; ++j) {
         v[j] = (i0 + j < n) ? g.ctile_cnt[i0 + j] : 0u;
         s += v[j];
-        if (i0 + j < n) cls += v[j] > kFullTile ? (1u << 16) : 1u;
     }
-    uint32_t x = s, y = cls;
+    uint32_t x = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t a = __shfl_up_sync(0xffffffffu, x, o);
-        const uint32_t b = __shfl_up_sync(0xffffffffu, y, o);
-        if (lane >= o) {
-            x += a;
-            y += b;
-        }
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    if (lane == 31) {
-        red[warp] = x;
-        red2[warp] = y;
-    }
+    if (lane == 31) red[warp] = x;
     __syncthreads();
-    uint32_t e = x - s, ec = y - cls, tc = 0u;
-    for (int w = 0; w < kScanWarps; ++w) {
-        if (w < warp) {
-            e += red[w];
-            ec += red2[w];
-        }
-        tc += red2[w];
-    }
-    const uint32_t n_full = tc >> 16;
+    uint32_t e = x - s;
+    for (int w = 0; w < warp; ++w) e += red[w];
 #pragma unroll
     for (int j = 0; j < kCtilePer; ++j) {
         if (i0 + j < n) {
             g.ctile_start[i0 + j] = e;
-            if (v[j] > kFullTile) {
-                g.ctile_order[ec >> 16] = (uint32_t)(i0 + j);
-                ec += 1u << 16;
-            } else {
-                g.ctile_order[n_full + (ec & 0xffffu)] = (uint32_t)(i0 + j);
-                ec += 1u;
-            }
+            atomicAdd(&cls_count[15 - min(15, 32 - __clz((int)v[j]))], 1u);
         }
         e += v[j];
     }
     if (i0 < n && n <= i0 + kCtilePer) g.ctile_start[n] = e;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t c = lane < 16 ? cls_count[lane] : 0u;
+        uint32_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane < 16) cls_next[lane] = inc - c;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kCtilePer; ++j)
+        if (i0 + j < n) g.ctile_order[atomicAdd(&cls_next[15 - min(15, 32 - __clz((int)v[j]))], 1u)] = (uint32_t)(i0 + j);
     __syncthreads();
 }
 
