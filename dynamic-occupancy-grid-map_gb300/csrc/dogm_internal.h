@@ -56,7 +56,7 @@ struct FrameState {
     // written by one update, read by the next
     float w_res;          // common particle weight after the last resampling (or 1/N)
     uint32_t status;      // sticky error bits (kStatus*)
-    // per-frame accumulators (zeroed by the frame-begin kernel)
+    // per-frame accumulators (zeroed by predict; all of them by the frame-begin kernel)
     unsigned long long qb_total;   // sum of quantised newborn masses (exact)
     unsigned long long joint_total;// sum of quantised joint weights (exact)
     unsigned long long qo_total;   // first frame: sum of quantised measured occupancy
@@ -154,9 +154,10 @@ cudaError_t launch_draws(const GridDesc& g, int iteration, float2* init_u, float
 cudaError_t launch_lower_bound(const float* accum, int n_accum, const float* q, int n_q, int* out, int clamp_last,
                                cudaStream_t s);
 
-// Kernel launches per update (for the launch-count claim): frame-begin, predict, 2 x (digit
-// scan, sort pass), cells, newborn, resample.
-constexpr int kLaunchesPerFrame = 9;
+// Kernel launches per steady-state update (for the launch-count claim): predict, 2 x (digit
+// scan, sort pass), cells, newborn, resample.  A grid's first frame, and a frame after a
+// failed one, adds the frame-begin reset.
+constexpr int kLaunchesPerFrame = 8;
 constexpr int kLaunchesInit = 2;
 
 }  // namespace dogm_gb300

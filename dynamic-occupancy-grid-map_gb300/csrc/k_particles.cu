@@ -47,6 +47,21 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, in
     __shared__ uint32_t h1[kSortMaxBins];
     __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (ranges of the cell pass)
     const int total = batch_total(bt, kStPredict);
+    if (mode == 0) {
+        // this frame's exact sums start at zero: the cell and newborn passes add into them
+        // after this kernel, and the last reader (the previous frame's resampling) is done
+        const int stride = gridDim.x * blockDim.x;
+        const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+        for (int gi = 0; gi < bt->n_grids; ++gi) {
+            const GridDesc& g = bt->g[gi];
+            for (int i = tid; i < g.tiles[kStResample]; i += stride) g.res_sum[i] = 0ull;
+            if (tid == 0) {
+                g.fs->status = 0u;
+                g.fs->qb_total = 0ull;
+                g.fs->joint_total = 0ull;
+            }
+        }
+    }
     const int lane = threadIdx.x & 31;
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
         const int gi = grid_of_tile(bt, kStPredict, t);

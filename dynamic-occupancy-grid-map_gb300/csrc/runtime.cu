@@ -38,9 +38,9 @@ int bitlen(unsigned long long v) {
 
 int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-constexpr int kStages = 9;
-const char* const kStageNames[kStages] = {"frame_begin", "predict", "sort_scan0", "sort_pass0", "sort_scan1",
-                                          "sort_pass1",  "cells",   "newborn",    "resample"};
+constexpr int kStages = 8;
+const char* const kStageNames[kStages] = {"predict",    "sort_scan0", "sort_pass0", "sort_scan1",
+                                          "sort_pass1", "cells",      "newborn",    "resample"};
 
 // One launch context: a device copy of a Batch, two pinned host mirrors (the host fills one
 // while the device may still read the other, so frame k+1 is queued while frame k runs) and
@@ -260,7 +260,7 @@ cudaError_t download_status(Ctx& c) {
 }
 
 // The steady-state frame: 8 kernels; with profiling, a CUDA event before each and at the end.
-cudaError_t frame_kernels(Ctx& c, bool with_init) {
+cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
     LaunchCfg cfg{c.num_sms, c.stream};
     const bool prof = c.profile && !with_init;
     cudaError_t e;
@@ -269,31 +269,34 @@ cudaError_t frame_kernels(Ctx& c, bool with_init) {
         if (prof && (e = cudaEventRecord(c.ev[i], c.stream)) != cudaSuccess) return e; \
         if ((e = (call)) != cudaSuccess) return e;                                  \
     } while (0)
-    STAGE(0, launch_frame_begin(c.d_batch, 0, cfg));
+    // the per-frame counters are reset by predict and the cell pass of the previous frame; a
+    // full reset runs only on a grid's first frame or after a failed frame
+    if ((with_begin || with_init) && (e = launch_frame_begin(c.d_batch, 0, cfg)) != cudaSuccess) return e;
     if (with_init && (e = launch_init_particles(c.d_batch, cfg)) != cudaSuccess) return e;
-    STAGE(1, launch_predict(c.d_batch, 0, cfg));
-    STAGE(2, launch_sort_scan(c.d_batch, 0, cfg));
-    STAGE(3, launch_sort_pass(c.d_batch, 0, cfg));
-    STAGE(4, launch_sort_scan(c.d_batch, 1, cfg));
-    STAGE(5, launch_sort_pass(c.d_batch, 1, cfg));
-    STAGE(6, launch_cells(c.d_batch, cfg));
-    STAGE(7, launch_newborn(c.d_batch, cfg));
-    STAGE(8, launch_resample(c.d_batch, cfg));
+    STAGE(0, launch_predict(c.d_batch, 0, cfg));
+    STAGE(1, launch_sort_scan(c.d_batch, 0, cfg));
+    STAGE(2, launch_sort_pass(c.d_batch, 0, cfg));
+    STAGE(3, launch_sort_scan(c.d_batch, 1, cfg));
+    STAGE(4, launch_sort_pass(c.d_batch, 1, cfg));
+    STAGE(5, launch_cells(c.d_batch, cfg));
+    STAGE(6, launch_newborn(c.d_batch, cfg));
+    STAGE(7, launch_resample(c.d_batch, cfg));
 #undef STAGE
     if (prof && (e = cudaEventRecord(c.ev[kStages], c.stream)) != cudaSuccess) return e;
     return cudaSuccess;
 }
 
 // Queues one frame from the current mirror and advances to the other mirror.
-dogm_status run_frame(Ctx& c, int n, bool any_init, int* launches) {
+dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launches) {
     cudaError_t e;
-    const bool plain = any_init || c.profile;
+    const bool plain = any_init || any_clear || c.profile;
     if (plain) {
-        // first frame of some grid (init runs between begin and predict) or per-stage timing
+        // first frame of some grid (init runs between begin and predict), a frame after a
+        // failed one (full counter reset first) or per-stage timing
         DOGM_CUDA(upload_batch(c, n));
-        DOGM_CUDA(frame_kernels(c, any_init));
+        DOGM_CUDA(frame_kernels(c, any_init, any_clear));
         DOGM_CUDA(download_status(c));
-        *launches = kLaunchesPerFrame + (any_init ? kLaunchesInit : 0);
+        *launches = kLaunchesPerFrame + (any_init || any_clear ? 1 : 0) + (any_init ? kLaunchesInit : 0);
     } else {
         const int key = n * 2 + c.cur;
         auto it = c.graphs.find(key);
@@ -301,7 +304,7 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, int* launches) {
             cudaGraph_t graph;
             DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
             e = upload_batch(c, n);
-            if (e == cudaSuccess) e = frame_kernels(c, false);
+            if (e == cudaSuccess) e = frame_kernels(c, false, false);
             if (e == cudaSuccess) e = download_status(c);
             cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
             if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -540,7 +543,7 @@ dogm_status dogm_update(dogm_handle* h, const dogm_measurement_cell* meas, float
     dogm_handle* hs[1] = {h};
     std::vector<int> init_mask(1, init ? 1 : 0);
     build_batch(c, hs, 1, init_mask);
-    st = run_frame(c, 1, init, &h->last_launches);
+    st = run_frame(c, 1, init, h->need_clear, &h->last_launches);
     if (st != DOGM_OK) { h->need_clear = true; return st; }
     advance(h);
     if (h->opt.sync_each_update) return finish_frame(c, hs, 1);
@@ -591,8 +594,10 @@ dogm_status dogm_update_batch(dogm_handle* const* hs, int n, const dogm_measurem
         fill_frame(h, dt[i], shifted, xm, ym, src, copy);
     }
     build_batch(*c, hs, n, init_mask);
+    bool any_clear = false;
+    for (int i = 0; i < n; ++i) any_clear |= hs[i]->need_clear;
     int launches = 0;
-    dogm_status st = run_frame(*c, n, any_init, &launches);
+    dogm_status st = run_frame(*c, n, any_init, any_clear, &launches);
     if (st != DOGM_OK) {
         for (int i = 0; i < n; ++i) hs[i]->need_clear = true;
         return st;
