@@ -17,6 +17,7 @@ namespace dogm_gb300 {
 // ---------------------------------------------------------------------------------------
 constexpr int kScanWarps = 32;
 constexpr int kScanBatch = 8;
+constexpr int kScanKeep = 16;  // tiles per warp kept in registers (N up to 2M particles)
 constexpr int kCtilePer = kMaxCellTiles / (kScanWarps * 32);
 static_assert(kCtilePer * kScanWarps * 32 == kMaxCellTiles, "one block scans every cell-tile count");
 
@@ -93,52 +94,65 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict
         const int nb = 1 << (pass ? g.d1_bits : g.d0_bits);
         const int b = group * 32 + lane;
         const uint32_t* hist = g.hist + pass * kSortMaxBins;
-        // digit base: sum of the global histogram over digits < b
+        // each warp owns a contiguous chunk of tiles; up to kScanKeep counts per lane stay in
+        // registers between the sum and the rewrite (one load round), more are reloaded
+        uint32_t* H = g.hsort + (size_t)pass * g.sort_tiles * kSortMaxBins;
+        const int T = g.sort_tiles;
+        const int per = (T + kScanWarps - 1) / kScanWarps;
+        const int t0 = warp * per, t1 = min(T, t0 + per);
+        const bool keep = per <= kScanKeep;  // block-uniform
+        uint32_t v[kScanKeep];
+        uint32_t s = 0;
+        if (keep) {
+#pragma unroll
+            for (int i = 0; i < kScanKeep; ++i)
+                v[i] = (b < nb && t0 + i < t1) ? H[(size_t)(t0 + i) * kSortMaxBins + b] : 0u;
+#pragma unroll
+            for (int i = 0; i < kScanKeep; ++i) s += v[i];
+        } else if (b < nb) {
+            for (int tb = t0; tb < t1; tb += kScanBatch) {
+                uint32_t w[kScanBatch];
+#pragma unroll
+                for (int i = 0; i < kScanBatch; ++i)
+                    w[i] = (tb + i < t1) ? H[(size_t)(tb + i) * kSortMaxBins + b] : 0u;
+#pragma unroll
+                for (int i = 0; i < kScanBatch; ++i) s += w[i];
+            }
+        }
+        // digit base: sum of the global histogram over digits < b (loads issued alongside)
         uint32_t part = 0;
         for (int i = threadIdx.x; i < group * 32; i += blockDim.x) part += hist[i];
+        const uint32_t own = (b < nb) ? hist[b] : 0u;
         for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-        if (lane == 0) red[warp] = part;
-        __syncthreads();
-        uint32_t base = 0;
-        for (int w = 0; w < kScanWarps; ++w) base += red[w];
-        uint32_t own = (b < nb) ? hist[b] : 0u;
         uint32_t lanepre = own;
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, lanepre, o);
             if (lane >= o) lanepre += y;
         }
-        base += lanepre - own;
-        // each warp owns a contiguous chunk of tiles; its counts are loaded once, in batches
-        // of kScanBatch independent loads, summed, then rewritten as offsets
-        uint32_t* H = g.hsort + (size_t)pass * g.sort_tiles * kSortMaxBins;
-        const int T = g.sort_tiles;
-        const int per = (T + kScanWarps - 1) / kScanWarps;
-        const int t0 = warp * per, t1 = min(T, t0 + per);
-        uint32_t s = 0;
-        if (b < nb) {
-            for (int tb = t0; tb < t1; tb += kScanBatch) {
-                uint32_t v[kScanBatch];
-#pragma unroll
-                for (int i = 0; i < kScanBatch; ++i)
-                    v[i] = (tb + i < t1) ? H[(size_t)(tb + i) * kSortMaxBins + b] : 0u;
-#pragma unroll
-                for (int i = 0; i < kScanBatch; ++i) s += v[i];
-            }
-        }
+        if (lane == 0) red[warp] = part;
         chunk[warp][lane] = s;
         __syncthreads();
-        uint32_t pre = base;
+        uint32_t pre = lanepre - own;
+        for (int w = 0; w < kScanWarps; ++w) pre += red[w];
         for (int w = 0; w < warp; ++w) pre += chunk[w][lane];
         if (b < nb) {
-            for (int tb = t0; tb < t1; tb += kScanBatch) {
-                uint32_t v[kScanBatch];
+            if (keep) {
 #pragma unroll
-                for (int i = 0; i < kScanBatch; ++i)
-                    v[i] = (tb + i < t1) ? H[(size_t)(tb + i) * kSortMaxBins + b] : 0u;
-#pragma unroll
-                for (int i = 0; i < kScanBatch; ++i) {
-                    if (tb + i < t1) H[(size_t)(tb + i) * kSortMaxBins + b] = pre;
+                for (int i = 0; i < kScanKeep; ++i) {
+                    if (t0 + i < t1) H[(size_t)(t0 + i) * kSortMaxBins + b] = pre;
                     pre += v[i];
+                }
+            } else {
+                for (int tb = t0; tb < t1; tb += kScanBatch) {
+                    uint32_t w[kScanBatch];
+#pragma unroll
+                    for (int i = 0; i < kScanBatch; ++i)
+                        w[i] = (tb + i < t1) ? H[(size_t)(tb + i) * kSortMaxBins + b] : 0u;
+#pragma unroll
+                    for (int i = 0; i < kScanBatch; ++i) {
+                        if (tb + i < t1) H[(size_t)(tb + i) * kSortMaxBins + b] = pre;
+                        pre += w[i];
+                    }
                 }
             }
         }
