@@ -320,9 +320,164 @@ def run_gb300(args, rank: int, world: int):
     g.close()
     for d in dbufs:
         d.free()
+    if not args.no_serving:
+        line["batched"] = run_batched(dogm, scene)
+        line["serving"] = run_serving(dogm, scene, seconds=args.serve_seconds)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(frames, cfg, args.cpu_frames)
     return line
+
+
+def _stream_pool(dogm, scene, n: int, seed: int, pinned: bool):
+    """n uneven streams (scene.stream_configs) with two measurement frames each, in HBM
+    (device buffers) or in one pinned host block."""
+    cfgs = scene.stream_configs(n, seed=seed)
+    params, frames = [], []
+    for i, c in enumerate(cfgs):
+        params.append(dogm.make_params(**scene.params_dict(c)))
+        sc = scene.Scene(c, seed=seed * 1000 + i)
+        frames.append([sc.frame(k)[0] for k in range(2)])
+    cells = [f[0].shape[0] for f in frames]
+    if pinned:
+        block = dogm.PinnedArray((2 * sum(cells), 4), np.float32)
+        bufs, off = [], 0
+        for f in frames:
+            pair = []
+            for m in f:
+                v = block.array[off:off + m.shape[0]]
+                v[:] = m
+                pair.append(v)
+                off += m.shape[0]
+            bufs.append(pair)
+        return params, cells, bufs, block
+    bufs = []
+    for f in frames:
+        pair = []
+        for m in f:
+            d = dogm.DeviceBuffer(m.nbytes)
+            d.upload(m)
+            pair.append(d)
+        bufs.append(pair)
+    return params, cells, bufs, None
+
+
+def run_batched(dogm, scene, n_streams: int = 64, rounds: int = 30, warm: int = 3) -> dict:
+    """Batched uneven grids: n_streams independent grids updated per frame by one launch per
+    stage (dogm_update_batch, CUDA graph) against one dogm_update per grid on its own CUDA
+    stream; measurement grids resident in HBM; host wall clock over `rounds` frames of all
+    grids (synchronised at both ends)."""
+    params, cells, bufs, _ = _stream_pool(dogm, scene, n_streams, seed=2, pinned=False)
+    grids = [dogm.DOGM(p, seed=1000 + i, stream_id=i, sync_each_update=False) for i, p in enumerate(params)]
+    zeros = [0.0] * n_streams
+    dts = [0.1] * n_streams
+
+    def batched(r):
+        dogm.update_batch(grids, [bufs[i][r % 2].ptr for i in range(n_streams)], zeros, zeros, zeros, dts,
+                          device=True)
+
+    def plain(r):
+        for i, g in enumerate(grids):
+            g.update_grid(bufs[i][r % 2].ptr, 0.0, 0.0, 0.0, 0.1, device=True)
+
+    def sync():
+        for g in grids:
+            g.synchronize()
+
+    out = {}
+    for name, step in (("batched", batched), ("per_stream", plain)):
+        for r in range(warm):
+            step(r)
+        sync()
+        t0 = time.perf_counter()
+        for r in range(rounds):
+            step(r)
+        sync()
+        dt = time.perf_counter() - t0
+        out[name] = n_streams * rounds / dt
+    for g in grids:
+        g.close()
+    for pair in bufs:
+        for d in pair:
+            d.free()
+    total_cells = sum(cells)
+    total_particles = sum(p.particle_count for p in params)
+    return {"frames_per_s": round(out["batched"], 1), "per_stream_frames_per_s": round(out["per_stream"], 1),
+            "speedup": round(out["batched"] / out["per_stream"], 2), "streams": n_streams, "rounds": rounds,
+            "cells": total_cells, "particles": total_particles,
+            "config": "%d grids, side log-uniform [128, 1024] cells at 0.1-0.2 m, 1.5 particles per cell, "
+                      "10%% newborns; measurement grids in HBM; host wall clock" % n_streams}
+
+
+def run_serving(dogm, scene, n_streams: int = 200, rate_hz: float = 10.0, seconds: float = 10.0,
+                saturate_frames: int = 8, budget: int = 150 * 10**9) -> dict:
+    """Serving: n_streams sensor streams with Poisson frame arrivals (rate_hz each) submitted
+    to dogm_server_* under an HBM budget, in batched (continuous batching) and per-stream
+    (one dogm_update per frame) mode.  Latency = result ready minus submission; measurement
+    grids come from pinned host memory (H2D copy inside the served frame)."""
+    params, cells, bufs, block = _stream_pool(dogm, scene, n_streams, seed=4, pinned=True)
+    rng = np.random.default_rng(9)
+    arrivals = []
+    for i in range(n_streams):
+        t = rng.exponential(1.0 / rate_hz)
+        while t < seconds:
+            arrivals.append((t, i))
+            t += rng.exponential(1.0 / rate_hz)
+    arrivals.sort()
+    out = {}
+    for mode_name, mode in (("batched", dogm.SERVE_BATCHED), ("per_stream", dogm.SERVE_PER_STREAM)):
+        srv = dogm.Server(hbm_budget_bytes=budget, mode=mode, max_batch=64, max_inflight=2)
+        sids = [srv.open_stream(p, seed=2000 + i, stream_id=i) for i, p in enumerate(params)]
+        frame_no = [0] * n_streams
+
+        def submit(i, tag):
+            k = frame_no[i]
+            frame_no[i] += 1
+            srv.submit(sids[i], bufs[i][k % 2], 0.0, 0.0, 0.0, 0.1, tag=tag)
+
+        # warm-up: first frames (initialisation) and the graphs of the batch sizes
+        for r in range(3):
+            for i in range(n_streams):
+                submit(i, 0)
+            srv.drain(600000)
+        srv.poll_array(1 << 20)
+        # saturation: every stream has `saturate_frames` frames queued at once
+        t0 = time.perf_counter()
+        for r in range(saturate_frames):
+            for i in range(n_streams):
+                submit(i, 0)
+        srv.drain(600000)
+        sat_s = time.perf_counter() - t0
+        srv.poll_array(1 << 20)
+        # Poisson arrivals paced on the host clock
+        t_start = time.perf_counter()
+        for j, (t, i) in enumerate(arrivals):
+            delay = t_start + t - time.perf_counter()
+            if delay > 2e-4:
+                time.sleep(delay - 1e-4)
+            submit(i, j + 1)
+        srv.drain(600000)
+        wall = time.perf_counter() - t_start
+        res = srv.poll_array(len(arrivals) + 16)
+        st = srv.stats()
+        srv.close()
+        assert len(res) == len(arrivals) and (res["status"] == 0).all(), "served frames failed"
+        lat = (res["t_done_ns"] - res["t_submit_ns"]) / 1e6
+        out[mode_name] = {
+            "saturated_frames_per_s": round(n_streams * saturate_frames / sat_s, 1),
+            "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+            "p999_ms": round(float(np.percentile(lat, 99.9)), 3), "max_ms": round(float(lat.max()), 3),
+            "frames": int(len(res)), "served_frames_per_s": round(len(res) / wall, 1),
+            "mean_batch": round(float(res["batch_size"].mean()), 2),
+            "resident_gb": round(st["resident_bytes"] / 1e9, 2),
+        }
+    block.free()
+    return {"batched": out["batched"], "per_stream": out["per_stream"],
+            "saturated_speedup": round(out["batched"]["saturated_frames_per_s"] /
+                                       out["per_stream"]["saturated_frames_per_s"], 2),
+            "config": "%d streams, Poisson %.0f Hz each (%.0f frames/s offered) for %.0f s, grids as the batched "
+                      "workload, %.0f GB HBM budget; latency = submit to result on the device; saturation = %d "
+                      "frames queued per stream" % (n_streams, rate_hz, n_streams * rate_hz, seconds, budget / 1e9,
+                                                    saturate_frames)}
 
 
 def read_traffic(kernel: str):
@@ -399,6 +554,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-frames", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true", help="skip the batched and serving workloads")
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="seconds of Poisson arrivals per serving mode (the serving workload names 60)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -43,6 +43,9 @@ ABI_SYMBOLS = [
     "dogm_lower_bound_f32", "dogm_host_alloc", "dogm_host_free", "dogm_device_alloc", "dogm_device_free",
     "dogm_memcpy", "dogm_state_bytes", "dogm_last_launch_count", "dogm_last_error", "dogm_status_string",
     "dogm_abi_version", "dogm_get_stream", "dogm_profile_enable", "dogm_stage_times", "dogm_stage_name",
+    "dogm_server_default_config", "dogm_server_create", "dogm_server_destroy", "dogm_server_open_stream",
+    "dogm_server_close_stream", "dogm_server_submit", "dogm_server_pause", "dogm_server_poll", "dogm_server_drain",
+    "dogm_server_get_stats", "dogm_server_stream_state", "dogm_server_stream_handle", "dogm_server_now_ns",
 ]
 
 
@@ -58,6 +61,27 @@ class Params(C.Structure):
 class Options(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("stream_id", C.c_uint32), ("resample_mode", C.c_int),
                 ("sync_each_update", C.c_int)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("mode", C.c_int), ("max_batch", C.c_int),
+                ("max_inflight", C.c_int), ("queue_admission", C.c_int)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("stream", C.c_int), ("status", C.c_int), ("tag", C.c_uint64), ("iteration", C.c_int),
+                ("batch_size", C.c_int), ("t_submit_ns", C.c_int64), ("t_launch_ns", C.c_int64),
+                ("t_done_ns", C.c_int64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("frames_submitted", C.c_uint64), ("frames_done", C.c_uint64), ("launches", C.c_uint64),
+                ("streams_active", C.c_int), ("streams_waiting", C.c_int), ("resident_bytes", C.c_size_t),
+                ("budget_bytes", C.c_size_t), ("mean_batch", C.c_double)]
+
+
+SERVE_BATCHED, SERVE_PER_STREAM = 0, 1
+STREAM_WAITING, STREAM_ACTIVE, STREAM_CLOSED = 0, 1, 2
 
 
 class DogmError(RuntimeError):
@@ -99,6 +123,12 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_memcpy": ([vp, vp, sz, i], i), "dogm_state_bytes": ([vp], sz), "dogm_last_launch_count": ([vp], i),
         "dogm_last_error": ([], C.c_char_p), "dogm_get_stream": ([vp], vp), "dogm_profile_enable": ([vp, i], i),
         "dogm_stage_times": ([vp, vp, i], i), "dogm_stage_name": ([i], C.c_char_p), "dogm_status_string": ([i], C.c_char_p), "dogm_abi_version": ([], i),
+        "dogm_server_default_config": ([vp], i), "dogm_server_create": ([vp, vp], i), "dogm_server_destroy": ([vp], i),
+        "dogm_server_open_stream": ([vp, vp, vp, vp], i), "dogm_server_close_stream": ([vp, i], i),
+        "dogm_server_submit": ([vp, i, vp, i, f, f, f, f, vp, u64], i), "dogm_server_poll": ([vp, vp, i, i, vp], i), "dogm_server_pause": ([vp, i], i),
+        "dogm_server_drain": ([vp, i], i), "dogm_server_get_stats": ([vp, vp], i),
+        "dogm_server_stream_state": ([vp, i], i), "dogm_server_stream_handle": ([vp, i, vp], i),
+        "dogm_server_now_ns": ([], C.c_int64),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -389,3 +419,117 @@ def lower_bound_f32(accum: np.ndarray, queries: np.ndarray, clamp_last: bool = T
 
 def state_bytes(params: Params) -> int:
     return int(load().dogm_state_bytes(C.byref(params)))
+
+
+class _StreamView(DOGM):
+    """Readback view of a server stream's handle (owned by the server; never destroyed here)."""
+
+    def __init__(self, h, params: Params):
+        lib = load()
+        self.params = params
+        self.h = h
+        self.grid_size = lib.dogm_get_grid_size(h)
+        self.cell_count = self.grid_size * self.grid_size
+        self.particle_count = lib.dogm_get_particle_count(h)
+        self.new_born_particle_count = lib.dogm_get_new_born_particle_count(h)
+
+    def close(self) -> None:
+        self.h = None
+
+
+class Server:
+    """Serving loop over the C ABI (dogm_server_*): resident streams admitted under an HBM
+    budget, frames updated by continuous batching (or per stream, for comparison)."""
+
+    def __init__(self, hbm_budget_bytes: int | None = None, mode: int = SERVE_BATCHED, max_batch: int = 64,
+                 max_inflight: int = 2, queue_admission: bool = True):
+        lib = load()
+        cfg = ServerConfig()
+        check(lib.dogm_server_default_config(C.byref(cfg)), "dogm_server_default_config")
+        if hbm_budget_bytes is not None:
+            cfg.hbm_budget_bytes = int(hbm_budget_bytes)
+        cfg.mode, cfg.max_batch, cfg.max_inflight = mode, max_batch, max_inflight
+        cfg.queue_admission = 1 if queue_admission else 0
+        s = C.c_void_p()
+        check(lib.dogm_server_create(C.byref(cfg), C.byref(s)), "dogm_server_create")
+        self.s = s
+        self.params: dict[int, Params] = {}
+        self._keep: dict[int, object] = {}
+
+    def close(self) -> None:
+        if self.s:
+            check(load().dogm_server_destroy(self.s), "dogm_server_destroy")
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def open_stream(self, params: Params, seed: int = 123456, stream_id: int = 0) -> int:
+        lib = load()
+        opt = Options()
+        check(lib.dogm_default_options(C.byref(opt)), "dogm_default_options")
+        opt.seed, opt.stream_id = seed, stream_id
+        sid = C.c_int(-1)
+        check(lib.dogm_server_open_stream(self.s, C.byref(params), C.byref(opt), C.byref(sid)),
+              "dogm_server_open_stream")
+        self.params[sid.value] = params
+        return sid.value
+
+    def close_stream(self, sid: int) -> None:
+        check(load().dogm_server_close_stream(self.s, sid), "dogm_server_close_stream")
+
+    def submit(self, sid: int, meas, x: float, y: float, yaw: float, dt: float, cells_out=None, tag: int = 0,
+               device: bool = False) -> None:
+        """meas: MEAS_DTYPE host array (kept alive until the result), an int device pointer or None."""
+        if meas is None:
+            p = None
+        elif isinstance(meas, int):
+            p = C.c_void_p(meas)
+        else:
+            p = _ptr(meas)
+        check(load().dogm_server_submit(self.s, sid, p, 1 if device else 0, x, y, yaw, dt, _ptr(cells_out), tag),
+              "dogm_server_submit")
+
+    def pause(self, paused: bool = True) -> None:
+        """Hold back new launches (True) or resume (False); submitted frames keep queueing."""
+        check(load().dogm_server_pause(self.s, 1 if paused else 0), "dogm_server_pause")
+
+    def poll(self, max_results: int = 1024, timeout_us: int = 0) -> list[dict]:
+        buf = (ServerResult * max_results)()
+        n = C.c_int(0)
+        check(load().dogm_server_poll(self.s, buf, max_results, timeout_us, C.byref(n)), "dogm_server_poll")
+        return [{k: getattr(buf[i], k) for k, _ in ServerResult._fields_} for i in range(n.value)]
+
+    def poll_array(self, max_results: int = 65536, timeout_us: int = 0) -> np.ndarray:
+        """Like poll, as a structured numpy array (cheap for many results)."""
+        dt = np.dtype([("stream", "<i4"), ("status", "<i4"), ("tag", "<u8"), ("iteration", "<i4"),
+                       ("batch_size", "<i4"), ("t_submit_ns", "<i8"), ("t_launch_ns", "<i8"), ("t_done_ns", "<i8")])
+        assert dt.itemsize == C.sizeof(ServerResult)
+        out = np.empty(max_results, dt)
+        n = C.c_int(0)
+        check(load().dogm_server_poll(self.s, _ptr(out), max_results, timeout_us, C.byref(n)), "dogm_server_poll")
+        return out[:n.value]
+
+    def drain(self, timeout_ms: int = 60000) -> None:
+        check(load().dogm_server_drain(self.s, timeout_ms), "dogm_server_drain")
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(load().dogm_server_get_stats(self.s, C.byref(st)), "dogm_server_get_stats")
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def stream_state(self, sid: int) -> int:
+        return load().dogm_server_stream_state(self.s, sid)
+
+    def stream(self, sid: int) -> DOGM:
+        """Readback view (get_grid_cells, get_particles ...) of an admitted stream; drain first."""
+        h = C.c_void_p()
+        check(load().dogm_server_stream_handle(self.s, sid, C.byref(h)), "dogm_server_stream_handle")
+        return _StreamView(h, self.params[sid])
+
+
+def now_ns() -> int:
+    return int(load().dogm_server_now_ns())

@@ -160,4 +160,29 @@ cudaError_t launch_lower_bound(const float* accum, int n_accum, const float* q, 
 constexpr int kLaunchesPerFrame = 8;
 constexpr int kLaunchesInit = 2;
 
+// ---- batch slots (runtime.cu): the launch contexts of the serving loop (serving.cu) ------
+// A slot owns a stream, a device batch and its pinned mirrors.  slot_launch queues one
+// batched frame of n distinct handles and returns without waiting; slot_done tells whether
+// that frame finished; slot_finish waits for it and returns its status.  A handle must not
+// be in two unfinished launches at once (the serving loop keeps one frame per stream in
+// flight); a slot takes its next launch only after slot_finish.
+struct BatchSlot;
+struct SlotFrame {
+    dogm_handle* h;
+    const dogm_measurement_cell* meas;  // NULL keeps the resident grid
+    int device;                         // meas is a device pointer
+    float x, y, yaw, dt;
+    dogm_grid_cell* cells_out;          // host buffer for the grid after the update, or NULL
+};
+dogm_status slot_create(int device, BatchSlot** out);
+void slot_destroy(BatchSlot* s);
+dogm_status slot_launch(BatchSlot* s, const SlotFrame* frames, int n);
+bool slot_done(BatchSlot* s);
+dogm_status slot_finish(BatchSlot* s);
+// Per-handle helpers of the per-stream serving mode.
+cudaStream_t handle_stream(dogm_handle* h);
+const dogm_grid_cell* handle_cells(dogm_handle* h);
+int handle_cell_count(const dogm_handle* h);
+void set_last_error(const char* msg);
+
 }  // namespace dogm_gb300

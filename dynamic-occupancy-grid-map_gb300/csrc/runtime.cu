@@ -286,8 +286,26 @@ cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
     return cudaSuccess;
 }
 
+// Steady-state graphs are keyed by a power-of-two bucket of the batch size: the kernels read
+// only descriptors [0, n_grids), so a graph that uploads bucket(n) >= n descriptors serves
+// every batch size in the bucket and a serving loop with changing batch sizes instantiates at
+// most 9 graphs per mirror.
+int graph_bucket(int n) {
+    int b = 1;
+    while (b < n) b <<= 1;
+    return std::min(b, kMaxBatch);
+}
+
+// A device-to-host copy queued after a frame's kernels and before its completion event.
+struct HostCopy {
+    void* dst;
+    const void* src;
+    size_t bytes;
+};
+
 // Queues one frame from the current mirror and advances to the other mirror.
-dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launches) {
+dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launches,
+                      const std::vector<HostCopy>* after = nullptr) {
     cudaError_t e;
     const bool plain = any_init || any_clear || c.profile;
     if (plain) {
@@ -298,12 +316,13 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
         DOGM_CUDA(download_status(c));
         *launches = kLaunchesPerFrame + (any_init || any_clear ? 1 : 0) + (any_init ? kLaunchesInit : 0);
     } else {
-        const int key = n * 2 + c.cur;
+        const int nb = graph_bucket(n);
+        const int key = nb * 2 + c.cur;
         auto it = c.graphs.find(key);
         if (it == c.graphs.end()) {
             cudaGraph_t graph;
             DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-            e = upload_batch(c, n);
+            e = upload_batch(c, nb);
             if (e == cudaSuccess) e = frame_kernels(c, false, false);
             if (e == cudaSuccess) e = download_status(c);
             cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
@@ -319,6 +338,9 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
         DOGM_CUDA(cudaGraphLaunch(it->second, c.stream));
         *launches = kLaunchesPerFrame;
     }
+    if (after)
+        for (const HostCopy& hc : *after)
+            DOGM_CUDA(cudaMemcpyAsync(hc.dst, hc.src, hc.bytes, cudaMemcpyDeviceToHost, c.stream));
     DOGM_CUDA(cudaEventRecord(c.done[c.cur], c.stream));
     c.pending[c.cur] = true;
     c.cur ^= 1;
@@ -933,3 +955,103 @@ dogm_status dogm_memcpy(void* dst, const void* src, size_t bytes, int kind) {
 }
 
 }  // extern "C"
+
+// ---- batch slots of the serving loop ---------------------------------------------------------
+
+namespace dogm_gb300 {
+
+struct BatchSlot {
+    Ctx ctx;
+    std::vector<dogm_handle*> hs;  // handles of the unfinished launch
+    int mirror = -1;               // mirror whose done event marks that launch
+};
+
+dogm_status slot_create(int device, BatchSlot** out) {
+    *out = nullptr;
+    DeviceGuard dg(device);
+    BatchSlot* s = new BatchSlot();
+    dogm_status st = ctx_init(s->ctx, device);
+    if (st != DOGM_OK) { delete s; return st; }
+    if (prepare_kernels() != cudaSuccess || prepare_cells() != cudaSuccess) {
+        delete s;
+        return fail(DOGM_ERR_CUDA, "kernel attribute setup failed");
+    }
+    *out = s;
+    return DOGM_OK;
+}
+
+void slot_destroy(BatchSlot* s) {
+    if (!s) return;
+    DeviceGuard dg(s->ctx.device);
+    cudaStreamSynchronize(s->ctx.stream);
+    delete s;
+}
+
+// The same per-handle steps as dogm_update_batch (measurement copy, pose bookkeeping, frame
+// descriptors, one launch per stage for all handles), without the waits: the caller
+// guarantees that no handle has unfinished work elsewhere.
+dogm_status slot_launch(BatchSlot* s, const SlotFrame* fr, int n) {
+    if (!s || !fr || n <= 0 || n > kMaxBatch) return fail(DOGM_ERR_INVALID_ARGUMENT, "bad slot launch");
+    if (s->mirror >= 0) return fail(DOGM_ERR_NOT_READY, "slot launch before the previous one was finished");
+    Ctx& c = s->ctx;
+    DeviceGuard dg(c.device);
+    dogm_status st = acquire_mirror(c);
+    if (st != DOGM_OK) return st;
+    s->hs.assign(n, nullptr);
+    std::vector<int> init_mask(n, 0);
+    std::vector<HostCopy> copies;
+    bool any_init = false, any_clear = false;
+    for (int i = 0; i < n; ++i) {
+        dogm_handle* h = fr[i].h;
+        s->hs[i] = h;
+        const dogm_measurement_cell* src;
+        int copy;
+        st = prepare_measurement(h, fr[i].meas, fr[i].device, c.stream, &src, &copy);
+        if (st != DOGM_OK) return st;
+        init_mask[i] = h->first_measurement_received ? 0 : 1;
+        any_init |= init_mask[i] != 0;
+        any_clear |= h->need_clear;
+        int shifted, xm, ym;
+        pose_update(h, fr[i].x, fr[i].y, fr[i].yaw, &shifted, &xm, &ym);
+        fill_frame(h, fr[i].dt, shifted, xm, ym, src, copy);
+        if (fr[i].cells_out)
+            copies.push_back({fr[i].cells_out, h->desc.cells, sizeof(dogm_grid_cell) * (size_t)h->C});
+    }
+    build_batch(c, s->hs.data(), n, init_mask);
+    const int mirror = c.cur;
+    int launches = 0;
+    st = run_frame(c, n, any_init, any_clear, &launches, &copies);
+    if (st != DOGM_OK) {
+        for (int i = 0; i < n; ++i) s->hs[i]->need_clear = true;
+        s->hs.clear();
+        return st;
+    }
+    for (int i = 0; i < n; ++i) {
+        advance(s->hs[i]);
+        s->hs[i]->last_launches = launches;
+    }
+    s->mirror = mirror;
+    return DOGM_OK;
+}
+
+bool slot_done(BatchSlot* s) {
+    if (!s || s->mirror < 0) return true;
+    DeviceGuard dg(s->ctx.device);
+    return cudaEventQuery(s->ctx.done[s->mirror]) != cudaErrorNotReady;
+}
+
+dogm_status slot_finish(BatchSlot* s) {
+    if (!s || s->mirror < 0) return DOGM_OK;
+    DeviceGuard dg(s->ctx.device);
+    s->mirror = -1;
+    dogm_status st = finish_frame(s->ctx, s->hs.data(), (int)s->hs.size());
+    s->hs.clear();
+    return st;
+}
+
+cudaStream_t handle_stream(dogm_handle* h) { return h->ctx.stream; }
+const dogm_grid_cell* handle_cells(dogm_handle* h) { return h->desc.cells; }
+int handle_cell_count(const dogm_handle* h) { return h->C; }
+void set_last_error(const char* msg) { g_last_error = msg; }
+
+}  // namespace dogm_gb300

@@ -153,3 +153,29 @@ def random_measurements(gs: int, seed: int, occ_fraction: float = 0.02) -> np.nd
     m[:, 2] = 1.0
     m[:, 3] = 1.0
     return m
+
+
+def stream_configs(n: int, seed: int = 0, side_min: int = 128, side_max: int = 1024,
+                   density: float = 0.004) -> list[dict]:
+    """Uneven sensor streams for the batched and serving workloads: square grids with a side
+    drawn log-uniform in [side_min, side_max] cells at a resolution U(0.1, 0.2) m, 1.5
+    persistent particles per cell and 10 % newborns, and a static sensor among obstacles at
+    `density` per square metre (the small workload's scene: 2 x 4.5 m vehicles at U(0, 15) m/s,
+    1080 beams).  The size is chosen so that int(float(size) / float(resolution)) is the side."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        side = int(round(np.exp(rng.uniform(np.log(side_min), np.log(side_max)))))
+        res = float(np.float32(rng.uniform(0.1, 0.2)))
+        size = float(np.float32(side * res))
+        while int(np.float32(size) / np.float32(res)) < side:
+            size = float(np.nextafter(np.float32(size), np.float32(np.inf)))
+        while int(np.float32(size) / np.float32(res)) > side:
+            size = float(np.nextafter(np.float32(size), np.float32(0)))
+        cells = side * side
+        n_part = int(1.5 * cells)
+        area = (side * res) ** 2
+        out.append(dict(size=size, resolution=res, particle_count=n_part, new_born_particle_count=n_part // 10,
+                        frames=2, vehicles=max(1, int(round(density * area))), pedestrians=0, beams=1080,
+                        ego_speed=0.0, yaw_rate=0.0, range_noise=0.05))
+    return out

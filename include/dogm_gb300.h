@@ -224,6 +224,117 @@ dogm_status dogm_memcpy(void* dst, const void* src, size_t bytes, int kind /* cu
 /* Device bytes a handle with these parameters holds (admission control). */
 size_t dogm_state_bytes(const dogm_params* params);
 
+/* ---- serving loop ----------------------------------------------------------------------
+ *
+ * No counterpart in the reference (one dogm::DOGM per sensor, updated synchronously by its
+ * caller, dogm/demo/main.cpp:81-92).  A server keeps many sensor streams resident on one
+ * device -- each stream is a dogm_handle with its particles and grid -- admits streams under an
+ * HBM budget, and updates the frames that callers submit by continuous batching: a worker
+ * thread takes the oldest pending frame of every stream that has no frame on the device, up to
+ * max_batch of them, and queues them as one batched update (dogm_update_batch's launch
+ * sequence and CUDA graph) on one of max_inflight launch slots, so that frames arriving while
+ * others run join the next launch and launches overlap on the device.  Each frame's result is
+ * bit-identical to updating its stream alone with dogm_update (same handle, same frames).
+ * DOGM_SERVE_PER_STREAM instead updates every frame on its own with dogm_update on the
+ * stream's own CUDA stream (the plain-launch comparison).  All calls are thread-safe. */
+
+typedef enum dogm_serve_mode {
+    DOGM_SERVE_BATCHED = 0,   /* continuous batching over launch slots                       */
+    DOGM_SERVE_PER_STREAM = 1 /* one dogm_update per frame on the stream's own CUDA stream     */
+} dogm_serve_mode;
+
+typedef struct dogm_server_config {
+    size_t hbm_budget_bytes; /* resident stream state (dogm_state_bytes) stays within this      */
+    int mode;                /* dogm_serve_mode                                                */
+    int max_batch;           /* frames per batched launch, 1..256                              */
+    int max_inflight;        /* batched launches queued on the device at once, 1..4            */
+    int queue_admission;     /* 1: a stream that does not fit waits for memory to free up;
+                                0: dogm_server_open_stream refuses it with DOGM_ERR_BUDGET      */
+} dogm_server_config;
+
+/* One finished frame.  Times are nanoseconds of the monotonic clock of dogm_server_now_ns. */
+typedef struct dogm_server_result {
+    int stream;          /* id from dogm_server_open_stream                                    */
+    int status;          /* dogm_status of the frame                                           */
+    uint64_t tag;        /* the caller's tag from dogm_server_submit                           */
+    int iteration;       /* completed updates of the stream, this one included                 */
+    int batch_size;      /* frames in the launch that carried this one (1 per stream)          */
+    int64_t t_submit_ns; /* dogm_server_submit accepted the frame                              */
+    int64_t t_launch_ns; /* the frame's launch was queued on the device                        */
+    int64_t t_done_ns;   /* the worker saw the launch finished (update and readback done)      */
+} dogm_server_result;
+
+typedef struct dogm_server_stats {
+    uint64_t frames_submitted, frames_done, launches;
+    int streams_active;      /* admitted, with device state                                    */
+    int streams_waiting;     /* opened, waiting for the budget                                 */
+    size_t resident_bytes;   /* dogm_state_bytes of the admitted streams                       */
+    size_t budget_bytes;
+    double mean_batch;       /* frames per launch so far                                       */
+} dogm_server_stats;
+
+typedef struct dogm_server dogm_server;
+
+/* Stream states reported by dogm_server_stream_state. */
+#define DOGM_STREAM_WAITING 0 /* opened, not admitted yet (over budget)                          */
+#define DOGM_STREAM_ACTIVE 1  /* admitted: device state allocated                                 */
+#define DOGM_STREAM_CLOSED 2  /* closed, or admission failed                                      */
+
+/* Defaults: 150 GB budget, batched, max_batch 64, max_inflight 2, queued admission. */
+dogm_status dogm_server_default_config(dogm_server_config* cfg);
+
+/* Creates a server on the current device and starts its worker thread. */
+dogm_status dogm_server_create(const dogm_server_config* cfg, dogm_server** out);
+
+/* Finishes every submitted frame of the admitted streams, frees all streams, stops the worker. */
+dogm_status dogm_server_destroy(dogm_server* s);
+
+/* Opens a stream with the filter parameters of one dogm_handle (opt may be NULL).  If its
+ * dogm_state_bytes fit the budget next to the admitted streams (and no earlier stream waits),
+ * its device state is allocated now; otherwise, with queue_admission, it waits (state
+ * DOGM_STREAM_WAITING; frames may already be submitted) until closed streams free the budget,
+ * and without queue_admission the call returns DOGM_ERR_BUDGET.  A stream larger than the
+ * whole budget is always refused with DOGM_ERR_BUDGET. */
+dogm_status dogm_server_open_stream(dogm_server* s, const dogm_params* params, const dogm_options* opt,
+                                    int* stream_id);
+
+/* Finishes the stream's submitted frames, frees its device state and admits waiting streams
+ * that now fit.  Returns when the stream is closed. */
+dogm_status dogm_server_close_stream(dogm_server* s, int stream_id);
+
+/* Queues one frame of a stream (the arguments of dogm_update).  meas (host, or device with
+ * device != 0; pinned host memory copies fastest) must stay valid and unchanged until the
+ * frame's result is returned.  cells_out, if not NULL, is a host buffer of grid_size^2 cells
+ * that receives the stream's grid after this update.  A stream's frames run in submission
+ * order, one at a time. */
+dogm_status dogm_server_submit(dogm_server* s, int stream_id, const dogm_measurement_cell* meas, int device,
+                               float new_x, float new_y, float new_yaw, float dt, dogm_grid_cell* cells_out,
+                               uint64_t tag);
+
+/* paused != 0 holds back new launches (launches in flight finish; submitted frames queue);
+ * paused == 0 resumes, and the next launches take every frame that queued meanwhile. */
+dogm_status dogm_server_pause(dogm_server* s, int paused);
+
+/* Moves up to max finished frames into out, waiting up to timeout_us for the first one;
+ * *n_out receives the count (0 on timeout). */
+dogm_status dogm_server_poll(dogm_server* s, dogm_server_result* out, int max, int timeout_us, int* n_out);
+
+/* Waits until every submitted frame has finished (DOGM_ERR_NOT_READY after timeout_ms, for
+ * example while frames of a waiting stream cannot run). */
+dogm_status dogm_server_drain(dogm_server* s, int timeout_ms);
+
+dogm_status dogm_server_get_stats(dogm_server* s, dogm_server_stats* out);
+
+/* DOGM_STREAM_* state of a stream, or -1 for an unknown id. */
+int dogm_server_stream_state(dogm_server* s, int stream_id);
+
+/* The dogm_handle of an admitted stream, for the readback calls (dogm_get_grid_cells ...).
+ * Use it only while none of the stream's frames is pending (after dogm_server_drain). */
+dogm_status dogm_server_stream_handle(dogm_server* s, int stream_id, dogm_handle** out);
+
+/* The clock of dogm_server_result (monotonic, nanoseconds). */
+int64_t dogm_server_now_ns(void);
+
 /* ---- measurement ---------------------------------------------------------------------- */
 
 /* The cudaStream_t (as void*) the handle launches on: record CUDA events on it to time updates. */

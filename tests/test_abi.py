@@ -75,3 +75,29 @@ def test_cpp_dropin_compiles_and_links(dogm, tmp_path):
     r = subprocess.run([gxx, "-std=c++17", "-O1", "-I", os.path.join(REPO, "include"), src, "-o", exe,
                         "-L" + lib_dir, "-ldogm_gb300", "-Wl,-rpath," + lib_dir], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_server_argument_checks_without_gpu(dogm):
+    """Serving-loop configuration and stream checks that return before any device call."""
+    lib = dogm.load()
+    cfg = dogm.ServerConfig()
+    assert lib.dogm_server_default_config(ctypes.byref(cfg)) == 0
+    assert cfg.hbm_budget_bytes == 150 * 10**9 and cfg.mode == dogm.SERVE_BATCHED
+    assert cfg.max_batch == 64 and cfg.max_inflight == 2 and cfg.queue_admission == 1
+    s = ctypes.c_void_p()
+    for field, value in (("max_batch", 0), ("max_batch", 257), ("max_inflight", 5), ("mode", 7),
+                         ("hbm_budget_bytes", 0)):
+        bad = dogm.ServerConfig()
+        lib.dogm_server_default_config(ctypes.byref(bad))
+        setattr(bad, field, value)
+        assert lib.dogm_server_create(ctypes.byref(bad), ctypes.byref(s)) == 1, field
+    assert lib.dogm_server_create(None, ctypes.byref(s)) == 1
+    sid = ctypes.c_int(0)
+    assert lib.dogm_server_open_stream(None, None, None, ctypes.byref(sid)) == 1
+    assert lib.dogm_server_submit(None, 0, None, 0, 0.0, 0.0, 0.0, 0.1, None, 0) == 1
+    assert lib.dogm_server_stream_state(None, 0) == -1
+    n = ctypes.c_int(5)
+    assert lib.dogm_server_poll(None, None, 0, 0, ctypes.byref(n)) == 1
+    t0 = lib.dogm_server_now_ns()
+    assert lib.dogm_server_now_ns() >= t0 > 0
+    assert ctypes.sizeof(dogm.ServerResult) == 48 and ctypes.sizeof(dogm.ServerStats) == 56
