@@ -505,6 +505,7 @@ def run_reference(args, rank: int, world: int):
     b = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(b)
     b.build_oracle()
+    b.build_ref_harness()
     dogm = importlib.import_module(PKG)
     p = dogm.make_params(**importlib.import_module(PKG + ".scene").params_dict(cfg))
     ref = pyoracle.ReferencePipeline(p, threads=0)
@@ -517,7 +518,7 @@ def run_reference(args, rank: int, world: int):
         ref.update(m, x, y, yaw, 0.1)
     ms = (time.perf_counter() - t0) * 1e3 / K
     sample = "%d full updates of the %s workload (1.44e6 cells, 2e6 + 2e5 particles)" % (K, WORKLOAD)
-    return {"impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/update", "n_gpus": world,
+    line = {"impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/update", "n_gpus": world,
             "steps": K, "warmup": W, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "large: 120 x 120 m at 0.1 m (1200^2 cells), 2e6 + 2e5 particles",
@@ -526,6 +527,51 @@ def run_reference(args, rank: int, world: int):
             "cpu_baseline": {"value": round(ms, 3), "unit": "ms/update", "cores": ref.threads_used, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(ms, 3), "unit": "ms/update", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["reference_cuda"] = reference_cuda(dogm, p, frames, W, min(K, 100))
+    return line
+
+
+def reference_cuda(dogm, p, frames, warm: int, steps: int) -> dict:
+    """The reference's own CUDA build on this GPU: its kernels (cubins compiled from
+    dogm/src/kernel/) in the restated updateGrid sequence (oracle/ref/ref_harness.cu).  Each
+    update is synchronous, like the reference's (dogm.cu:130): host wall clock per update,
+    measurement grids resident in HBM; e2e adds the host measurement copy and the grid readback
+    (getGridCells) per update."""
+    import pyref
+    why = pyref.missing()
+    if why:
+        return {"unavailable": why}
+    bufs = []
+    for m, *_ in frames:
+        d = dogm.DeviceBuffer(m.nbytes)
+        d.upload(m)
+        bufs.append(d)
+    ref = pyref.ReferenceDOGM(p)
+    fr = lambda k: pingpong(k, len(frames))
+    for k in range(warm + 1):
+        _, x, y, yaw = frames[fr(k)]
+        ref.update(bufs[fr(k)].ptr, x, y, yaw, 0.1, device=True)
+    times = []
+    for k in range(warm + 1, warm + 1 + steps):
+        _, x, y, yaw = frames[fr(k)]
+        t0 = time.perf_counter()
+        ref.update(bufs[fr(k)].ptr, x, y, yaw, 0.1, device=True)
+        times.append((time.perf_counter() - t0) * 1e3)
+    e2e = []
+    for k in range(warm + 1 + steps, warm + 1 + steps + max(steps // 4, 5)):
+        m, x, y, yaw = frames[fr(k)]
+        t0 = time.perf_counter()
+        ref.update(m, x, y, yaw, 0.1, device=False)
+        ref.get_grid_cells()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    ref.close()
+    for d in bufs:
+        d.free()
+    return {"ms_per_update": round(statistics.median(times), 3), "mean_ms": round(statistics.fmean(times), 3),
+            "e2e_ms": round(statistics.median(e2e), 3), "steps": steps,
+            "kind": "reference kernels compiled from dogm/src/kernel/*.cu for sm_103a, run in the restated "
+                    "dogm::DOGM::updateGrid host sequence (Thrust from the CUDA toolkit, legacy stream, its "
+                    "host synchronisations and per-frame temporaries)"}
 
 
 _dist = None

@@ -101,9 +101,28 @@ def build_oracle(verbose: bool = False) -> str:
     return ORACLE_LIB
 
 
+REF_HARNESS_SRC = os.path.join(ORACLE_DIR, "ref", "ref_harness.cu")
+REF_HARNESS_LIB = os.path.join(ORACLE_BUILD, "libdogm_ref.so")
+
+
+def build_ref_harness(verbose: bool = False) -> str:
+    """Compile the reference-build harness (test infrastructure: loads the reference's kernel
+    cubins from oracle/_ref and runs them in the reference's host sequence)."""
+    os.makedirs(ORACLE_BUILD, exist_ok=True)
+    if _stale(REF_HARNESS_LIB, [REF_HARNESS_SRC, __file__]):
+        tmp = REF_HARNESS_LIB + ".tmp"
+        _run([_nvcc()] + ARCH + ["-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", REF_HARNESS_SRC, "-lcuda",
+                                 "-o", tmp])
+        os.replace(tmp, REF_HARNESS_LIB)
+    if verbose:
+        print("built", REF_HARNESS_LIB)
+    return REF_HARNESS_LIB
+
+
 def build_all(verbose: bool = False) -> None:
     build_cuda(verbose)
     build_oracle(verbose)
+    build_ref_harness(verbose)
 
 
 if __name__ == "__main__":

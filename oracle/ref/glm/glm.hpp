@@ -1,0 +1,4 @@
+// Minimal GLM-compatible umbrella header (see vec4.hpp).
+#pragma once
+#include "mat4x4.hpp"
+#include "vec4.hpp"

@@ -43,3 +43,15 @@ def dogm():
 @pytest.fixture(scope="session")
 def scene():
     return importlib.import_module(PKG + ".scene")
+
+
+@pytest.fixture(scope="session")
+def pyref():
+    """The reference's own CUDA build (oracle/pyref.py); skips where its cubins are absent."""
+    _build().build_ref_harness()
+    import pyref as mod
+    why = mod.missing()
+    if why:
+        pytest.skip(why)
+    mod.load()
+    return mod
