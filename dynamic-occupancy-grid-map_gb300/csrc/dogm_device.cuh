@@ -268,15 +268,12 @@ __device__ __forceinline__ unsigned long long block_sum_before(const unsigned lo
     return total;
 }
 
-// Exclusive scan of one 64-bit value per thread, offset by sums[0 .. t) (the per-tile sums a
-// previous kernel completed): returns sums[0..t) + (exclusive prefix of v); *total gets the
-// block's sum of v.  One barrier round for both.
-__device__ __forceinline__ unsigned long long block_scan_after(unsigned long long v, const unsigned long long* sums,
-                                                               int t, unsigned long long* scratch16,
-                                                               unsigned long long* total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+// This thread's share of sums[0 .. t) (the per-tile sums a previous kernel completed), four
+// independent loads in flight per thread.  Split from the scan below so that a caller can
+// issue these loads next to its own before waiting on either.
+__device__ __forceinline__ unsigned long long block_prefix_part(const unsigned long long* sums, int t) {
     unsigned long long part = 0ull;
-    for (int i0 = 0; i0 < t; i0 += 4 * kThreads) {  // four independent loads in flight per thread
+    for (int i0 = 0; i0 < t; i0 += 4 * kThreads) {
         unsigned long long a[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -285,6 +282,16 @@ __device__ __forceinline__ unsigned long long block_scan_after(unsigned long lon
         }
         part += (a[0] + a[1]) + (a[2] + a[3]);
     }
+    return part;
+}
+
+// Exclusive scan of one 64-bit value per thread, offset by the block total of the threads'
+// parts (block_prefix_part): returns sum(parts) + (exclusive prefix of v); *total gets the
+// block's sum of v.  One barrier round for both.
+__device__ __forceinline__ unsigned long long block_scan_with_part(unsigned long long v, unsigned long long part,
+                                                                   unsigned long long* scratch16,
+                                                                   unsigned long long* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -306,6 +313,15 @@ __device__ __forceinline__ unsigned long long block_scan_after(unsigned long lon
     __syncthreads();
     *total = tot;
     return before + wpre + x - v;
+}
+
+// Exclusive scan of one 64-bit value per thread, offset by sums[0 .. t) (the per-tile sums a
+// previous kernel completed): returns sums[0..t) + (exclusive prefix of v); *total gets the
+// block's sum of v.
+__device__ __forceinline__ unsigned long long block_scan_after(unsigned long long v, const unsigned long long* sums,
+                                                               int t, unsigned long long* scratch16,
+                                                               unsigned long long* total) {
+    return block_scan_with_part(v, block_prefix_part(sums, t), scratch16, total);
 }
 
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {

@@ -92,7 +92,7 @@ struct GridDesc {
     const dogm_measurement_cell* meas_src;
     dogm_measurement_cell* meas_own;
     float* free_old; float* free_new;   // free mass of the previous / this frame (ping-pong)
-    float* rho_b;           // per cell newborn mass of this frame
+    float2* rho_b;          // per cell {newborn mass, p_A} of this frame (the newborn kernel's input)
     float* w_cell;          // per cell weight of an in-grid persistent particle after reweighting
     // scratch
     uint32_t* hist;         // 2 x kSortMaxBins digit histograms

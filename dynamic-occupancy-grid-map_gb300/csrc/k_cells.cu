@@ -92,11 +92,22 @@ struct CellSmem {
     int end[kCellTile];     // sorted position of the last particle
     int n_in[kCellTile];    // in-grid particles
     float vx[kCellTile], vy[kCellTile], vxx[kCellTile], vyy[kCellTile], vxy[kCellTile];
+    // per warp: its 32 cell records (2 KB), staged so that the warp stores them as 512
+    // contiguous bytes per instruction instead of four 16-byte pieces at 64-byte stride
+    float4 stage[kCellThreads / 32][32 * 4];
     Run wagg[kCellThreads / 32];
     unsigned long long red[kCellThreads / 32], red2[kCellThreads / 32];
     int tile;
 };
 static_assert(offsetof(CellSmem, meas) % 16 == 0, "16-byte cp.async destination");
+static_assert(offsetof(CellSmem, stage) % 16 == 0, "16-byte staged records");
+static_assert(sizeof(dogm_grid_cell) == 64, "a record is four float4");
+
+// Record chunk j of lane l is staged at float4 slot 4 l + (j ^ ((l >> 1) & 3)): for each j the
+// eight lanes of a 128-byte shared-memory wavefront hit eight distinct 16-byte bank groups, and
+// reading record r's chunk c back from slot 4 r + (c ^ ((r >> 1) & 3)) gives lanes 4 q .. 4 q + 3
+// one whole record, again without conflicts.
+__device__ __forceinline__ int stage_slot(int rec, int chunk) { return rec * 4 + (chunk ^ ((rec >> 1) & 3)); }
 
 // The quantised weights of a cell's in-grid persistent particles (sorted positions
 // [start, end]) added to the resample tiles that hold them.  Out-of-grid particles (weight
@@ -268,7 +279,10 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
         for (int r = 0; r < kCellTile / kCellThreads; ++r) {
             const int cl = r * kCellThreads + threadIdx.x;
             const int k = base + cl;
-            if (k >= g.C) break;
+            const int warp_first = base + r * kCellThreads + warp * 32;  // the warp's 32 cells
+            if (warp_first >= g.C) break;                                // warp-uniform
+            float4* stage = sm.stage[warp];
+            if (k < g.C) {
             const bool occupied = sm.start[cl] >= 0;  // end, count and sums are set only then
             const int start = occupied ? sm.start[cl] : -1, end = occupied ? sm.end[cl] : -1;
             const int n_in = occupied ? sm.n_in[cl] : 0;
@@ -294,13 +308,12 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                     cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.vxy[cl])), __fmul_rn(mx, my));
                 }
             }
-            float4* rec = reinterpret_cast<float4*>(g.cells + k);
-            rec[0] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
-            rec[1] = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
-            rec[2] = make_float4(muUA, 0.0f, 0.0f, mx);
-            rec[3] = make_float4(my, vx, vy, cxy);
+            stage[stage_slot(lane, 0)] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
+            stage[stage_slot(lane, 1)] = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
+            stage[stage_slot(lane, 2)] = make_float4(muUA, 0.0f, 0.0f, mx);
+            stage[stage_slot(lane, 3)] = make_float4(my, vx, vy, cxy);
             g.free_new[k] = o.free_up;
-            g.rho_b[k] = o.rho_b;
+            g.rho_b[k] = make_float2(o.rho_b, m.p_A);
             g.w_cell[k] = wp;
             qb += quantize(o.rho_b, g.q_shift);
             const unsigned long long qw = n_in > 0 ? quantize(wp, g.q_shift) : 0ull;
@@ -308,6 +321,17 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                 jq += (unsigned long long)n_in * qw;
                 add_persistent(g, start, end, n_in, qw);
             }
+            }  // k < g.C
+            // the warp's records, 512 contiguous bytes per store instruction
+            __syncwarp();
+            const int n_rec = min(32, g.C - warp_first);
+            float4* dst = reinterpret_cast<float4*>(g.cells + warp_first);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int rec = q * 8 + (lane >> 2), chunk = lane & 3;
+                if (rec < n_rec) dst[rec * 4 + chunk] = stage[stage_slot(rec, chunk)];
+            }
+            __syncwarp();  // the stage is refilled by the next r
         }
         unsigned long long tile_qb, tile_jq;
         block_excl_scan_u64<kCellThreads>(qb, sm.red, &tile_qb);
@@ -365,17 +389,24 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
         const unsigned long long T = g.fs->qb_total;
         unsigned long long q[kCellIpt];
         float rb[kCellIpt], pA[kCellIpt];
-        unsigned long long v = 0ull;
+        float2 bp[kCellIpt];
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
             const int k = base + threadIdx.x * kCellIpt + j;
-            rb[j] = (k < g.C) ? g.rho_b[k] : 0.0f;
-            q[j] = (k < g.C) ? quantize(rb[j], g.q_shift) : 0ull;
-            pA[j] = q[j] ? g.meas_own[k].p_A : 0.0f;  // only a cell with mass can get newborns
+            bp[j] = (k < g.C) ? g.rho_b[k] : make_float2(0.0f, 0.0f);  // {rho_b, p_A}
+        }
+        // the earlier tiles' sums load while the cells' values are in flight
+        const unsigned long long part = block_prefix_part(g.cell_sum, lt);
+        unsigned long long v = 0ull;
+#pragma unroll
+        for (int j = 0; j < kCellIpt; ++j) {
+            rb[j] = bp[j].x;
+            pA[j] = bp[j].y;
+            q[j] = quantize(rb[j], g.q_shift);
             v += q[j];
         }
         unsigned long long tile_sum;
-        unsigned long long acc = block_scan_after(v, g.cell_sum, lt, red, &tile_sum);
+        unsigned long long acc = block_scan_with_part(v, part, red, &tile_sum);
         const float sc = T ? __fdiv_rn((float)g.B, __ull2float_rn(T)) : 0.0f;
         int bnd[kCellIpt + 1];
         bnd[0] = alloc_boundary_fast(acc, T, g.B, sc);

@@ -439,8 +439,8 @@ size_t dogm_state_bytes(const dogm_params* p) {
     size_t b = 0;
     b += N * (16 + 4) + N * (4 + 4) + N * (16 + 4);    // P, T, S particles
     b += B * (16 + 4 + 4);                            // newborns
-    // per cell: record 64, measurement copy 16, free mass 2 x 4, newborn mass 4, cell weight 4
-    b += C * (sizeof(dogm_grid_cell) + sizeof(dogm_measurement_cell) + 2 * 4 + 4 + 4);
+    // per cell: record 64, measurement copy 16, free mass 2 x 4, {newborn mass, p_A} 8, cell weight 4
+    b += C * (sizeof(dogm_grid_cell) + sizeof(dogm_measurement_cell) + 2 * 4 + 8 + 4);
     b += 2 * kSortMaxBins * 4 + (size_t)2 * s.sort_tiles * kSortMaxBins * 4;
     b += (size_t)s.cell_tiles * (16 + 12) + 4 + (size_t)s.res_tiles * 8;
     b += sizeof(Batch);
