@@ -42,7 +42,12 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
 // weight w_res, so the predicted weight is p_S * w_res, or 0 out of the grid (bit 30).
 // mode 0: full frame (shift + digit histograms); mode 1: stage call (no histograms).
 // ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, int mode) {
+// 512 threads per 4096-particle tile (8 particles each): the kernel is issue-bound, and twice
+// the warps of a 256-thread block keep about 50 warps per SM in flight over the frame's tiles.
+constexpr int kPredictThreads = 512;
+static_assert(kPredictTile % kPredictThreads == 0, "whole particles per thread");
+
+__global__ void __launch_bounds__(kPredictThreads) k_predict(Batch* __restrict__ bt, int mode) {
     __shared__ uint32_t h0[kSortMaxBins];
     __shared__ uint32_t h1[kSortMaxBins];
     __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (ranges of the cell pass)
@@ -69,9 +74,9 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, in
         const int lt = t - bt->prefix[gi][kStPredict];
         const int nb0 = 1 << g.d0_bits, nb1 = 1 << g.d1_bits;
         if (mode == 0) {
-            for (int i = threadIdx.x; i < nb0; i += kThreads) h0[i] = 0u;
-            for (int i = threadIdx.x; i < nb1; i += kThreads) h1[i] = 0u;
-            for (int i = threadIdx.x; i < g.tiles[kStCell]; i += kThreads) h2[i] = 0u;
+            for (int i = threadIdx.x; i < nb0; i += kPredictThreads) h0[i] = 0u;
+            for (int i = threadIdx.x; i < nb1; i += kPredictThreads) h1[i] = 0u;
+            for (int i = threadIdx.x; i < g.tiles[kStCell]; i += kPredictThreads) h2[i] = 0u;
             __syncthreads();
         }
         const float gsm1 = (float)(g.gs - 1);
@@ -80,8 +85,8 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, in
         const float fsx = (float)g.shift_x, fsy = (float)g.shift_y;
         const int base = lt * kPredictTile;
 #pragma unroll 4
-        for (int k = 0; k < kPredictTile / kThreads; ++k) {
-            const int i = base + k * kThreads + threadIdx.x;
+        for (int k = 0; k < kPredictTile / kPredictThreads; ++k) {
+            const int i = base + k * kPredictThreads + threadIdx.x;
             const bool valid = i < g.N;
             uint32_t key = 0xffffffffu;
             if (valid) {
@@ -130,13 +135,13 @@ __global__ void __launch_bounds__(kThreads) k_predict(Batch* __restrict__ bt, in
             __syncthreads();
             // this tile's digit-0 counts (upsweep of sort pass 0: predict and sort tiles coincide)
             uint32_t* row = g.hsort + (size_t)lt * kSortMaxBins;
-            for (int i = threadIdx.x; i < nb0; i += kThreads) {
+            for (int i = threadIdx.x; i < nb0; i += kPredictThreads) {
                 row[i] = h0[i];
                 if (h0[i]) atomicAdd(&g.hist[i], h0[i]);
             }
-            for (int i = threadIdx.x; i < nb1; i += kThreads)
+            for (int i = threadIdx.x; i < nb1; i += kPredictThreads)
                 if (h1[i]) atomicAdd(&g.hist[kSortMaxBins + i], h1[i]);
-            for (int i = threadIdx.x; i < g.tiles[kStCell]; i += kThreads)
+            for (int i = threadIdx.x; i < g.tiles[kStCell]; i += kPredictThreads)
                 if (h2[i]) atomicAdd(&g.ctile_cnt[i], h2[i]);
             __syncthreads();
         }
@@ -306,7 +311,7 @@ cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCf
 }
 
 cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg) {
-    k_predict<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), stage_mode);
+    k_predict<<<cfg.num_sms * 4, kPredictThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), stage_mode);
     return cudaGetLastError();
 }
 
