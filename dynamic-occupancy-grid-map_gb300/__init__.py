@@ -40,6 +40,7 @@ ABI_SYMBOLS = [
     "dogm_get_iteration", "dogm_get_particle_count", "dogm_get_new_born_particle_count", "dogm_particle_prediction",
     "dogm_update_pose", "dogm_update_pose_noalloc", "dogm_initialize_particles", "dogm_set_measurement_cells", "dogm_set_particles",
     "dogm_set_replay", "dogm_clear_replay", "dogm_generate_draws", "dogm_debug_enable", "dogm_debug_export",
+    "dogm_debug_joint_weights",
     "dogm_lower_bound_f32", "dogm_host_alloc", "dogm_host_free", "dogm_device_alloc", "dogm_device_free",
     "dogm_memcpy", "dogm_state_bytes", "dogm_last_launch_count", "dogm_last_error", "dogm_status_string",
     "dogm_abi_version", "dogm_get_stream", "dogm_profile_enable", "dogm_stage_times", "dogm_stage_name",
@@ -116,7 +117,7 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_initialize_particles": ([vp], i), "dogm_set_measurement_cells": ([vp, vp, sz], i),
         "dogm_set_particles": ([vp, vp, vp, vp, f, sz], i), "dogm_set_replay": ([vp, vp, vp, vp, vp], i),
         "dogm_clear_replay": ([vp], i), "dogm_generate_draws": ([vp, i, vp, vp, vp, vp], i),
-        "dogm_debug_enable": ([vp, i], i),
+        "dogm_debug_enable": ([vp, i], i), "dogm_debug_joint_weights": ([vp, vp, sz, vp], i),
         "dogm_debug_export": ([vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp], i),
         "dogm_lower_bound_f32": ([vp, i, vp, i, vp, i, vp], i), "dogm_host_alloc": ([vp, sz], i),
         "dogm_host_free": ([vp], i), "dogm_device_alloc": ([vp, sz], i), "dogm_device_free": ([vp], i),
@@ -378,6 +379,14 @@ class DOGM:
         return {"sorted_cell": sc, "sorted_state": ss, "sort_perm": sp, "birth_state": bs[:b], "birth_cell": bc[:b],
                 "birth_assoc": ba[:b], "birth_weight": bw[:b], "resample_src": rs, "joint_total": int(jt[0]),
                 "q_shift": int(qs[0]), "n_birth": int(nb[0])}
+
+    def debug_joint_weights(self) -> np.ndarray:
+        """The last update's joint resampling weights (persistent sorted, then newborns)."""
+        n = self.particle_count + self.new_born_particle_count
+        w = np.empty(max(n, 1), np.float32)
+        m = C.c_int(0)
+        check(load().dogm_debug_joint_weights(self.h, _ptr(w), w.size, C.byref(m)), "dogm_debug_joint_weights")
+        return w[:m.value]
 
 
 def update_batch(grids: list[DOGM], meas: list, xs, ys, yaws, dts, device: bool = False) -> None:

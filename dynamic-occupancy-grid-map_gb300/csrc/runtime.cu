@@ -896,6 +896,27 @@ dogm_status dogm_debug_export(dogm_handle* h, int* sorted_cell, float* sorted_st
     return DOGM_OK;
 }
 
+dogm_status dogm_debug_joint_weights(dogm_handle* h, float* weights, size_t n, int* n_joint) {
+    if (!h || !weights) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!h->debug) return fail(DOGM_ERR_NOT_READY, "enable debug before the update to export the joint weights");
+    if (n < (size_t)h->N + (size_t)h->B) return fail(DOGM_ERR_INVALID_ARGUMENT, "n < particle_count + newborns");
+    DeviceGuard dg(h->device);
+    DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+    const size_t N = (size_t)h->N, C = (size_t)h->C;
+    FrameState fs;
+    DOGM_CUDA(cudaMemcpy(&fs, h->desc.fs, sizeof(fs), cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> k(N);
+    std::vector<float> wc(C);
+    DOGM_CUDA(cudaMemcpy(k.data(), h->desc.S_key, 4 * N, cudaMemcpyDeviceToHost));
+    DOGM_CUDA(cudaMemcpy(wc.data(), h->desc.w_cell, 4 * C, cudaMemcpyDeviceToHost));
+    // persistent items in sorted order: the reweighted weight of their cell, 0 out of the grid
+    for (size_t i = 0; i < N; ++i) weights[i] = (k[i] & kOutBit) ? 0.0f : wc[k[i] & kCellMask];
+    const size_t nb = (size_t)std::max(fs.n_birth, 0);
+    if (nb) DOGM_CUDA(cudaMemcpy(weights + N, h->desc.B_w, 4 * nb, cudaMemcpyDeviceToHost));
+    if (n_joint) *n_joint = (int)(N + nb);
+    return DOGM_OK;
+}
+
 // ---- measurement -------------------------------------------------------------------------
 
 void* dogm_get_stream(dogm_handle* h) { return h ? (void*)h->ctx.stream : nullptr; }

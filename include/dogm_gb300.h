@@ -204,6 +204,13 @@ dogm_status dogm_debug_export(dogm_handle* h, int* sorted_cell, float* sorted_st
                               float* birth_state, int* birth_cell, unsigned char* birth_assoc, float* birth_weight,
                               int* resample_src, uint64_t* joint_total, int* q_shift, int* n_birth);
 
+/* Debug export of the last update's resampling input (debug enabled before the update): the
+ * joint weights in joint order -- the N persistent particles in sorted order with their
+ * reweighted weights (the reference's weight_array, dogm.cu:393), then the newborns' weights
+ * (birth_particle_array.weight, dogm.cu:394) -- as float; n >= particle_count + newborns;
+ * *n_joint receives the count. */
+dogm_status dogm_debug_joint_weights(dogm_handle* h, float* weights, size_t n, int* n_joint);
+
 /* ---- utilities ------------------------------------------------------------------------ */
 
 /* Multinomial index search of the reference (thrust::lower_bound at

@@ -562,3 +562,72 @@ int dogm_oracle_reference_f32(const dogm_oracle_params* p, const float* meas, fl
     for (int k = 0; k < 5; ++k) { free(vel[k]); free(vacc[k]); }
     return nthreads;
 }
+
+/* ---- resampling-scan precision study (test infrastructure) ---------------------------------
+ * Systematic resampling of n slots over the joint weights w[0..m): slot i takes the first item
+ * j whose inclusive prefix A[j] exceeds the tooth (i + u) * A[m-1] / n, u in [0, 1) -- the comb
+ * of the GB300 path, here with the prefix kept in
+ *   mode 0: float32, summed sequentially (what a plain float scan gives at best),
+ *   mode 1: compensated float32 -- a float pair (hi, lo) per prefix built with TwoSum, teeth
+ *           and comparisons on the pair (about 48 significant bits),
+ *   mode 2: float64.
+ * out[i] = the item of slot i.  Merge walk, O(m + n). */
+static void two_sum_f(float a, float b, float* s, float* e) {
+    const float x = a + b;
+    const float bv = x - a;
+    *e = (a - (x - bv)) + (b - bv);
+    *s = x;
+}
+
+void dogm_oracle_comb_indices(const float* w, int m, int n, double u, int mode, int* out) {
+    if (m <= 0 || n <= 0) return;
+    int j = 0;
+    if (mode == 0) {
+        float* acc = (float*)malloc(sizeof(float) * (size_t)m);
+        float s = 0.0f;
+        for (int k = 0; k < m; ++k) { s = s + w[k]; acc[k] = s; }
+        const float step = acc[m - 1] / (float)n;
+        for (int i = 0; i < n; ++i) {
+            const float t = ((float)i + (float)u) * step;
+            while (j < m - 1 && !(acc[j] > t)) ++j;
+            out[i] = j;
+        }
+        free(acc);
+    } else if (mode == 1) {
+        float* hi = (float*)malloc(sizeof(float) * (size_t)m);
+        float* lo = (float*)malloc(sizeof(float) * (size_t)m);
+        float sh = 0.0f, sl = 0.0f;
+        for (int k = 0; k < m; ++k) {
+            float e;
+            two_sum_f(sh, w[k], &sh, &e);
+            sl = sl + e;
+            float h2, l2;
+            two_sum_f(sh, sl, &h2, &l2);  /* renormalise the pair */
+            sh = h2;
+            sl = l2;
+            hi[k] = sh;
+            lo[k] = sl;
+        }
+        /* tooth (i + u) * J / n with J = (hi, lo): double-float product, compared as a pair */
+        const double J = (double)hi[m - 1] + (double)lo[m - 1];
+        for (int i = 0; i < n; ++i) {
+            const double t = ((double)i + u) * (J / (double)n);
+            const float th = (float)t, tl = (float)(t - (double)th);
+            while (j < m - 1 && !(hi[j] > th || (hi[j] == th && lo[j] > tl))) ++j;
+            out[i] = j;
+        }
+        free(hi);
+        free(lo);
+    } else {
+        double* acc = (double*)malloc(sizeof(double) * (size_t)m);
+        double s = 0.0;
+        for (int k = 0; k < m; ++k) { s += (double)w[k]; acc[k] = s; }
+        const double step = acc[m - 1] / (double)n;
+        for (int i = 0; i < n; ++i) {
+            const double t = ((double)i + u) * step;
+            while (j < m - 1 && !(acc[j] > t)) ++j;
+            out[i] = j;
+        }
+        free(acc);
+    }
+}

@@ -89,4 +89,9 @@ int dogm_oracle_reference_f32(const dogm_oracle_params* p, const float* meas, fl
                               int shifted, int x_move, int y_move, uint64_t seed, uint32_t frame, float* P_state,
                               int* P_idx, float* P_w, unsigned char* P_assoc, float* cells, int threads);
 
+/* Resampling-scan precision study: systematic comb of n slots over joint weights w[0..m) with
+ * offset u in [0,1) and the prefix in float32 (mode 0), compensated float32 (1) or float64 (2);
+ * out[i] = joint item of slot i. */
+void dogm_oracle_comb_indices(const float* w, int m, int n, double u, int mode, int* out);
+
 #endif /* DOGM_ORACLE_H */

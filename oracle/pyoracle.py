@@ -57,6 +57,7 @@ def load() -> C.CDLL:
         lib.dogm_oracle_predict_f32.argtypes = [vp, C.c_float, vp, vp, vp, vp, C.c_int]
         lib.dogm_oracle_shift_particles_f32.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         lib.dogm_oracle_pose.argtypes = [C.c_float, vp, vp, vp, vp, C.c_float, C.c_float, C.c_float, vp, vp]
+        lib.dogm_oracle_comb_indices.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int, vp]
         lib.dogm_oracle_reference_f32.argtypes = [vp, vp, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64,
                                                   C.c_uint32, vp, vp, vp, vp, vp, C.c_int]
         _lib = lib
@@ -212,3 +213,15 @@ class ReferencePipeline:
             _p(self.P_state), _p(self.P_idx), _p(self.P_w), _p(self.P_assoc), _p(self.cells), self.threads)
         self.first_measurement = False
         self.frame += 1
+
+
+COMB_MODES = {"fp32": 0, "compensated_fp32": 1, "fp64": 2}
+
+
+def comb_indices(weights: np.ndarray, n: int, u: float, mode: str) -> np.ndarray:
+    """Systematic resampling of n slots over the joint weights with the prefix sum in the given
+    precision ("fp32", "compensated_fp32", "fp64"): the joint item of every slot."""
+    w = np.ascontiguousarray(weights, np.float32)
+    out = np.empty(n, np.int32)
+    load().dogm_oracle_comb_indices(_p(w), w.size, n, float(u), COMB_MODES[mode], _p(out))
+    return out
