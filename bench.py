@@ -220,6 +220,9 @@ def run_gb300(args, rank: int, world: int):
         d = dogm.DeviceBuffer(m.nbytes)
         d.upload(m)
         dbufs.append(d)
+    # launch widths and the radix split chosen by the autotuner on this GPU (a scratch handle
+    # fed the first frame; kept only when faster than the defaults)
+    tune = g.autotune(dbufs[0].ptr, reps=10, device=True) if not args.no_autotune else None
     # first measurement (initialisation) + warm-up (graph capture for both mirrors)
     for k in range(W + 1):
         m, x, y, yaw = frames[fr(k)]
@@ -305,7 +308,8 @@ def run_gb300(args, rank: int, world: int):
         "config": {"workload": "large: 120 x 120 m at 0.1 m (1200^2 = 1.44e6 cells), 2e6 persistent + 2e5 newborn "
                                "particles, ego 10 m/s", "cells": C_, "particles": N, "newborn": B,
                    "l2": "inputs larger than L2 (per-update working set > 300 MB vs 129 MB L2); no flush",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "autotune": tune.as_dict() if tune is not None else "off"},
         "hbm_gbs_whole_update": round(alg / (ms * 1e-3) / 1e9, 1),
         "updates_per_s": round(1e3 / ms, 1),
         "stage_ms": {k: round(v, 4) for k, v in stages.items()},
@@ -601,6 +605,7 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=200)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the batched and serving workloads")
+    ap.add_argument("--no-autotune", action="store_true", help="time the built-in launch shape")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="seconds of Poisson arrivals per serving mode (the serving workload names 60)")
     args = ap.parse_args()

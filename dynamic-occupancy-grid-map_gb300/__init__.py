@@ -47,6 +47,7 @@ ABI_SYMBOLS = [
     "dogm_server_default_config", "dogm_server_create", "dogm_server_destroy", "dogm_server_open_stream",
     "dogm_server_close_stream", "dogm_server_submit", "dogm_server_pause", "dogm_server_poll", "dogm_server_drain",
     "dogm_server_get_stats", "dogm_server_stream_state", "dogm_server_stream_handle", "dogm_server_now_ns",
+    "dogm_get_tune", "dogm_set_tune", "dogm_autotune",
 ]
 
 
@@ -79,6 +80,16 @@ class ServerStats(C.Structure):
     _fields_ = [("frames_submitted", C.c_uint64), ("frames_done", C.c_uint64), ("launches", C.c_uint64),
                 ("streams_active", C.c_int), ("streams_waiting", C.c_int), ("resident_bytes", C.c_size_t),
                 ("budget_bytes", C.c_size_t), ("mean_batch", C.c_double)]
+
+
+class Tune(C.Structure):
+    """dogm_tune: blocks per SM per stage (0 = default), radix low-digit width (0 = default)."""
+    _fields_ = [("blocks_per_sm", C.c_int * 8), ("radix_low_bits", C.c_int), ("ms_tuned", C.c_float),
+                ("ms_default", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {"blocks_per_sm": list(self.blocks_per_sm), "radix_low_bits": self.radix_low_bits,
+                "ms_tuned": round(self.ms_tuned, 4), "ms_default": round(self.ms_default, 4)}
 
 
 SERVE_BATCHED, SERVE_PER_STREAM = 0, 1
@@ -130,6 +141,8 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_server_drain": ([vp, i], i), "dogm_server_get_stats": ([vp, vp], i),
         "dogm_server_stream_state": ([vp, i], i), "dogm_server_stream_handle": ([vp, i, vp], i),
         "dogm_server_now_ns": ([], C.c_int64),
+        "dogm_get_tune": ([vp, vp], i), "dogm_set_tune": ([vp, vp], i),
+        "dogm_autotune": ([vp, vp, i, i, C.c_char_p, vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -303,6 +316,23 @@ class DOGM:
     def stream(self) -> int:
         """The cudaStream_t the handle launches on (record CUDA events on it)."""
         return load().dogm_get_stream(self.h) or 0
+
+    def autotune(self, meas, reps: int = 10, cache_path: str | None = None, device: bool = False) -> Tune:
+        """Times launch widths and the radix split on a scratch handle fed `meas` (host array
+        or int device pointer) and applies the fastest to this handle."""
+        t = Tune()
+        p = C.c_void_p(meas) if isinstance(meas, int) else _ptr(np.ascontiguousarray(meas))
+        check(load().dogm_autotune(self.h, p, 1 if device else 0, reps,
+                                   cache_path.encode() if cache_path else None, C.byref(t)), "dogm_autotune")
+        return t
+
+    def get_tune(self) -> Tune:
+        t = Tune()
+        check(load().dogm_get_tune(self.h, C.byref(t)), "dogm_get_tune")
+        return t
+
+    def set_tune(self, t: Tune) -> None:
+        check(load().dogm_set_tune(self.h, C.byref(t)), "dogm_set_tune")
 
     def profile_enable(self, enable: bool = True) -> None:
         check(load().dogm_profile_enable(self.h, 1 if enable else 0), "dogm_profile_enable")

@@ -130,7 +130,12 @@ struct Batch {
 struct LaunchCfg {
     int num_sms;
     cudaStream_t stream;
+    int mult = 0;  // blocks per SM of this launch (0: the kernel's built-in default)
 };
+// Blocks of a persistent launch: num_sms x the tuned multiplier, or x the default.
+inline int launch_blocks(const LaunchCfg& cfg, int default_mult) {
+    return cfg.num_sms * (cfg.mult > 0 ? cfg.mult : default_mult);
+}
 
 cudaError_t prepare_kernels();  // per device, before the first launch
 cudaError_t prepare_cells();

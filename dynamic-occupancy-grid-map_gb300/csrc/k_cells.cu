@@ -470,12 +470,12 @@ cudaError_t prepare_cells() {
 }
 
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg) {
-    k_cells<<<cfg.num_sms * 2, kCellThreads, sizeof(CellSmem), cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_cells<<<launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg) {
-    k_newborn<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_newborn<<<launch_blocks(cfg, 4), kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 

@@ -311,7 +311,7 @@ cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCf
 }
 
 cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg) {
-    k_predict<<<cfg.num_sms * 4, kPredictThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), stage_mode);
+    k_predict<<<launch_blocks(cfg, 4), kPredictThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), stage_mode);
     return cudaGetLastError();
 }
 

@@ -228,7 +228,7 @@ cudaError_t prepare_kernels() {
 
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg) {
     const int smem = (int)sizeof(ResSmem);
-    k_resample<<<cfg.num_sms * 4, kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_resample<<<launch_blocks(cfg, 4), kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 

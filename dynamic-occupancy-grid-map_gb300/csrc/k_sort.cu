@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ b
 }
 
 cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
-    k_sort_scan<<<cfg.num_sms * 2, kScanWarps * 32, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), pass);
+    k_sort_scan<<<launch_blocks(cfg, 2), kScanWarps * 32, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), pass);
     return cudaGetLastError();
 }
 
@@ -280,9 +280,9 @@ cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cf
     const size_t smem = sizeof(SortSmem);  // 48 KB: no opt-in attribute needed
     Batch* b = const_cast<Batch*>(d_batch);
     if (pass == 0)
-        k_sort_pass<false><<<cfg.num_sms * 4, kThreads, smem, cfg.stream>>>(b);
+        k_sort_pass<false><<<launch_blocks(cfg, 4), kThreads, smem, cfg.stream>>>(b);
     else
-        k_sort_pass<true><<<cfg.num_sms * 4, kThreads, smem, cfg.stream>>>(b);
+        k_sort_pass<true><<<launch_blocks(cfg, 4), kThreads, smem, cfg.stream>>>(b);
     return cudaGetLastError();
 }
 

@@ -59,6 +59,13 @@ struct Ctx {
     std::map<int, cudaGraphExec_t> graphs;
     bool profile = false;
     cudaEvent_t ev[kStages + 1] = {};
+    int mult[kStages] = {};  // tuned blocks per SM per stage (0: the kernel's default)
+
+    // Captured graphs hold the launch widths: drop them when the widths change.
+    void drop_graphs() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+    }
 
     ~Ctx() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
@@ -267,6 +274,7 @@ cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
 #define STAGE(i, call)                                                              \
     do {                                                                            \
         if (prof && (e = cudaEventRecord(c.ev[i], c.stream)) != cudaSuccess) return e; \
+        cfg.mult = c.mult[i];                                                       \
         if ((e = (call)) != cudaSuccess) return e;                                  \
     } while (0)
     // the per-frame counters are reset by predict and the cell pass of the previous frame; a
@@ -940,6 +948,196 @@ int dogm_stage_times(dogm_handle* h, float* ms, int n) {
 }
 
 const char* dogm_stage_name(int i) { return (i >= 0 && i < kStages) ? kStageNames[i] : ""; }
+
+// ---- autotuning ----------------------------------------------------------------------------
+
+static int key_bits_of(const dogm_handle* h) { return std::max(1, bitlen((unsigned long long)(h->C - 1))); }
+
+// Radix split of the cell-key sort: low digit d0 (0: the default, half rounded up), high digit
+// key_bits - d0; both at most kSortMaxBits.  The digit-scan tile counts follow the split.
+static dogm_status apply_split(dogm_handle* h, int d0) {
+    const int kb = key_bits_of(h);
+    if (d0 == 0) d0 = (kb + 1) / 2;
+    const int d1 = kb - d0;
+    if (d0 < 1 || d0 > kSortMaxBits || d1 < 0 || d1 > kSortMaxBits || (d1 == 0 && kb > 1))
+        return fail(DOGM_ERR_INVALID_ARGUMENT, "radix_low_bits " + std::to_string(d0) + " does not split a " +
+                                                   std::to_string(kb) + "-bit cell key into two digits of <= 11 bits");
+    h->desc.d0_bits = d0;
+    h->desc.d1_bits = d1;
+    h->desc.tiles[kStScan0] = div_up(1 << d0, 32);
+    h->desc.tiles[kStScan1] = div_up(1 << d1, 32) + 1;  // + the cell-tile start scan
+    return DOGM_OK;
+}
+
+// ms per update over `reps` graph-launched updates on the resident measurement grid.
+static dogm_status time_updates(dogm_handle* h, int reps, float* ms) {
+    Ctx& c = h->ctx;
+    dogm_status st;
+    for (int i = 0; i < 2; ++i)  // graph capture of both mirrors
+        if ((st = dogm_update(h, nullptr, 0.f, 0.f, 0.f, 0.1f, 0)) != DOGM_OK) return st;
+    DOGM_CUDA(cudaStreamSynchronize(c.stream));
+    DOGM_CUDA(cudaEventRecord(c.ev[0], c.stream));
+    for (int i = 0; i < reps; ++i)
+        if ((st = dogm_update(h, nullptr, 0.f, 0.f, 0.f, 0.1f, 0)) != DOGM_OK) return st;
+    DOGM_CUDA(cudaEventRecord(c.ev[kStages], c.stream));
+    DOGM_CUDA(cudaEventSynchronize(c.ev[kStages]));
+    float t = 0.f;
+    DOGM_CUDA(cudaEventElapsedTime(&t, c.ev[0], c.ev[kStages]));
+    *ms = t / (float)reps;
+    return dogm_synchronize(h);
+}
+
+static std::string tune_key(const dogm_handle* h) {
+    cudaDeviceProp prop;
+    std::string name = cudaGetDeviceProperties(&prop, h->device) == cudaSuccess ? prop.name : "unknown";
+    for (char& ch : name)
+        if (ch == '|' || ch == '\n') ch = '_';
+    return "dogm-tune v1|" + name + "|gs=" + std::to_string(h->gs) + "|N=" + std::to_string(h->N) +
+           "|B=" + std::to_string(h->B);
+}
+
+dogm_status dogm_get_tune(dogm_handle* h, dogm_tune* out) {
+    if (!h || !out) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    for (int i = 0; i < kStages; ++i) out->blocks_per_sm[i] = h->ctx.mult[i];
+    out->radix_low_bits = h->desc.d0_bits == (key_bits_of(h) + 1) / 2 ? 0 : h->desc.d0_bits;
+    return DOGM_OK;
+}
+
+dogm_status dogm_set_tune(dogm_handle* h, const dogm_tune* t) {
+    if (!h || !t) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (int i = 0; i < kStages; ++i)
+        if (t->blocks_per_sm[i] < 0 || t->blocks_per_sm[i] > 32)
+            return fail(DOGM_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 32]");
+    DeviceGuard dg(h->device);
+    dogm_status st = dogm_synchronize(h);  // no frame of the old shape in flight
+    if (st != DOGM_OK) return st;
+    const int d0_old = h->desc.d0_bits;
+    if ((st = apply_split(h, t->radix_low_bits)) != DOGM_OK) {
+        apply_split(h, d0_old);
+        return st;
+    }
+    for (int i = 0; i < kStages; ++i) h->ctx.mult[i] = t->blocks_per_sm[i];
+    h->ctx.drop_graphs();
+    return DOGM_OK;
+}
+
+dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int device, int reps,
+                          const char* cache_path, dogm_tune* out) {
+    if (!h || !meas || !out) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (reps <= 0) reps = 10;
+    reps = std::min(reps, 1000);
+    DeviceGuard dg(h->device);
+    const std::string key = tune_key(h);
+    if (cache_path) {
+        if (FILE* f = std::fopen(cache_path, "r")) {
+            char line[1024];
+            dogm_tune t{};
+            bool found = false;
+            while (std::fgets(line, sizeof(line), f)) {
+                const std::string ln(line);
+                const size_t sep = ln.find(" : ");
+                if (sep == std::string::npos || ln.compare(0, sep, key) != 0) continue;
+                int* m = t.blocks_per_sm;
+                found = std::sscanf(ln.c_str() + sep + 3, "%d %d %d %d %d %d %d %d %d %f %f", &m[0], &m[1], &m[2],
+                                    &m[3], &m[4], &m[5], &m[6], &m[7], &t.radix_low_bits, &t.ms_tuned,
+                                    &t.ms_default) == 11;
+            }
+            std::fclose(f);
+            if (found) {
+                dogm_status st = dogm_set_tune(h, &t);
+                if (st == DOGM_OK) *out = t;
+                return st;
+            }
+        }
+    }
+    // a scratch handle with the same parameters, the measurement grid resident in it
+    dogm_options opt = h->opt;
+    opt.sync_each_update = 0;
+    dogm_handle* s = nullptr;
+    dogm_status st = dogm_create(&h->params, &opt, &s);
+    if (st != DOGM_OK) return st;
+    struct Drop {
+        dogm_handle* s;
+        ~Drop() { dogm_destroy(s); }
+    } drop{s};
+    const size_t mbytes = sizeof(dogm_measurement_cell) * (size_t)s->C;
+    DOGM_CUDA(cudaMemcpy(s->desc.meas_own, meas, mbytes, device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+    for (int i = 0; i < 3; ++i)
+        if ((st = dogm_update(s, nullptr, 0.f, 0.f, 0.f, 0.1f, 0)) != DOGM_OK) return st;
+    float ms_def = 0.f;
+    if ((st = time_updates(s, reps, &ms_def)) != DOGM_OK) return st;
+
+    // 1: radix split, whole-update time
+    const int kb = key_bits_of(s);
+    const int d0_def = (kb + 1) / 2;
+    int best_d0 = d0_def;
+    float best_ms = ms_def;
+    for (int d0 = std::max(1, kb - kSortMaxBits); d0 <= std::min(kSortMaxBits, kb - 1); ++d0) {
+        if (d0 == d0_def) continue;
+        if ((st = apply_split(s, d0)) != DOGM_OK) return st;
+        float ms = 0.f;
+        if ((st = time_updates(s, reps, &ms)) != DOGM_OK) return st;
+        if (ms < 0.99f * best_ms) {
+            best_ms = ms;
+            best_d0 = d0;
+        }
+    }
+    if ((st = apply_split(s, best_d0)) != DOGM_OK) return st;
+
+    // 2: each stage's width, timed by the per-stage events (plain launches)
+    static const int kCand[] = {1, 2, 3, 4, 6, 8};
+    int best_mult[kStages] = {};
+    s->ctx.profile = true;
+    for (int stage = 0; stage < kStages; ++stage) {
+        float best = 0.f;
+        int bm = 0;
+        for (int ci = -1; ci < (int)(sizeof(kCand) / sizeof(kCand[0])); ++ci) {
+            const int m = ci < 0 ? 0 : kCand[ci];
+            s->ctx.mult[stage] = m;
+            float acc = 0.f;
+            for (int r = 0; r < reps; ++r) {
+                if ((st = dogm_update(s, nullptr, 0.f, 0.f, 0.f, 0.1f, 0)) != DOGM_OK) return st;
+                if ((st = dogm_synchronize(s)) != DOGM_OK) return st;
+                float ms[kStages];
+                dogm_stage_times(s, ms, kStages);
+                acc += ms[stage];
+            }
+            const float mean = acc / (float)reps;
+            if (ci < 0 || mean < 0.98f * best) {  // a width other than the default must win by 2 %
+                best = mean;
+                bm = m;
+            }
+        }
+        s->ctx.mult[stage] = bm;
+        best_mult[stage] = bm;
+    }
+    s->ctx.profile = false;
+    s->ctx.drop_graphs();
+    float ms_tuned = 0.f;
+    if ((st = time_updates(s, reps, &ms_tuned)) != DOGM_OK) return st;
+
+    dogm_tune t{};
+    if (ms_tuned < 0.995f * ms_def) {
+        for (int i = 0; i < kStages; ++i) t.blocks_per_sm[i] = best_mult[i];
+        t.radix_low_bits = best_d0 == d0_def ? 0 : best_d0;
+        t.ms_tuned = ms_tuned;
+    } else {
+        t.ms_tuned = ms_def;  // nothing beat the defaults
+    }
+    t.ms_default = ms_def;
+    if ((st = dogm_set_tune(h, &t)) != DOGM_OK) return st;
+    if (cache_path) {
+        if (FILE* f = std::fopen(cache_path, "a")) {
+            const int* m = t.blocks_per_sm;
+            std::fprintf(f, "%s : %d %d %d %d %d %d %d %d %d %.5f %.5f\n", key.c_str(), m[0], m[1], m[2], m[3], m[4],
+                         m[5], m[6], m[7], t.radix_low_bits, t.ms_tuned, t.ms_default);
+            std::fclose(f);
+        }
+    }
+    *out = t;
+    return DOGM_OK;
+}
 
 // ---- utilities ---------------------------------------------------------------------------
 
