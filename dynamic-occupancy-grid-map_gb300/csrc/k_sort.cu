@@ -229,7 +229,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ b
         }
         __syncthreads();
 
-        // scatter to the global sorted position; pass 0 also counts the pass-1 histogram
+        // scatter to the global sorted position; pass 0 also counts the pass-1 histogram.
+        // The final pass's arrays do not overlap: restrict lets the compiler issue the index
+        // loads and state gathers of several items before their stores.
+        const uint32_t* __restrict__ t_idx = g.T_idx;
+        const float4* __restrict__ p_state = g.P_state;
+        float4* __restrict__ s_state = g.S_state;
+        uint32_t* __restrict__ s_key = g.S_key;
         uint32_t* H1 = g.hsort + (size_t)g.sort_tiles * kSortMaxBins;
         const int shift1 = g.d0_bits;
         const uint32_t nb1m = (1u << g.d1_bits) - 1u;
@@ -248,9 +254,9 @@ __global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ b
             }
             if (FINAL) {
                 if (out != 0xffffffffu) {
-                    const uint32_t src = g.T_idx[pos];  // particle index carried by pass 0
-                    g.S_key[out] = key[k];
-                    g.S_state[out] = g.P_state[src];
+                    const uint32_t src = t_idx[pos];  // particle index carried by pass 0
+                    s_key[out] = key[k];
+                    s_state[out] = __ldg(p_state + src);
                     if (g.dbg_perm) g.dbg_perm[out] = (int)src;
                 }
             } else {
