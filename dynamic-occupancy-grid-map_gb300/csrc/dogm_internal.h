@@ -72,6 +72,7 @@ struct GridDesc {
     int d0_bits, d1_bits;   // radix digit widths (d0 low digit)
     int q_shift;            // fixed point: weight w -> round(w * 2^q_shift)
     int pad0;
+    unsigned long long gs_div;  // floor(2^42 / gs) + 1: k / gs == (k * gs_div) >> 42 for k < 2^22
     // filter parameters
     float p_S, sigma_pos, sigma_vel, p_B, sigma_birth, init_max_vel;
     // per-frame parameters
@@ -113,6 +114,12 @@ struct GridDesc {
     int sort_tiles;
     int pad1;
 };
+
+// Row of cell k: exact for k < 2^22 and gs <= 2048 (the error k * e / 2^42 < 2^-20 stays below
+// the 1 / gs margin of floor(k / gs)).
+__host__ __device__ __forceinline__ int cell_row(const GridDesc& g, int k) {
+    return (int)(((unsigned long long)k * g.gs_div) >> 42);
+}
 
 constexpr int kMaxBatch = 256;
 

@@ -95,7 +95,8 @@ struct CellSmem {
     // per warp: its 32 cell records (2 KB), staged so that the warp stores them as 512
     // contiguous bytes per instruction instead of four 16-byte pieces at 64-byte stride
     float4 stage[kCellThreads / 32][32 * 4];
-    Run wagg[kCellThreads / 32];
+    Run wagg[kCellThreads / 32];  // each warp's run, then (wpre) the runs before each warp
+    Run wpre[kCellThreads / 32];
     unsigned long long red[kCellThreads / 32], red2[kCellThreads / 32];
     int tile;
 };
@@ -187,7 +188,8 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             }
             int src = k;
             if (g.shifted) {
-                const int sx = k % g.gs + g.shift_x, sy = k / g.gs + g.shift_y;
+                const int row = cell_row(g, k);
+                const int sx = k - row * g.gs + g.shift_x, sy = row + g.shift_y;
                 const bool ok = sx > 0 && sx < g.gs && sy > 0 && sy < g.gs;  // strict, as the reference
                 src = ok ? sx + g.gs * sy : -1;
             }
@@ -265,8 +267,20 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             if (lane == 31) sm.wagg[warp] = inc;
             Run excl = run_shfl_up(inc, 1);
             __syncthreads();
-            Run pre = run_empty(0u);
-            for (int w = 0; w < warp; ++w) pre = run_combine(pre, sm.wagg[w]);
+            if (warp == 0) {  // exclusive scan of the warps' runs by one warp
+                constexpr int kWarps = kCellThreads / 32;
+                Run a = lane < kWarps ? sm.wagg[lane] : run_empty(0u);
+#pragma unroll
+                for (int o = 1; o < kWarps; o <<= 1) {
+                    const Run other = run_shfl_up(a, o);
+                    if (lane >= o) a = run_combine(other, a);
+                }
+                Run ex = run_shfl_up(a, 1);
+                if (lane == 0) ex = run_empty(0u);
+                if (lane < kWarps) sm.wpre[lane] = ex;
+            }
+            __syncthreads();
+            Run pre = sm.wpre[warp];
             if (lane > 0) pre = run_combine(pre, excl);
             if (first_last >= 0) put_cell(sm, g, first_cell - (uint32_t)base, first_last, run_combine(pre, first));
             __syncthreads();

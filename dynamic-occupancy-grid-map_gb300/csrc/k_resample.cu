@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_resample(Batch* __restrict__ bt
                     const U4 rr = draw_block(g, (uint32_t)b, g.frame, kDrawBirth);
                     z = box_muller(rr.x, rr.y);
                 }
-                st.x = __fadd_rn((float)(k % gs), 0.5f);
+                st.x = __fadd_rn((float)(k - cell_row(g, k) * gs), 0.5f);
                 st.y = __fadd_rn(__fdiv_rn((float)k, (float)gs), 0.5f);  // float division, as the reference
                 st.z = __fmaf_rn(z.x, g.sigma_birth, 0.0f);
                 st.w = __fmaf_rn(z.y, g.sigma_birth, 0.0f);

@@ -477,6 +477,7 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     g.d0_bits = (s.key_bits + 1) / 2;
     g.d1_bits = s.key_bits - g.d0_bits;
     g.q_shift = 61 - bitlen((unsigned long long)s.C);
+    g.gs_div = (1ull << 42) / (unsigned long long)s.gs + 1ull;
     g.p_S = params->persistence_prob;
     g.sigma_pos = params->stddev_process_noise_position;
     g.sigma_vel = params->stddev_process_noise_velocity;
