@@ -424,10 +424,14 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
         const float sc = T ? __fdiv_rn((float)g.B, __ull2float_rn(T)) : 0.0f;
         int bnd[kCellIpt + 1];
         bnd[0] = alloc_boundary_fast(acc, T, g.B, sc);
+        // boundaries are monotone in the prefix: when the thread's first and last agree, so do
+        // the ones between (most threads' cells get no newborn at all)
+        const int b_last = alloc_boundary_fast(acc + v, T, g.B, sc);  // v: the thread's q sum
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
             acc += q[j];
-            bnd[j + 1] = q[j] ? alloc_boundary_fast(acc, T, g.B, sc) : bnd[j];
+            if (j + 1 == kCellIpt) bnd[j + 1] = b_last;
+            else bnd[j + 1] = (b_last == bnd[0] || !q[j]) ? bnd[j] : alloc_boundary_fast(acc, T, g.B, sc);
             s_bnd[threadIdx.x * kCellIpt + j] = bnd[j];
         }
         if (threadIdx.x == kThreads - 1) s_bnd[kCellTile] = bnd[kCellIpt];
@@ -458,11 +462,14 @@ __global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
         }
 #pragma unroll
         for (int i = 0; i < kRunTiles; ++i) {
+            if (!__any_sync(0xffffffffu, racc[i] != 0ull)) continue;  // warp-uniform
             const unsigned long long s = warp_sum_u64(racc[i]);
             if (lane == 0 && s) atomicAdd(&g.res_sum[rt0 + i], s);
         }
-        jq = warp_sum_u64(jq);
-        if (lane == 0 && jq) atomicAdd(&g.fs->joint_total, jq);
+        if (__any_sync(0xffffffffu, jq != 0ull)) {
+            jq = warp_sum_u64(jq);
+            if (lane == 0 && jq) atomicAdd(&g.fs->joint_total, jq);
+        }
         __syncthreads();  // every s_nuA entry is written
         // key word of every newborn slot of the tile (cell | associated bit), slot by slot on
         // consecutive threads; the owner cell is the last c with s_bnd[c] <= slot
