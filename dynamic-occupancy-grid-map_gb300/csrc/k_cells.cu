@@ -389,7 +389,7 @@ __device__ __forceinline__ void add_joint_range(unsigned long long (&racc)[kRunT
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_newborn(Batch* __restrict__ bt) {
+__global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt) {
     __shared__ unsigned long long red[2 * (kThreads / 32)];
     __shared__ int s_bnd[kCellTile + 1];  // s_bnd[c]: first slot of cell c of the tile; [kCellTile]: end
     __shared__ int s_nuA[kCellTile];
@@ -496,7 +496,7 @@ cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg) {
 }
 
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg) {
-    k_newborn<<<launch_blocks(cfg, 4), kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
+    k_newborn<<<launch_blocks(cfg, 6), kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
     return cudaGetLastError();
 }
 
