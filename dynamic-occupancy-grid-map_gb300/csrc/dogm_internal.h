@@ -24,7 +24,7 @@ constexpr int kSegIpt = 4;           // sorted particles per thread in a chunk o
 constexpr int kSegTile = kThreads * kSegIpt;
 constexpr int kCellIpt = 4;          // cells per thread in the cell passes
 constexpr int kCellTile = kThreads * kCellIpt;
-constexpr int kResIpt = 8;           // joint particles per thread in resampling
+constexpr int kResIpt = 4;           // joint particles per thread in resampling
 constexpr int kResTile = kThreads * kResIpt;
 
 static_assert(kPredictTile == kSortTile, "predict writes the pass-0 digit counts of the sort tiles");

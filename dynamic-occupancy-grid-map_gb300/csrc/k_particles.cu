@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
 constexpr int kPredictThreads = 512;
 static_assert(kPredictTile % kPredictThreads == 0, "whole particles per thread");
 
-__global__ void __launch_bounds__(kPredictThreads) k_predict(Batch* __restrict__ bt, int mode) {
+__global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restrict__ bt, int mode) {
     __shared__ uint32_t h0[kSortMaxBins];
     __shared__ uint32_t h1[kSortMaxBins];
     __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (ranges of the cell pass)
