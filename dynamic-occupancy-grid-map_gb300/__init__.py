@@ -48,6 +48,8 @@ ABI_SYMBOLS = [
     "dogm_server_close_stream", "dogm_server_submit", "dogm_server_pause", "dogm_server_poll", "dogm_server_drain",
     "dogm_server_get_stats", "dogm_server_stream_state", "dogm_server_stream_handle", "dogm_server_now_ns",
     "dogm_get_tune", "dogm_set_tune", "dogm_autotune",
+    "dogm_meas_grid_create", "dogm_meas_grid_destroy", "dogm_meas_grid_generate", "dogm_meas_grid_size",
+    "dogm_meas_grid_polar", "dogm_meas_grid_fan",
 ]
 
 
@@ -143,6 +145,9 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_server_now_ns": ([], C.c_int64),
         "dogm_get_tune": ([vp, vp], i), "dogm_set_tune": ([vp, vp], i),
         "dogm_autotune": ([vp, vp, i, i, C.c_char_p, vp], i),
+        "dogm_meas_grid_create": ([vp, f, f, i, vp], i), "dogm_meas_grid_destroy": ([vp], i),
+        "dogm_meas_grid_generate": ([vp, vp, i, i, vp, vp], i), "dogm_meas_grid_size": ([vp], i),
+        "dogm_meas_grid_polar": ([vp, vp, sz, vp, vp], i), "dogm_meas_grid_fan": ([vp, vp, vp, vp, i, vp, vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -572,3 +577,70 @@ class Server:
 
 def now_ns() -> int:
     return int(load().dogm_server_now_ns())
+
+
+class LaserParams(C.Structure):
+    """LaserMeasurementGrid::Params (laser_to_meas_grid.h:16-22)."""
+    _fields_ = [("max_range", C.c_float), ("resolution", C.c_float), ("fov", C.c_float), ("stddev_range", C.c_float)]
+
+
+class MeasurementGridGenerator:
+    """Lidar scan -> measurement grid on the GPU (dogm_meas_grid_*): the inverse sensor model in
+    polar coordinates and the warp over the field of view, replacing the OpenGL path of the
+    reference's LaserMeasurementGrid (laser_to_meas_grid.cu:25-70)."""
+
+    def __init__(self, max_range: float, resolution: float, fov: float, stddev_range: float, grid_length: float,
+                 grid_resolution: float, beams: int):
+        self.params = LaserParams(max_range, resolution, fov, stddev_range)
+        self.beams = int(beams)
+        m = C.c_void_p()
+        check(load().dogm_meas_grid_create(C.byref(self.params), grid_length, grid_resolution, self.beams,
+                                           C.byref(m)), "dogm_meas_grid_create")
+        self.m = m
+        self.grid_size = load().dogm_meas_grid_size(m)
+        self.cell_count = self.grid_size ** 2
+        self._out = DeviceBuffer(16 * self.cell_count)
+
+    def close(self) -> None:
+        if self.m:
+            load().dogm_meas_grid_destroy(self.m)
+            self.m = None
+            self._out.free()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def generate_device(self, ranges, out_ptr: int | None = None, fuse: bool = False, device: bool = False) -> int:
+        """Writes the grid to device memory (out_ptr, or an internal buffer); returns the pointer."""
+        out = self._out.ptr if out_ptr is None else out_ptr
+        r = C.c_void_p(ranges) if isinstance(ranges, int) else _ptr(np.ascontiguousarray(ranges, np.float32))
+        check(load().dogm_meas_grid_generate(self.m, r, 1 if device else 0, 1 if fuse else 0, C.c_void_p(out), None),
+              "dogm_meas_grid_generate")
+        return out
+
+    def generate(self, ranges, fuse: bool = False) -> np.ndarray:
+        """The measurement grid of one scan (host ranges) as a MEAS_DTYPE host array."""
+        ptr = self.generate_device(ranges, fuse=fuse)
+        out = np.empty(self.cell_count, MEAS_DTYPE)
+        check(load().dogm_memcpy(_ptr(out), C.c_void_p(ptr), out.nbytes, 2), "dogm_memcpy D2H")
+        return out
+
+    def polar(self) -> np.ndarray:
+        nb, nr = C.c_int(0), C.c_int(0)
+        check(load().dogm_meas_grid_polar(self.m, None, 0, C.byref(nb), C.byref(nr)), "dogm_meas_grid_polar")
+        out = np.empty((nr.value, nb.value, 2), np.float32)
+        check(load().dogm_meas_grid_polar(self.m, _ptr(out), out.size, None, None), "dogm_meas_grid_polar")
+        return out
+
+    def fan(self) -> dict:
+        nv, a0 = C.c_int(0), C.c_int(0)
+        check(load().dogm_meas_grid_fan(self.m, None, None, None, 0, C.byref(nv), C.byref(a0)), "dogm_meas_grid_fan")
+        x = np.empty(nv.value, np.int64)
+        y = np.empty(nv.value, np.int64)
+        sv = np.empty(nv.value, np.float32)
+        check(load().dogm_meas_grid_fan(self.m, _ptr(x), _ptr(y), _ptr(sv), nv.value, None, None),
+              "dogm_meas_grid_fan")
+        return {"x256": x, "y256": y, "s": sv, "first_angle": a0.value}

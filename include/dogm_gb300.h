@@ -342,6 +342,51 @@ dogm_status dogm_server_stream_handle(dogm_server* s, int stream_id, dogm_handle
 /* The clock of dogm_server_result (monotonic, nanoseconds). */
 int64_t dogm_server_now_ns(void);
 
+/* ---- measurement-grid generation from a lidar scan --------------------------------------
+ *
+ * Replaces the demo's LaserMeasurementGrid (dogm/demo/simulator/include/mapping/
+ * laser_to_meas_grid.h:13-35), which needs OpenGL for its polar -> cartesian step: here the
+ * inverse sensor model (kernel/measurement_grid.cu:33-89) and the warp over the sensor's
+ * field of view (opengl/renderer.cpp:11-31, shader.cpp:22-35) are CUDA kernels.  The sensor
+ * sits at the centre of the grid's last row and looks towards row 0; beam 0 points
+ * 90 + fov/2 degrees from the x axis and the last beam 90 - fov/2 (the texture's u runs
+ * against the fan's angle).  Differences from the OpenGL path: the polar grid is sampled with
+ * level-0 bilinear filtering (no mipmaps, no anisotropy: those depend on the graphics driver)
+ * and coverage uses exact edge functions on vertices snapped to 1/256 pixel. */
+
+/* LaserMeasurementGrid::Params (laser_to_meas_grid.h:16-22). */
+typedef struct dogm_laser_params {
+    float max_range;    /* [m]; polar range bins = int(max_range / resolution)            */
+    float resolution;   /* range-bin length [m]                                           */
+    float fov;          /* field of view [degrees]                                        */
+    float stddev_range; /* range noise of the inverse sensor model [m]                    */
+} dogm_laser_params;
+
+typedef struct dogm_meas_grid dogm_meas_grid;
+
+/* LaserMeasurementGrid(params, grid_length, resolution) (laser_to_meas_grid.cu:10-18) for
+ * scans of `beams` ranges; grid_size = int(grid_length / grid_resolution). */
+dogm_status dogm_meas_grid_create(const dogm_laser_params* p, float grid_length, float grid_resolution, int beams,
+                                  dogm_meas_grid** out);
+dogm_status dogm_meas_grid_destroy(dogm_meas_grid* m);
+
+/* LaserMeasurementGrid::generateGrid (laser_to_meas_grid.cu:25-70): ranges[beams] in metres
+ * (host, or device with device != 0; non-finite = no return) -> grid_size^2 measurement cells
+ * written to out_device, a device buffer (then dogm_update(h, out_device, ..., 1)).  fuse != 0
+ * combines this scan into the previous polar grid by Dempster's rule instead of replacing it
+ * (fusePolarGridTextureKernel, measurement_grid.cu:91-113).  Runs on `stream`
+ * (a cudaStream_t, 0 = legacy default) and returns when the grid is written. */
+dogm_status dogm_meas_grid_generate(dogm_meas_grid* m, const float* ranges, int device, int fuse,
+                                    dogm_measurement_cell* out_device, void* stream);
+int dogm_meas_grid_size(const dogm_meas_grid* m);
+
+/* Debug exports: the polar grid (bins x beams float pairs {occ, free}, row = range bin) and the
+ * fan (apex, then one vertex per degree: window coordinates x 256 and texture s; the first arc
+ * vertex's angle in degrees). */
+dogm_status dogm_meas_grid_polar(dogm_meas_grid* m, float* host_out, size_t n, int* beams, int* bins);
+dogm_status dogm_meas_grid_fan(dogm_meas_grid* m, long long* x256, long long* y256, float* s, int n, int* nv,
+                               int* first_angle);
+
 /* ---- measurement ---------------------------------------------------------------------- */
 
 /* The cudaStream_t (as void*) the handle launches on: record CUDA events on it to time updates. */

@@ -1,0 +1,104 @@
+"""GPU: measurement-grid generation (dogm_meas_grid_*) against its CPU restatement
+(oracle/pymeas.py).  Tolerances stated here:
+  * fan vertices: within 1/256 pixel of the reference formula (renderer.cpp:11-31; cos and sin
+    in float may differ by an ulp between libraries), texture s exact;
+  * polar inverse sensor model: within 2e-6 of numpy float32 (exp differs by a few ulp; a
+    range bin whose occupancy sits exactly at a branch threshold may take the other branch:
+    at most 1e-3 of the entries);
+  * the warp, fed the GPU's own polar grid: bit-exact.
+The sensor geometry is checked on a scan with one return straight ahead."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+DEMO = dict(max_range=50.0, resolution=0.2, fov=120.0, stddev_range=0.5, grid_length=50.0, grid_resolution=0.2,
+            beams=100)  # dogm/demo/main.cpp:35-44
+
+
+@pytest.fixture(scope="module")
+def pymeas():
+    import pymeas as mod
+    return mod
+
+
+def _scan(beams, seed, max_range=50.0):
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(2.0, max_range * 0.9, beams).astype(np.float32)
+    r[rng.random(beams) < 0.2] = np.inf  # no return
+    return r
+
+
+@pytest.mark.parametrize("cfg", [DEMO, dict(max_range=60.0, resolution=0.1, fov=90.0, stddev_range=0.3,
+                                            grid_length=51.2, grid_resolution=0.1, beams=733)])
+def test_ism_and_warp_against_restatement(dogm, pymeas, cfg):
+    g = dogm.MeasurementGridGenerator(**cfg)
+    gs = g.grid_size
+    fan = g.fan()
+    ref_fan = pymeas.fan_vertices(cfg["max_range"], cfg["fov"], cfg["grid_length"], gs)
+    assert fan["first_angle"] == ref_fan["first_angle"]
+    assert np.array_equal(fan["s"], ref_fan["s"])
+    assert np.abs(fan["x256"] - ref_fan["x256"]).max() <= 1 and np.abs(fan["y256"] - ref_fan["y256"]).max() <= 1
+    for k in range(3):
+        ranges = _scan(cfg["beams"], seed=k, max_range=cfg["max_range"])
+        out = g.generate(ranges)
+        polar = g.polar()
+        bins = int(np.float32(cfg["max_range"]) / np.float32(cfg["resolution"]))
+        exp_polar = pymeas.polar_ism(ranges, bins, cfg["resolution"], cfg["stddev_range"])
+        err = np.abs(polar.astype(np.float64) - exp_polar)
+        assert np.mean(err > 2e-6) <= 1e-3, "inverse sensor model"
+        cells = out.view(np.float32).reshape(-1, 4)
+        assert np.array_equal(cells.view(np.uint32), pymeas.warp(polar, gs, fan).view(np.uint32)), "warp"
+    g.close()
+
+
+def test_fuse_second_scan(dogm, pymeas):
+    g = dogm.MeasurementGridGenerator(**DEMO)
+    g.generate(_scan(DEMO["beams"], 7))
+    first = g.polar()
+    r2 = _scan(DEMO["beams"], 8)
+    g.generate(r2, fuse=True)
+    fused = g.polar()
+    bins = first.shape[0]
+    exp = pymeas.combine(first, pymeas.polar_ism(r2, bins, DEMO["resolution"], DEMO["stddev_range"]))
+    assert np.mean(np.abs(fused.astype(np.float64) - exp) > 4e-6) <= 1e-3
+    g.close()
+
+
+def test_geometry_one_return_straight_ahead(dogm):
+    g = dogm.MeasurementGridGenerator(**DEMO)
+    gs = g.grid_size
+    beams = DEMO["beams"]
+    ranges = np.full(beams, np.inf, np.float32)
+    # u = 1 - s / t runs from the left edge of the fan (u=0) to the right (u=1): the middle
+    # beams look straight ahead (+y, towards row 0)
+    ranges[beams // 2 - 1: beams // 2 + 1] = 20.0
+    cells = g.generate(ranges)
+    occ = cells["occ_mass"].reshape(gs, gs)
+    free = cells["free_mass"].reshape(gs, gs)
+    row, col = np.unravel_index(np.argmax(occ), occ.shape)
+    dist = (gs - 1 - row + 0.5) * DEMO["grid_resolution"]
+    assert abs(col - gs // 2) <= 1, "the return lies straight ahead of the sensor"
+    assert abs(dist - 20.0) <= 1.0, "at its range (%.2f m)" % dist
+    assert occ.max() > 0.5
+    # outside the 120-degree fan (beside the sensor, low rows) there is no evidence at all
+    assert occ[gs - 2, 0] == 0 and free[gs - 2, 0] == 0
+    assert free[gs - 30, gs // 2] > 0.4, "free space before the return"
+    g.close()
+
+
+def test_generated_grid_feeds_the_update(dogm):
+    g = dogm.MeasurementGridGenerator(**DEMO)
+    p = dogm.make_params(size=DEMO["grid_length"], resolution=DEMO["grid_resolution"], particle_count=200000,
+                         new_born_particle_count=20000)
+    h = dogm.DOGM(p, seed=3)
+    assert h.grid_size == g.grid_size
+    for k in range(3):
+        ptr = g.generate_device(_scan(DEMO["beams"], 20 + k))
+        h.update_grid(ptr, 0.0, 0.0, 0.0, 0.1, device=True)
+    cells = h.get_grid_cells()
+    assert np.isfinite(cells["occ_mass"]).all() and cells["occ_mass"].max() > 0.3
+    h.close()
+    g.close()
