@@ -27,6 +27,9 @@ GRID_CELL_DTYPE = np.dtype([
     ("var_y_vel", "<f4"), ("covar_xy_vel", "<f4")])
 MEAS_DTYPE = np.dtype([("free_mass", "<f4"), ("occ_mass", "<f4"), ("likelihood", "<f4"), ("p_A", "<f4")])
 GRID_CELL_FIELDS = GRID_CELL_DTYPE.names
+# dogm_dynamic_cell: a kept cell of dogm_extract_dynamic_cells
+DYNAMIC_CELL_DTYPE = np.dtype([("index", "<i4"), ("x", "<f4"), ("y", "<f4"), ("occupancy", "<f4"),
+                               ("mahalanobis", "<f4"), ("cell", GRID_CELL_DTYPE)])
 
 DOGM_OK = 0
 STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA error", 4: "device wait timed out",
@@ -49,7 +52,7 @@ ABI_SYMBOLS = [
     "dogm_server_get_stats", "dogm_server_stream_state", "dogm_server_stream_handle", "dogm_server_now_ns",
     "dogm_get_tune", "dogm_set_tune", "dogm_autotune",
     "dogm_meas_grid_create", "dogm_meas_grid_destroy", "dogm_meas_grid_generate", "dogm_meas_grid_size",
-    "dogm_meas_grid_polar", "dogm_meas_grid_fan",
+    "dogm_meas_grid_polar", "dogm_meas_grid_fan", "dogm_extract_dynamic_cells", "dogm_extract_dynamic_cells_device",
 ]
 
 
@@ -148,6 +151,8 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_meas_grid_create": ([vp, f, f, i, vp], i), "dogm_meas_grid_destroy": ([vp], i),
         "dogm_meas_grid_generate": ([vp, vp, i, i, vp, vp], i), "dogm_meas_grid_size": ([vp], i),
         "dogm_meas_grid_polar": ([vp, vp, sz, vp, vp], i), "dogm_meas_grid_fan": ([vp, vp, vp, vp, i, vp, vp], i),
+        "dogm_extract_dynamic_cells": ([vp, f, f, vp, i, vp], i),
+        "dogm_extract_dynamic_cells_device": ([vp, i, f, f, vp, i, vp, vp, vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -321,6 +326,16 @@ class DOGM:
     def stream(self) -> int:
         """The cudaStream_t the handle launches on (record CUDA events on it)."""
         return load().dogm_get_stream(self.h) or 0
+
+    def extract_dynamic_cells(self, min_occupancy: float = 0.7, min_velocity: float = 4.0,
+                              max_out: int = 1 << 16) -> np.ndarray:
+        """Cells whose pignistic occupancy and velocity Mahalanobis length reach the thresholds
+        (computeCellsWithVelocity, image_creation.cpp:24-66), in row-major order."""
+        out = np.empty(max(max_out, 1), DYNAMIC_CELL_DTYPE)
+        n = C.c_int(0)
+        check(load().dogm_extract_dynamic_cells(self.h, min_occupancy, min_velocity, _ptr(out), max_out, C.byref(n)),
+              "dogm_extract_dynamic_cells")
+        return out[:min(n.value, max_out)]
 
     def autotune(self, meas, reps: int = 10, cache_path: str | None = None, device: bool = False) -> Tune:
         """Times launch widths and the radix split on a scratch handle fed `meas` (host array

@@ -130,6 +130,10 @@ struct dogm_handle {
     float2* rp_birth = nullptr;
     unsigned long long* rp_resample = nullptr;
     bool debug = false;
+    // dynamic-cell extraction staging (allocated on first use)
+    dogm_dynamic_cell* dyn_out = nullptr;
+    int dyn_cap = 0;
+    unsigned int* dyn_scratch = nullptr;
 };
 
 namespace {
@@ -535,7 +539,8 @@ dogm_status dogm_destroy(dogm_handle* h) {
     DeviceGuard dg(h->device);
     cudaDeviceSynchronize();
     for (void* p : h->allocations) cudaFree(p);
-    for (void* p : {(void*)h->rp_init, (void*)h->rp_predict, (void*)h->rp_birth, (void*)h->rp_resample})
+    for (void* p : {(void*)h->rp_init, (void*)h->rp_predict, (void*)h->rp_birth, (void*)h->rp_resample,
+                    (void*)h->dyn_out, (void*)h->dyn_scratch})
         if (p) cudaFree(p);
     delete h;
     return DOGM_OK;
@@ -949,6 +954,33 @@ int dogm_stage_times(dogm_handle* h, float* ms, int n) {
 }
 
 const char* dogm_stage_name(int i) { return (i >= 0 && i < kStages) ? kStageNames[i] : ""; }
+
+dogm_status dogm_extract_dynamic_cells(dogm_handle* h, float min_occupancy, float min_velocity,
+                                       dogm_dynamic_cell* host_out, int max_out, int* n_found) {
+    if (!h || !n_found || max_out < 0 || (max_out > 0 && !host_out))
+        return fail(DOGM_ERR_INVALID_ARGUMENT, "bad dynamic-cell extraction arguments");
+    DeviceGuard dg(h->device);
+    Ctx& c = h->ctx;
+    if (!h->dyn_scratch) DOGM_CUDA(cudaMalloc(&h->dyn_scratch, sizeof(unsigned int) * (size_t)div_up(h->C, 1024)));
+    if (max_out > h->dyn_cap) {
+        if (h->dyn_out) cudaFree(h->dyn_out);
+        h->dyn_out = nullptr;
+        h->dyn_cap = 0;
+        DOGM_CUDA(cudaMalloc(&h->dyn_out, sizeof(dogm_dynamic_cell) * (size_t)max_out));
+        h->dyn_cap = max_out;
+    }
+    dogm_dynamic_cell* out = h->dyn_out ? h->dyn_out : reinterpret_cast<dogm_dynamic_cell*>(h->dyn_scratch);
+    dogm_status st = dogm_extract_dynamic_cells_device(h->desc.cells, h->gs, min_occupancy, min_velocity, out, max_out,
+                                                       h->dyn_scratch, n_found, (void*)c.stream);
+    if (st != DOGM_OK) return st;
+    const int n = std::min(*n_found, max_out);
+    if (n > 0) {
+        DOGM_CUDA(cudaMemcpyAsync(host_out, h->dyn_out, sizeof(dogm_dynamic_cell) * (size_t)n, cudaMemcpyDeviceToHost,
+                                  c.stream));
+        DOGM_CUDA(cudaStreamSynchronize(c.stream));
+    }
+    return DOGM_OK;
+}
 
 // ---- autotuning ----------------------------------------------------------------------------
 

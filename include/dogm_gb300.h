@@ -342,6 +342,34 @@ dogm_status dogm_server_stream_handle(dogm_server* s, int stream_id, dogm_handle
 /* The clock of dogm_server_result (monotonic, nanoseconds). */
 int64_t dogm_server_now_ns(void);
 
+/* ---- dynamic-cell extraction -------------------------------------------------------------
+ *
+ * Replaces the demo's host-side computeCellsWithVelocity (dogm/demo/utils/image_creation.cpp:
+ * 19-66), which copies the whole grid back and filters it on the CPU: here the filter runs on
+ * the GPU and only the kept cells cross to the host.  A cell is kept when its pignistic
+ * occupancy occ + (1 - occ - free) / 2 >= min_occupancy and the Mahalanobis length of its mean
+ * velocity, v^T Sigma^-1 v with Sigma = [[var_x, cov], [cov, var_y]], >= min_velocity (0 for a
+ * singular Sigma).  Cells come in row-major order, as the reference's loops visit them. */
+typedef struct dogm_dynamic_cell {
+    int index;          /* y * grid_size + x                                              */
+    float x, y;         /* column and row of the cell (image_creation.cpp:53-54)          */
+    float occupancy;    /* pignistic occupancy                                            */
+    float mahalanobis;  /* v^T Sigma^-1 v                                                 */
+    dogm_grid_cell cell;
+} dogm_dynamic_cell;
+
+/* Extracts from the handle's current grid into host_out (up to max_out cells, the first in
+ * row-major order); *n_found receives how many cells pass, which may exceed max_out.  The
+ * handle keeps a device staging buffer of max_out cells (allocated on first use or growth). */
+dogm_status dogm_extract_dynamic_cells(dogm_handle* h, float min_occupancy, float min_velocity,
+                                       dogm_dynamic_cell* host_out, int max_out, int* n_found);
+
+/* The same over any grid in device memory: cells (grid_size^2), out (device, max_out entries),
+ * scratch (device, ceil(grid_size^2 / 1024) words); runs on `stream` and returns when done. */
+dogm_status dogm_extract_dynamic_cells_device(const dogm_grid_cell* cells, int grid_size, float min_occupancy,
+                                              float min_velocity, dogm_dynamic_cell* out, int max_out,
+                                              unsigned int* scratch, int* n_found, void* stream);
+
 /* ---- measurement-grid generation from a lidar scan --------------------------------------
  *
  * Replaces the demo's LaserMeasurementGrid (dogm/demo/simulator/include/mapping/

@@ -140,3 +140,21 @@ def warp(polar: np.ndarray, gs: int, fan: dict) -> np.ndarray:
     out[:, 2] = 1
     out[:, 3] = 1
     return out
+
+
+def dynamic_cells(cells: np.ndarray, gs: int, min_occ: float, min_vel: float) -> dict:
+    """computeCellsWithVelocity (dogm/demo/utils/image_creation.cpp:24-66) in the GPU's FP32
+    order: pignistic occupancy, v^T Sigma^-1 v by the closed-form 2 x 2 inverse (0 when
+    singular), kept cells in row-major order."""
+    occ_m, free_m = cells["occ_mass"].astype(F), cells["free_mass"].astype(F)
+    occ = occ_m + F(0.5) * ((F(1) - occ_m) - free_m)
+    vx, vy, c = cells["var_x_vel"].astype(F), cells["var_y_vel"].astype(F), cells["covar_xy_vel"].astype(F)
+    mx, my = cells["mean_x_vel"].astype(F), cells["mean_y_vel"].astype(F)
+    det = vx * vy - c * c
+    q = (vy * (mx * mx) - F(2) * (c * (mx * my))) + vx * (my * my)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        m = np.where(det != 0, q / np.where(det != 0, det, F(1)), F(0)).astype(F)
+    keep = (occ >= F(min_occ)) & (m >= F(min_vel))
+    idx = np.flatnonzero(keep)
+    return {"index": idx.astype(np.int32), "occupancy": occ[idx], "mahalanobis": m[idx],
+            "x": (idx % gs).astype(F), "y": (idx // gs).astype(F)}
