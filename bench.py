@@ -439,21 +439,12 @@ def run_serving(dogm, scene, n_streams: int = 200, rate_hz: float = 10.0, second
             frame_no[i] += 1
             srv.submit(sids[i], bufs[i][k % 2], 0.0, 0.0, 0.0, 0.1, tag=tag)
 
-        # warm-up: first frames (initialisation), then one launch of every batch-size bucket
-        # (1, 2, 4, ... 64 frames) so that no CUDA graph is instantiated in the timed phases
+        # warm-up: first frames (initialisation); the batched slots' CUDA graphs of every
+        # batch-size bucket are built when the server is created
         for r in range(3):
             for i in range(n_streams):
                 submit(i, 0)
             srv.drain(600000)
-        b = 1
-        while b <= 64:
-            for rep in range(2):  # both launch slots
-                srv.pause(True)
-                for i in range(b):
-                    submit(i, 0)
-                srv.pause(False)
-                srv.drain(600000)
-            b *= 2
         srv.poll_array(1 << 20)
         # saturation: every stream has `saturate_frames` frames queued at once
         t0 = time.perf_counter()

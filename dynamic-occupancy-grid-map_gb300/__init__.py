@@ -53,6 +53,7 @@ ABI_SYMBOLS = [
     "dogm_get_tune", "dogm_set_tune", "dogm_autotune",
     "dogm_meas_grid_create", "dogm_meas_grid_destroy", "dogm_meas_grid_generate", "dogm_meas_grid_size",
     "dogm_meas_grid_polar", "dogm_meas_grid_fan", "dogm_extract_dynamic_cells", "dogm_extract_dynamic_cells_device",
+    "dogm_snapshot_bytes", "dogm_snapshot", "dogm_restore",
 ]
 
 
@@ -153,6 +154,7 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_meas_grid_polar": ([vp, vp, sz, vp, vp], i), "dogm_meas_grid_fan": ([vp, vp, vp, vp, i, vp, vp], i),
         "dogm_extract_dynamic_cells": ([vp, f, f, vp, i, vp], i),
         "dogm_extract_dynamic_cells_device": ([vp, i, f, f, vp, i, vp, vp, vp], i),
+        "dogm_snapshot_bytes": ([vp], sz), "dogm_snapshot": ([vp, vp, sz], i), "dogm_restore": ([vp, vp, sz], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -326,6 +328,17 @@ class DOGM:
     def stream(self) -> int:
         """The cudaStream_t the handle launches on (record CUDA events on it)."""
         return load().dogm_get_stream(self.h) or 0
+
+    def snapshot(self) -> bytes:
+        """The state this handle carries into its next update (dogm_snapshot)."""
+        n = load().dogm_snapshot_bytes(self.h)
+        buf = np.empty(n, np.uint8)
+        check(load().dogm_snapshot(self.h, _ptr(buf), n), "dogm_snapshot")
+        return buf.tobytes()
+
+    def restore(self, snap: bytes) -> None:
+        buf = np.frombuffer(snap, np.uint8)
+        check(load().dogm_restore(self.h, _ptr(buf), buf.size), "dogm_restore")
 
     def extract_dynamic_cells(self, min_occupancy: float = 0.7, min_velocity: float = 4.0,
                               max_out: int = 1 << 16) -> np.ndarray:

@@ -189,6 +189,7 @@ struct SlotFrame {
 dogm_status slot_create(int device, BatchSlot** out);
 void slot_destroy(BatchSlot* s);
 dogm_status slot_launch(BatchSlot* s, const SlotFrame* frames, int n);
+dogm_status slot_prewarm(BatchSlot* s, int max_n);  // build the graphs of batches up to max_n
 bool slot_done(BatchSlot* s);
 dogm_status slot_finish(BatchSlot* s);
 // Per-handle helpers of the per-stream serving mode.

@@ -955,6 +955,113 @@ int dogm_stage_times(dogm_handle* h, float* ms, int n) {
 
 const char* dogm_stage_name(int i) { return (i >= 0 && i < kStages) ? kStageNames[i] : ""; }
 
+// ---- snapshot and restore --------------------------------------------------------------------
+
+namespace {
+struct SnapshotHeader {
+    char magic[8];  // "DOGMSNP1"
+    uint32_t header_bytes;
+    int32_t gs, N, B;
+    dogm_params params;
+    uint64_t seed;
+    uint32_t stream_id;
+    int32_t iteration;
+    int32_t first_pose, first_measurement, need_clear;
+    float position_x, position_y, yaw;
+    FrameState fs;
+};
+constexpr char kSnapMagic[8] = {'D', 'O', 'G', 'M', 'S', 'N', 'P', '1'};
+
+size_t snapshot_payload(const dogm_handle* h) {
+    const size_t N = (size_t)h->N, C = (size_t)h->C;
+    return N * (16 + 4) + C * (4 + sizeof(dogm_measurement_cell) + sizeof(dogm_grid_cell));
+}
+}  // namespace
+
+size_t dogm_snapshot_bytes(const dogm_handle* h) { return h ? sizeof(SnapshotHeader) + snapshot_payload(h) : 0; }
+
+dogm_status dogm_snapshot(dogm_handle* h, void* host_buf, size_t n) {
+    if (!h || !host_buf) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n < dogm_snapshot_bytes(h)) return fail(DOGM_ERR_INVALID_ARGUMENT, "buffer smaller than dogm_snapshot_bytes");
+    DeviceGuard dg(h->device);
+    dogm_status st = dogm_synchronize(h);
+    if (st != DOGM_OK) return st;
+    SnapshotHeader hd;
+    std::memset(&hd, 0, sizeof(hd));
+    std::memcpy(hd.magic, kSnapMagic, 8);
+    hd.header_bytes = sizeof(SnapshotHeader);
+    hd.gs = h->gs;
+    hd.N = h->N;
+    hd.B = h->B;
+    hd.params = h->params;
+    hd.seed = h->opt.seed;
+    hd.stream_id = h->opt.stream_id;
+    hd.iteration = h->iteration;
+    hd.first_pose = h->first_pose_received;
+    hd.first_measurement = h->first_measurement_received;
+    hd.need_clear = h->need_clear;
+    hd.position_x = h->position_x;
+    hd.position_y = h->position_y;
+    hd.yaw = h->yaw;
+    DOGM_CUDA(cudaMemcpy(&hd.fs, h->desc.fs, sizeof(FrameState), cudaMemcpyDeviceToHost));
+    unsigned char* p = static_cast<unsigned char*>(host_buf);
+    std::memcpy(p, &hd, sizeof(hd));
+    p += sizeof(hd);
+    const size_t N = (size_t)h->N, C = (size_t)h->C;
+    DOGM_CUDA(cudaMemcpy(p, h->desc.P_state, 16 * N, cudaMemcpyDeviceToHost));
+    p += 16 * N;
+    DOGM_CUDA(cudaMemcpy(p, h->desc.P_key, 4 * N, cudaMemcpyDeviceToHost));
+    p += 4 * N;
+    DOGM_CUDA(cudaMemcpy(p, h->desc.free_old, 4 * C, cudaMemcpyDeviceToHost));  // carried into the next update
+    p += 4 * C;
+    DOGM_CUDA(cudaMemcpy(p, h->desc.meas_own, sizeof(dogm_measurement_cell) * C, cudaMemcpyDeviceToHost));
+    p += sizeof(dogm_measurement_cell) * C;
+    DOGM_CUDA(cudaMemcpy(p, h->desc.cells, sizeof(dogm_grid_cell) * C, cudaMemcpyDeviceToHost));
+    return DOGM_OK;
+}
+
+dogm_status dogm_restore(dogm_handle* h, const void* host_buf, size_t n) {
+    if (!h || !host_buf) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n < sizeof(SnapshotHeader)) return fail(DOGM_ERR_INVALID_ARGUMENT, "buffer shorter than a snapshot header");
+    SnapshotHeader hd;
+    std::memcpy(&hd, host_buf, sizeof(hd));
+    if (std::memcmp(hd.magic, kSnapMagic, 8) != 0 || hd.header_bytes != sizeof(SnapshotHeader))
+        return fail(DOGM_ERR_INVALID_ARGUMENT, "not a snapshot of this library version");
+    if (hd.gs != h->gs || hd.N != h->N || hd.B != h->B || std::memcmp(&hd.params, &h->params, sizeof(dogm_params)) != 0)
+        return fail(DOGM_ERR_INVALID_ARGUMENT, "snapshot of a handle with other parameters");
+    if (n < dogm_snapshot_bytes(h)) return fail(DOGM_ERR_INVALID_ARGUMENT, "truncated snapshot");
+    DeviceGuard dg(h->device);
+    dogm_status st = dogm_synchronize(h);
+    if (st != DOGM_OK) return st;
+    const unsigned char* p = static_cast<const unsigned char*>(host_buf) + sizeof(hd);
+    const size_t N = (size_t)h->N, C = (size_t)h->C;
+    DOGM_CUDA(cudaMemcpy(h->desc.P_state, p, 16 * N, cudaMemcpyHostToDevice));
+    p += 16 * N;
+    DOGM_CUDA(cudaMemcpy(h->desc.P_key, p, 4 * N, cudaMemcpyHostToDevice));
+    p += 4 * N;
+    DOGM_CUDA(cudaMemcpy(h->desc.free_old, p, 4 * C, cudaMemcpyHostToDevice));
+    p += 4 * C;
+    DOGM_CUDA(cudaMemcpy(h->desc.meas_own, p, sizeof(dogm_measurement_cell) * C, cudaMemcpyHostToDevice));
+    p += sizeof(dogm_measurement_cell) * C;
+    DOGM_CUDA(cudaMemcpy(h->desc.cells, p, sizeof(dogm_grid_cell) * C, cudaMemcpyHostToDevice));
+    FrameState fs = hd.fs;
+    fs.status = 0u;
+    DOGM_CUDA(cudaMemcpy(h->desc.fs, &fs, sizeof(FrameState), cudaMemcpyHostToDevice));
+    h->opt.seed = hd.seed;
+    h->opt.stream_id = hd.stream_id;
+    h->desc.seed_lo = (uint32_t)(hd.seed & 0xffffffffull);
+    h->desc.seed_hi = (uint32_t)(hd.seed >> 32);
+    h->desc.stream_id = hd.stream_id;
+    h->iteration = hd.iteration;
+    h->first_pose_received = hd.first_pose != 0;
+    h->first_measurement_received = hd.first_measurement != 0;
+    h->position_x = hd.position_x;
+    h->position_y = hd.position_y;
+    h->yaw = hd.yaw;
+    h->need_clear = true;  // the restored frame starts with a full reset of the per-frame counters
+    return DOGM_OK;
+}
+
 dogm_status dogm_extract_dynamic_cells(dogm_handle* h, float min_occupancy, float min_velocity,
                                        dogm_dynamic_cell* host_out, int max_out, int* n_found) {
     if (!h || !n_found || max_out < 0 || (max_out > 0 && !host_out))
@@ -1283,6 +1390,39 @@ dogm_status slot_launch(BatchSlot* s, const SlotFrame* fr, int n) {
         s->hs[i]->last_launches = launches;
     }
     s->mirror = mirror;
+    return DOGM_OK;
+}
+
+// Captures and instantiates the steady-state graph of every batch-size bucket up to max_n for
+// both mirrors, without launching it: a graph records the launches on the slot's device batch
+// and the copies from its pinned mirrors, none of which depends on the handles of a frame.
+dogm_status slot_prewarm(BatchSlot* s, int max_n) {
+    if (!s) return fail(DOGM_ERR_INVALID_ARGUMENT, "slot is NULL");
+    Ctx& c = s->ctx;
+    DeviceGuard dg(c.device);
+    const int cur = c.cur;
+    for (int m = 0; m < 2; ++m) {
+        for (int nb = 1; nb <= graph_bucket(std::max(1, max_n)); nb <<= 1) {
+            const int key = nb * 2 + m;
+            if (c.graphs.count(key)) continue;
+            c.cur = m;
+            cudaGraph_t graph;
+            DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = upload_batch(c, nb);
+            if (e == cudaSuccess) e = frame_kernels(c, false, false);
+            if (e == cudaSuccess) e = download_status(c);
+            cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
+            c.cur = cur;
+            if (e != cudaSuccess || e2 != cudaSuccess)
+                return fail(DOGM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
+            cudaGraphExec_t exec;
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+            c.graphs.emplace(key, exec);
+        }
+    }
+    c.cur = cur;
     return DOGM_OK;
 }
 

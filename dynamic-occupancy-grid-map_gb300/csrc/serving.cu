@@ -360,8 +360,10 @@ dogm_status dogm_server_create(const dogm_server_config* cfg, dogm_server** out)
     if (cfg->mode == DOGM_SERVE_BATCHED) {
         for (int i = 0; i < cfg->max_inflight; ++i) {
             BatchSlot* slot = nullptr;
-            const dogm_status rc = slot_create(s->device, &slot);
+            dogm_status rc = slot_create(s->device, &slot);
+            if (rc == DOGM_OK) rc = slot_prewarm(slot, cfg->max_batch);  // no graph built mid-serving
             if (rc != DOGM_OK) {
+                slot_destroy(slot);
                 for (BatchSlot* b : s->all_slots) slot_destroy(b);
                 delete s;
                 return rc;

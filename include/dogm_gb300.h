@@ -342,6 +342,21 @@ dogm_status dogm_server_stream_handle(dogm_server* s, int stream_id, dogm_handle
 /* The clock of dogm_server_result (monotonic, nanoseconds). */
 int64_t dogm_server_now_ns(void);
 
+/* ---- snapshot and restore -----------------------------------------------------------------
+ *
+ * No counterpart in the reference.  A snapshot is the state one update carries into the next:
+ * particles (state and key words), the free mass, the common particle weight, the resident
+ * measurement grid, the last cell records, the pose bookkeeping, the update count and the
+ * random-number identity (seed, stream id).  Restoring it into a handle created with the same
+ * dogm_params makes that handle continue bit-identically to the original (used to move a
+ * serving stream, or to resume after a restart).  The buffer is host memory in native byte
+ * order, starting with a versioned header. */
+size_t dogm_snapshot_bytes(const dogm_handle* h);
+dogm_status dogm_snapshot(dogm_handle* h, void* host_buf, size_t n);
+/* DOGM_ERR_INVALID_ARGUMENT (handle unchanged) if the buffer is not a snapshot of a handle with
+ * the same parameters. */
+dogm_status dogm_restore(dogm_handle* h, const void* host_buf, size_t n);
+
 /* ---- dynamic-cell extraction -------------------------------------------------------------
  *
  * Replaces the demo's host-side computeCellsWithVelocity (dogm/demo/utils/image_creation.cpp:
