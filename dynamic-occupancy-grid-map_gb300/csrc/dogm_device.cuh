@@ -172,6 +172,17 @@ __device__ __forceinline__ CellOut cell_masses(int n_in, float c, float free_pre
 }
 
 // ---------------------------------------------------------------------------------------
+// Programmatic dependent launch: wait until the previous kernel of the stream has completed
+// and its writes are visible (a no-op for a launch without the attribute).  First statement of
+// every frame kernel, so no global access of this kernel overlaps the previous one.  No kernel
+// triggers its dependents early: the next launch is prepared while this one completes (an
+// early trigger, with the next kernel's blocks parked on the SMs, measured 3 % slower).
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void grid_dependency_begin() {
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------------------
 // Asynchronous global -> shared copies (cp.async): a thread's copies land while it works on
 // something else; cp_async_wait_all() makes that thread's own copies visible to it.
 // ---------------------------------------------------------------------------------------

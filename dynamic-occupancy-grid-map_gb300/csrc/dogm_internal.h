@@ -137,8 +137,29 @@ struct Batch {
 struct LaunchCfg {
     int num_sms;
     cudaStream_t stream;
-    int mult = 0;  // blocks per SM of this launch (0: the kernel's built-in default)
+    int mult = 0;      // blocks per SM of this launch (0: the kernel's built-in default)
+    bool pdl = false;  // programmatic dependent launch after the previous kernel on the stream
 };
+
+// Launches a frame kernel.  With cfg.pdl the launch is programmatically serialised after the
+// previous kernel on the stream (its launch is processed while that kernel completes); every
+// frame kernel begins with grid_dependency_begin(), which waits for the previous kernel to
+// complete and flush before any of its own memory accesses.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_kernel(const LaunchCfg& cfg, void (*kernel)(KArgs...), int grid, int block, size_t smem,
+                          Args... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)grid);
+    lc.blockDim = dim3((unsigned)block);
+    lc.dynamicSmemBytes = smem;
+    lc.stream = cfg.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = cfg.pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&lc, kernel, args...);
+}
 // Blocks of a persistent launch: num_sms x the tuned multiplier, or x the default.
 inline int launch_blocks(const LaunchCfg& cfg, int default_mult) {
     return cfg.num_sms * (cfg.mult > 0 ? cfg.mult : default_mult);

@@ -147,6 +147,7 @@ __device__ __forceinline__ void put_cell(CellSmem& sm, const GridDesc& g, uint32
 }
 
 __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ bt) {
+    grid_dependency_begin();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CellSmem& sm = *reinterpret_cast<CellSmem*>(smem_raw);
     const int total = batch_total(bt, kStCell);
@@ -390,6 +391,7 @@ __device__ __forceinline__ void add_joint_range(unsigned long long (&racc)[kRunT
 }
 
 __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt) {
+    grid_dependency_begin();
     __shared__ unsigned long long red[2 * (kThreads / 32)];
     __shared__ int s_bnd[kCellTile + 1];  // s_bnd[c]: first slot of cell c of the tile; [kCellTile]: end
     __shared__ int s_nuA[kCellTile];
@@ -491,13 +493,11 @@ cudaError_t prepare_cells() {
 }
 
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg) {
-    k_cells<<<launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), cfg.stream>>>(const_cast<Batch*>(d_batch));
-    return cudaGetLastError();
+    return launch_kernel(cfg, k_cells, launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), const_cast<Batch*>(d_batch));
 }
 
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg) {
-    k_newborn<<<launch_blocks(cfg, 6), kThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch));
-    return cudaGetLastError();
+    return launch_kernel(cfg, k_newborn, launch_blocks(cfg, 6), kThreads, 0, const_cast<Batch*>(d_batch));
 }
 
 }  // namespace dogm_gb300

@@ -48,6 +48,7 @@ constexpr int kPredictThreads = 512;
 static_assert(kPredictTile % kPredictThreads == 0, "whole particles per thread");
 
 __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restrict__ bt, int mode) {
+    grid_dependency_begin();
     __shared__ uint32_t h0[kSortMaxBins];
     __shared__ uint32_t h1[kSortMaxBins];
     __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (ranges of the cell pass)

@@ -52,6 +52,7 @@ struct ResSmem {
 };
 
 __global__ void __launch_bounds__(kThreads, 6) k_resample(Batch* __restrict__ bt) {
+    grid_dependency_begin();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ResSmem& sm = *reinterpret_cast<ResSmem*>(smem_raw);
     const int total = batch_total(bt, kStResample);
@@ -228,8 +229,7 @@ cudaError_t prepare_kernels() {
 
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg) {
     const int smem = (int)sizeof(ResSmem);
-    k_resample<<<launch_blocks(cfg, 6), kThreads, smem, cfg.stream>>>(const_cast<Batch*>(d_batch));
-    return cudaGetLastError();
+    return launch_kernel(cfg, k_resample, launch_blocks(cfg, 6), kThreads, (size_t)smem, const_cast<Batch*>(d_batch));
 }
 
 // ---------------------------------------------------------------------------------------

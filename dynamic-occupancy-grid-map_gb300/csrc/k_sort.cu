@@ -78,6 +78,7 @@ __device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) 
 }
 
 __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict__ bt, int pass) {
+    grid_dependency_begin();
     __shared__ uint32_t chunk[kScanWarps][33];
     __shared__ uint32_t red[kScanWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -172,6 +173,7 @@ struct SortSmem {
 // Four blocks per SM: a 2M-particle frame's 489 tiles run in one wave.
 template <bool FINAL>
 __global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ bt) {
+    grid_dependency_begin();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SortSmem& sm = *reinterpret_cast<SortSmem*>(smem_raw);
     const int stage = FINAL ? kStSort1 : kStSort0;
@@ -278,18 +280,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ b
 }
 
 cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
-    k_sort_scan<<<launch_blocks(cfg, 2), kScanWarps * 32, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), pass);
-    return cudaGetLastError();
+    return launch_kernel(cfg, k_sort_scan, launch_blocks(cfg, 2), kScanWarps * 32, 0, const_cast<Batch*>(d_batch), pass);
 }
 
 cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
     const size_t smem = sizeof(SortSmem);  // 48 KB: no opt-in attribute needed
     Batch* b = const_cast<Batch*>(d_batch);
     if (pass == 0)
-        k_sort_pass<false><<<launch_blocks(cfg, 4), kThreads, smem, cfg.stream>>>(b);
+        return launch_kernel(cfg, k_sort_pass<false>, launch_blocks(cfg, 4), kThreads, smem, b);
     else
-        k_sort_pass<true><<<launch_blocks(cfg, 4), kThreads, smem, cfg.stream>>>(b);
-    return cudaGetLastError();
+        return launch_kernel(cfg, k_sort_pass<true>, launch_blocks(cfg, 4), kThreads, smem, b);
 }
 
 cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg) {

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -60,6 +61,9 @@ struct Ctx {
     bool profile = false;
     cudaEvent_t ev[kStages + 1] = {};
     int mult[kStages] = {};  // tuned blocks per SM per stage (0: the kernel's default)
+    // programmatic dependent launch between the frame's kernels (environment DOGM_PDL=0 turns
+    // it off, for comparison)
+    bool pdl = true;
 
     // Captured graphs hold the launch widths: drop them when the widths change.
     void drop_graphs() {
@@ -83,6 +87,7 @@ struct Ctx {
 
 dogm_status ctx_init(Ctx& c, int device) {
     c.device = device;
+    if (const char* v = std::getenv("DOGM_PDL")) c.pdl = std::strcmp(v, "0") != 0;
     DOGM_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
     DOGM_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     c.own_stream = true;
@@ -279,6 +284,7 @@ cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
     do {                                                                            \
         if (prof && (e = cudaEventRecord(c.ev[i], c.stream)) != cudaSuccess) return e; \
         cfg.mult = c.mult[i];                                                       \
+        cfg.pdl = c.pdl && !prof && i > 0; /* predict follows the batch upload */   \
         if ((e = (call)) != cudaSuccess) return e;                                  \
     } while (0)
     // the per-frame counters are reset by predict and the cell pass of the previous frame; a
