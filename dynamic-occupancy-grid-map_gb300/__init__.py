@@ -54,6 +54,8 @@ ABI_SYMBOLS = [
     "dogm_meas_grid_create", "dogm_meas_grid_destroy", "dogm_meas_grid_generate", "dogm_meas_grid_size",
     "dogm_meas_grid_polar", "dogm_meas_grid_fan", "dogm_extract_dynamic_cells", "dogm_extract_dynamic_cells_device",
     "dogm_snapshot_bytes", "dogm_snapshot", "dogm_restore",
+    "dogm_cluster_cells", "dogm_evaluator_create", "dogm_evaluator_destroy", "dogm_evaluator_add_step",
+    "dogm_evaluator_summary",
 ]
 
 
@@ -155,6 +157,9 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_extract_dynamic_cells": ([vp, f, f, vp, i, vp], i),
         "dogm_extract_dynamic_cells_device": ([vp, i, f, f, vp, i, vp, vp, vp], i),
         "dogm_snapshot_bytes": ([vp], sz), "dogm_snapshot": ([vp, vp, sz], i), "dogm_restore": ([vp, vp, sz], i),
+        "dogm_cluster_cells": ([vp, i, f, i, i, vp, vp], i), "dogm_evaluator_create": ([f, f, i, vp], i),
+        "dogm_evaluator_destroy": ([vp], i), "dogm_evaluator_add_step": ([vp, vp, i, vp, i, vp, i, vp], i),
+        "dogm_evaluator_summary": ([vp, vp, vp, vp, vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -672,3 +677,74 @@ class MeasurementGridGenerator:
         check(load().dogm_meas_grid_fan(self.m, _ptr(x), _ptr(y), _ptr(sv), nv.value, None, None),
               "dogm_meas_grid_fan")
         return {"x256": x, "y256": y, "s": sv, "first_angle": a0.value}
+
+
+# ---- accuracy evaluation (host code: dogm_cluster_cells, dogm_evaluator_*) -------------------
+DBSCAN_REFERENCE, DBSCAN_STANDARD = 0, 1
+_DBSCAN_MODES = {"reference": DBSCAN_REFERENCE, "standard": DBSCAN_STANDARD}
+# dogm_object_truth: a ground-truth vehicle, metres and m/s with y up
+OBJECT_TRUTH_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("vx", "<f4"), ("vy", "<f4")])
+# dogm_cluster: one DBSCAN cluster of a frame and its match
+CLUSTER_DTYPE = np.dtype([("x", "<f4"), ("y", "<f4"), ("vx", "<f4"), ("vy", "<f4"), ("cells", "<i4"),
+                          ("truth", "<i4"), ("err_x", "<f4"), ("err_y", "<f4"), ("err_vx", "<f4"),
+                          ("err_vy", "<f4")])
+
+
+def _cells(cells) -> np.ndarray:
+    return np.ascontiguousarray(cells, DYNAMIC_CELL_DTYPE)
+
+
+def cluster_cells(cells, eps: float = 3.0, min_cells: int = 5, mode: str = "reference") -> tuple[np.ndarray, int]:
+    """DBSCAN over dynamic cells (dbscan.cpp:24-114): per-cell cluster labels (-1: none) and the
+    cluster count."""
+    c = _cells(cells)
+    label = np.empty(max(len(c), 1), np.int32)
+    n = C.c_int(0)
+    check(load().dogm_cluster_cells(_ptr(c), len(c), eps, min_cells, _DBSCAN_MODES[mode], _ptr(label), C.byref(n)),
+          "dogm_cluster_cells")
+    return label[:len(c)], n.value
+
+
+class Evaluator:
+    """PrecisionEvaluator with its MAE and RMSE metrics (precision_evaluator.cpp:16-139)."""
+
+    def __init__(self, resolution: float, grid_length: float, mode: str = "reference"):
+        e = C.c_void_p()
+        check(load().dogm_evaluator_create(resolution, grid_length, _DBSCAN_MODES[mode], C.byref(e)),
+              "dogm_evaluator_create")
+        self.e = e
+
+    def close(self) -> None:
+        if self.e:
+            load().dogm_evaluator_destroy(self.e)
+            self.e = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_step(self, cells, truth) -> np.ndarray:
+        """Clusters one frame's cells, matches them to `truth` (OBJECT_TRUTH_DTYPE or rows of
+        x, y, vx, vy) and accumulates the errors; returns the frame's clusters."""
+        c = _cells(cells)
+        t = np.asarray(truth)
+        if t.dtype == OBJECT_TRUTH_DTYPE:
+            t = np.ascontiguousarray(t).reshape(-1)
+        else:
+            t = np.ascontiguousarray(np.asarray(truth, np.float32).reshape(-1, 4)).view(OBJECT_TRUTH_DTYPE).reshape(-1)
+        cap = max(len(c), 1)
+        out = np.zeros(cap, CLUSTER_DTYPE)
+        n = C.c_int(0)
+        check(load().dogm_evaluator_add_step(self.e, _ptr(c), len(c), _ptr(t), len(t), _ptr(out), cap,
+                                             C.byref(n)), "dogm_evaluator_add_step")
+        return out[:n.value]
+
+    def summary(self) -> dict:
+        mae = np.empty(4, np.float32)
+        rmse = np.empty(4, np.float32)
+        det, una = C.c_int(0), C.c_int(0)
+        check(load().dogm_evaluator_summary(self.e, _ptr(mae), _ptr(rmse), C.byref(det), C.byref(una)),
+              "dogm_evaluator_summary")
+        return {"mae": mae, "rmse": rmse, "detections": det.value, "unassigned": una.value}

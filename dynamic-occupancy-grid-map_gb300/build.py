@@ -24,9 +24,9 @@ ORACLE_DIR = os.path.join(REPO, "oracle")
 ORACLE_BUILD = os.path.join(ORACLE_DIR, "_build")
 ORACLE_LIB = os.path.join(ORACLE_BUILD, "libdogm_oracle.so")
 
-CUDA_SOURCES = ["k_particles.cu", "k_sort.cu", "k_cells.cu", "k_resample.cu", "runtime.cu", "serving.cu", "k_meas.cu", "k_extract.cu"]
+CUDA_SOURCES = ["k_particles.cu", "k_sort.cu", "k_cells.cu", "k_resample.cu", "runtime.cu", "serving.cu", "k_meas.cu", "k_extract.cu", "evaluate.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",
               "-I" + INCLUDE, "-I" + CSRC]
 
 

@@ -385,6 +385,58 @@ dogm_status dogm_extract_dynamic_cells_device(const dogm_grid_cell* cells, int g
                                               float min_velocity, dogm_dynamic_cell* out, int max_out,
                                               unsigned int* scratch, int* n_found, void* stream);
 
+/* ---- accuracy evaluation against ground truth (host code) --------------------------------
+ *
+ * Replaces the demo's PrecisionEvaluator with its DBSCAN and MAE/RMSE metrics
+ * (dogm/demo/utils/precision_evaluator.cpp:16-139, dbscan.cpp:24-114, metrics.cpp:8-56):
+ * the dynamic cells of a frame are clustered (eps 3 cells, at least 5 cells within eps counting
+ * the cell itself), each cluster's mean (x, y, vx, vy) is converted to metres with y up
+ * (x * r, grid_length - y * r, vx * r, -vy * r, precision_evaluator.cpp:98-121) and matched to the
+ * nearest object closer than 5 m; errors accumulate into MAE and RMSE, unmatched clusters into
+ * the unassigned count.  The functions touch no GPU. */
+typedef enum dogm_dbscan_mode {
+    DOGM_DBSCAN_REFERENCE = 0, /* dbscan.cpp:55-98 exactly, including its labelling of the first
+                                  |seeds| input points (dbscan.cpp:64-67) instead of the seeds   */
+    DOGM_DBSCAN_STANDARD = 1   /* the published DBSCAN, same visiting order                      */
+} dogm_dbscan_mode;
+
+/* Vehicle of the simulator (dogm/demo/simulator/include/simulator.h:11-31): position of the
+ * facing side's centre and velocity, metres and m/s, x right, y up. */
+typedef struct dogm_object_truth {
+    float x, y, vx, vy;
+} dogm_object_truth;
+
+typedef struct dogm_cluster {
+    float x, y, vx, vy;                  /* cluster mean in metres / m/s, y up (NaN if empty) */
+    int cells;                           /* cells in the cluster                              */
+    int truth;                           /* matched object, -1 if none within 5 m             */
+    float err_x, err_y, err_vx, err_vy;  /* mean - object (0 if unmatched)                    */
+} dogm_cluster;
+
+/* DBSCAN over the cells' (x, y); label[i] receives the cluster of cell i or -1.  Cells must have
+ * distinct coordinates. */
+dogm_status dogm_cluster_cells(const dogm_dynamic_cell* cells, int n, float eps, int min_cells, int mode,
+                               int* label, int* n_clusters);
+
+typedef struct dogm_evaluator dogm_evaluator;
+
+/* resolution: metres per cell; grid_length: the grid's side in metres (GridParams::size). */
+dogm_status dogm_evaluator_create(float resolution, float grid_length, int dbscan_mode, dogm_evaluator** out);
+dogm_status dogm_evaluator_destroy(dogm_evaluator* e);
+
+/* PrecisionEvaluator::evaluateAndStoreStep: clusters the frame's cells and accumulates the errors
+ * of the matched clusters.  With no cells or no objects the frame adds nothing.  Up to
+ * max_clusters clusters are written to `clusters` (may be NULL); *n_clusters receives how many
+ * the frame had. */
+dogm_status dogm_evaluator_add_step(dogm_evaluator* e, const dogm_dynamic_cell* cells, int n,
+                                    const dogm_object_truth* truth, int n_truth, dogm_cluster* clusters,
+                                    int max_clusters, int* n_clusters);
+
+/* MAE and RMSE of (x, y, vx, vy) over all matched clusters so far (NaN before the first match),
+ * the number of matched clusters and of unassigned ones.  Any output may be NULL. */
+dogm_status dogm_evaluator_summary(const dogm_evaluator* e, float* mae4, float* rmse4, int* detections,
+                                   int* unassigned);
+
 /* ---- measurement-grid generation from a lidar scan --------------------------------------
  *
  * Replaces the demo's LaserMeasurementGrid (dogm/demo/simulator/include/mapping/

@@ -12,6 +12,11 @@ stand-in (vec4, mat4x4, transpose, matrix-vector product).  dogm_types.h uses as
 including <cassert>, so it is force-included.  The reference's CMake build cannot be used here
 (it requires OpenGL and downloads googletest, dogm/CMakeLists.txt:9,31).
 
+The demo's accuracy evaluator (dogm/demo/utils/dbscan.cpp, metrics.cpp,
+precision_evaluator.cpp) is plain host C++; it is compiled where it lies together with
+oracle/ref/eval_harness.cu into oracle/_ref/libref_eval.so, a host library for the CPU tests of
+this machine (it does not run on the Arm GPU machine, where the tests that need it skip).
+
     python oracle/ref/build_ref.py            # where the reference sources are present
 """
 from __future__ import annotations
@@ -60,6 +65,28 @@ def _one(name: str) -> str:
     return dst
 
 
+EVAL_SOURCES = ["dbscan.cpp", "metrics.cpp", "precision_evaluator.cpp"]
+EVAL_LIB = os.path.join(OUT, "libref_eval.so")
+
+
+def build_eval() -> str:
+    """Builds oracle/_ref/libref_eval.so: the reference's evaluator plus eval_harness.cu."""
+    utils = os.path.join(REFERENCE, "demo", "utils")
+    srcs = [os.path.join(utils, f) for f in EVAL_SOURCES] + [os.path.join(HERE, "eval_harness.cu")]
+    deps = srcs + [__file__] + [os.path.join(HERE, "glm", f) for f in os.listdir(os.path.join(HERE, "glm"))]
+    if os.path.exists(EVAL_LIB) and all(os.path.getmtime(d) <= os.path.getmtime(EVAL_LIB) for d in deps):
+        return EVAL_LIB
+    tmp = EVAL_LIB + ".tmp"
+    cmd = [_nvcc(), "-x", "cu", "-O2", "-std=c++17", "-shared", "-Xcompiler", "-fPIC,-ffp-contract=off",
+           "-include", "cassert", "-I" + HERE, "-I" + os.path.join(REFERENCE, "include"),
+           "-I" + os.path.join(utils, "include"), "-I" + os.path.join(REFERENCE, "demo", "simulator", "include")]
+    r = subprocess.run(cmd + srcs + ["-o", tmp], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference evaluator did not compile:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, EVAL_LIB)
+    return EVAL_LIB
+
+
 def build(verbose: bool = False) -> list[str]:
     """Builds oracle/_ref/*.cubin from the reference sources (no-op without them)."""
     if not available():
@@ -68,7 +95,8 @@ def build(verbose: bool = False) -> list[str]:
         return []
     os.makedirs(OUT, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(KERNEL_FILES)) as ex:
-        outs = list(ex.map(_one, KERNEL_FILES))
+        ev = ex.submit(build_eval)
+        outs = list(ex.map(_one, KERNEL_FILES)) + [ev.result()]
     if verbose:
         print("built %d reference cubins in %s" % (len(outs), OUT))
     return outs
