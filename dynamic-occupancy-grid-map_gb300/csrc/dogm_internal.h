@@ -85,7 +85,7 @@ struct GridDesc {
     uint32_t seed_lo, seed_hi;
     // particles (persistent: P, sort temporaries: T, sorted: S, newborn: Bp)
     float4* P_state; uint32_t* P_key;
-    uint32_t* T_key; uint32_t* T_idx;
+    uint2* T_pair;          // pass-0 output: {key word, index of the particle in P}
     float4* S_state; uint32_t* S_key;
     float4* B_state; uint32_t* B_key; float* B_w;  // newborns: key words always, state/weight for debug export
     // cells
@@ -173,6 +173,8 @@ cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg
 cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg);
 cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cfg);
+// pass-1 digit counts of every pass-0 output tile (k_sort_hist), then their column scan
+cudaError_t launch_sort_offsets1(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg);
@@ -190,7 +192,7 @@ cudaError_t launch_lower_bound(const float* accum, int n_accum, const float* q, 
 // Kernel launches per steady-state update (for the launch-count claim): predict, 2 x (digit
 // scan, sort pass), cells, newborn, resample.  A grid's first frame, and a frame after a
 // failed one, adds the frame-begin reset.
-constexpr int kLaunchesPerFrame = 8;
+constexpr int kLaunchesPerFrame = 9;
 constexpr int kLaunchesInit = 2;
 
 // ---- batch slots (runtime.cu): the launch contexts of the serving loop (serving.cu) ------

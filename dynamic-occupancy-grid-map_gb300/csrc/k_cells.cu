@@ -154,17 +154,13 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     {
         // the next frame's counters start at zero: predict adds the digit and cell-tile
-        // counts and sort pass 0 the pass-1 digit counts; their readers (the digit scans and
-        // the sort passes) finished before this kernel
+        // counts; their readers (the digit scans) finished before this kernel
         const int stride = gridDim.x * blockDim.x;
         const int tid = blockIdx.x * blockDim.x + threadIdx.x;
         for (int gi = 0; gi < bt->n_grids; ++gi) {
             const GridDesc& g = bt->g[gi];
             for (int i = tid; i < 2 * kSortMaxBins; i += stride) g.hist[i] = 0u;
             for (int i = tid; i < g.tiles[kStCell]; i += stride) g.ctile_cnt[i] = 0u;
-            uint4* h1 = reinterpret_cast<uint4*>(g.hsort + (size_t)g.sort_tiles * kSortMaxBins);
-            const int n1 = g.sort_tiles * kSortMaxBins / 4;
-            for (int i = tid; i < n1; i += stride) h1[i] = make_uint4(0u, 0u, 0u, 0u);
         }
     }
     for (;;) {

@@ -19,10 +19,7 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
         for (int i = tid; i < g.tiles[kStCell]; i += stride) g.ctile_cnt[i] = 0u;
         for (int i = tid; i < 2 * g.tiles[kStCell]; i += stride) g.cell_sum[i] = 0ull;
         for (int i = tid; i < g.tiles[kStResample]; i += stride) g.res_sum[i] = 0ull;
-        // pass-1 digit counts are accumulated by pass 0 (the pass-0 counts are written whole)
-        uint4* h1 = reinterpret_cast<uint4*>(g.hsort + (size_t)g.sort_tiles * kSortMaxBins);
-        const size_t n1 = (size_t)g.sort_tiles * kSortMaxBins / 4;
-        for (size_t i = tid; i < n1; i += stride) h1[i] = make_uint4(0u, 0u, 0u, 0u);
+        // (the per-tile digit counts of both passes are written whole each frame)
         if (tid == 0) {
             g.fs->status = 0u;
             g.fs->qb_total = 0ull;

@@ -1,11 +1,13 @@
 // Stable particle-to-cell sort: two LSD radix passes over the cell index (<= 11-bit digits),
 // reduce-then-scan.  Replaces thrust::sort_by_key with a zip payload (dogm/src/dogm.cu:262-281).
 //   upsweep    pass 0: per-tile digit histograms written by predict (same 4096-particle tiles);
-//              pass 1: counted by pass 0 at the output position of every key
+//              pass 1: k_sort_hist counts each tile of the pass-0 output in shared memory and
+//              writes its row whole (no global atomics, no zeroing between frames)
 //   k_sort_scan  column scan of the [tile][digit] histogram -> the global output offset of
 //              every (tile, digit) pair (digit base from predict's global histogram)
-//   k_sort_pass  stable warp ranking inside the tile, scatter to offset + rank; pass 1 also
-//              gathers the predicted particle state, so the payload moves once.
+//   k_sort_pass  stable warp ranking inside the tile, scatter to offset + rank; pass 0 moves
+//              {key, index} pairs (one 8-byte store per particle), pass 1 also gathers the
+//              predicted particle state, so the payload moves once.
 // Stability makes the permutation identical to the reference's stable sort.
 #include "dogm_device.cuh"
 
@@ -199,12 +201,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ b
         // load the tile warp-striped (item k of lane l: warp base + k*32 + l)
         const int base = lt * kSortTile + warp * (32 * kSortIpt);
         uint16_t* rank = sm.rank + warp * (32 * kSortIpt) + lane;  // item k at rank[k * 32]
+        // one base pointer per thread, items at constant offsets (k * 32 particles)
+        const uint32_t* src_kw = FINAL ? reinterpret_cast<const uint32_t*>(g.T_pair + base + lane) : g.P_key + base + lane;
+        constexpr int kw_stride = FINAL ? 64 : 32;  // words between a lane's items
         uint32_t key[kSortIpt];
 #pragma unroll
-        for (int k = 0; k < kSortIpt; ++k) {
-            const int pos = base + k * 32 + lane;
-            key[k] = pos < g.N ? (FINAL ? g.T_key[pos] : g.P_key[pos]) : 0xffffffffu;
-        }
+        for (int k = 0; k < kSortIpt; ++k)
+            key[k] = base + k * 32 + lane < g.N ? src_kw[k * kw_stride] : 0xffffffffu;
         // stable rank within the warp: rounds in input order, peers by match_any
 #pragma unroll
         for (int k = 0; k < kSortIpt; ++k) {
@@ -231,16 +234,15 @@ __global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ b
         }
         __syncthreads();
 
-        // scatter to the global sorted position; pass 0 also counts the pass-1 histogram.
-        // The final pass's arrays do not overlap: restrict lets the compiler issue the index
-        // loads and state gathers of several items before their stores.
-        const uint32_t* __restrict__ t_idx = g.T_idx;
+        // scatter to the global sorted position.  The final pass's arrays do not overlap:
+        // restrict lets the compiler issue the index loads and state gathers of several items
+        // before their stores.
+        const uint32_t* __restrict__ t_idx = src_kw + 1;  // .y words of the pass-0 pairs (final pass)
         const float4* __restrict__ p_state = g.P_state;
         float4* __restrict__ s_state = g.S_state;
         uint32_t* __restrict__ s_key = g.S_key;
-        uint32_t* H1 = g.hsort + (size_t)g.sort_tiles * kSortMaxBins;
-        const int shift1 = g.d0_bits;
-        const uint32_t nb1m = (1u << g.d1_bits) - 1u;
+        uint2* __restrict__ t_pair = g.T_pair;
+        const int pos0 = base + lane;
 #pragma unroll
         for (int k = 0; k < kSortIpt; ++k) {
             const int pos = base + k * 32 + lane;
@@ -254,27 +256,50 @@ __global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ b
                     out = 0xffffffffu;
                 }
             }
-            if (FINAL) {
-                if (out != 0xffffffffu) {
-                    const uint32_t src = t_idx[pos];  // particle index carried by pass 0
+            if (out != 0xffffffffu) {
+                if (FINAL) {
+                    const uint32_t src = t_idx[k * kw_stride];  // particle index carried by pass 0
                     s_key[out] = key[k];
                     s_state[out] = __ldg(p_state + src);
                     if (g.dbg_perm) g.dbg_perm[out] = (int)src;
+                } else {
+                    t_pair[out] = make_uint2(key[k], (uint32_t)(pos0 + k * 32));
                 }
-            } else {
-                uint32_t hk = 0xffffffffu;
-                if (out != 0xffffffffu) {
-                    g.T_key[out] = key[k];
-                    g.T_idx[out] = (uint32_t)pos;
-                    const uint32_t d1 = ((key[k] & kCellMask) >> shift1) & nb1m;
-                    hk = ((out / (uint32_t)kSortTile) << kSortMaxBits) | d1;
-                }
-                const uint32_t peers = __match_any_sync(0xffffffffu, hk);
-                if (hk != 0xffffffffu && lane == __ffs(peers) - 1)
-                    atomicAdd(&H1[(size_t)(hk >> kSortMaxBits) * kSortMaxBins + (hk & (kSortMaxBins - 1))],
-                              (uint32_t)__popc(peers));
             }
         }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Pass-1 digit counts: one tile of the pass-0 output per block iteration, counted in shared
+// memory; the row H1[tile][0 .. 2^d1) is written whole.
+// ---------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_sort_hist(Batch* __restrict__ bt) {
+    grid_dependency_begin();
+    __shared__ uint32_t cnt[kSortMaxBins];
+    const int total = batch_total(bt, kStSort1);
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+        const int gi = grid_of_tile(bt, kStSort1, t);
+        const GridDesc& g = bt->g[gi];
+        const int lt = t - bt->prefix[gi][kStSort1];
+        const int nb1 = 1 << g.d1_bits;
+        const int shift1 = g.d0_bits;
+        for (int i = threadIdx.x; i < nb1; i += kThreads) cnt[i] = 0u;
+        const int base = lt * kSortTile;
+        const uint32_t* kw = reinterpret_cast<const uint32_t*>(g.T_pair + base + threadIdx.x);
+        uint32_t key[kSortIpt];
+#pragma unroll
+        for (int k = 0; k < kSortIpt; ++k)
+            key[k] = base + k * kThreads + (int)threadIdx.x < g.N ? kw[2 * k * kThreads] : 0xffffffffu;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kSortIpt; ++k)
+            if (base + k * kThreads + (int)threadIdx.x < g.N)
+                atomicAdd(&cnt[((key[k] & kCellMask) >> shift1) & (uint32_t)(nb1 - 1)], 1u);
+        __syncthreads();
+        uint32_t* H1 = g.hsort + (size_t)g.sort_tiles * kSortMaxBins + (size_t)lt * kSortMaxBins;
+        for (int i = threadIdx.x; i < nb1; i += kThreads) H1[i] = cnt[i];
         __syncthreads();
     }
 }
@@ -292,11 +317,17 @@ cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cf
         return launch_kernel(cfg, k_sort_pass<true>, launch_blocks(cfg, 4), kThreads, smem, b);
 }
 
+cudaError_t launch_sort_offsets1(const Batch* d_batch, const LaunchCfg& cfg) {
+    cudaError_t e = launch_kernel(cfg, k_sort_hist, launch_blocks(cfg, 4), kThreads, 0, const_cast<Batch*>(d_batch));
+    if (e != cudaSuccess) return e;
+    return launch_sort_scan(d_batch, 1, cfg);
+}
+
 cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg) {
     cudaError_t e;
     if ((e = launch_sort_scan(d_batch, 0, cfg)) != cudaSuccess) return e;
     if ((e = launch_sort_pass(d_batch, 0, cfg)) != cudaSuccess) return e;
-    if ((e = launch_sort_scan(d_batch, 1, cfg)) != cudaSuccess) return e;
+    if ((e = launch_sort_offsets1(d_batch, cfg)) != cudaSuccess) return e;
     return launch_sort_pass(d_batch, 1, cfg);
 }
 

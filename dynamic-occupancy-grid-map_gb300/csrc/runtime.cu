@@ -275,7 +275,8 @@ cudaError_t download_status(Ctx& c) {
                            c.stream);
 }
 
-// The steady-state frame: 8 kernels; with profiling, a CUDA event before each and at the end.
+// The steady-state frame: 9 kernels in 8 stages; with profiling, a CUDA event before each
+// stage and at the end.
 cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
     LaunchCfg cfg{c.num_sms, c.stream};
     const bool prof = c.profile && !with_init;
@@ -294,7 +295,7 @@ cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
     STAGE(0, launch_predict(c.d_batch, 0, cfg));
     STAGE(1, launch_sort_scan(c.d_batch, 0, cfg));
     STAGE(2, launch_sort_pass(c.d_batch, 0, cfg));
-    STAGE(3, launch_sort_scan(c.d_batch, 1, cfg));
+    STAGE(3, launch_sort_offsets1(c.d_batch, cfg));
     STAGE(4, launch_sort_pass(c.d_batch, 1, cfg));
     STAGE(5, launch_cells(c.d_batch, cfg));
     STAGE(6, launch_newborn(c.d_batch, cfg));
@@ -501,7 +502,7 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
 
 #define ALLOC(ptr, n) if ((st = dalloc(h, &(ptr), (n))) != DOGM_OK) return cleanup(st)
     ALLOC(g.P_state, s.N); ALLOC(g.P_key, s.N);
-    ALLOC(g.T_key, s.N); ALLOC(g.T_idx, s.N);
+    ALLOC(g.T_pair, s.N);
     ALLOC(g.S_state, s.N); ALLOC(g.S_key, s.N);
     ALLOC(g.B_state, s.B); ALLOC(g.B_key, s.B); ALLOC(g.B_w, s.B);
     ALLOC(g.cells, s.C);
