@@ -49,7 +49,7 @@ def stage_bytes(N: int, B: int, C_: int, n_occ: int, n_birth_cells: int, sort_ti
         "predict": 40 * N + 4 * sort_tiles * nb0,  # state R/W 16+16, key R/W 4+4; digit counts W
         "sort_scan0": 8 * sort_tiles * nb0,      # digit counts R, offsets W
         "sort_pass0": 12 * N + 4 * sort_tiles * nb0,  # key R 4, (key, index) W 8; offsets R
-        "sort_scan1": 8 * sort_tiles * nb1,
+        "sort_scan1": 4 * N + 12 * sort_tiles * nb1,  # pass-1 digit counts: keys R, counts W; scan R/W
         "sort_pass1": 44 * N,                    # (key, index) R 8, state gather R 16, state+key W 20
         "cells": 20 * N + 112 * C_,              # key 4 + state 16 R; meas 16 + free 4 R;
                                                  # record 64 + free 4 + rho_b 4 + w 4 + meas copy 16 W
