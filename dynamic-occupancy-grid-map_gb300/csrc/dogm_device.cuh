@@ -56,20 +56,12 @@ __device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b) {
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long quantize(float w, int S) {
     // round-to-nearest-even of w * 2^S for w in [0, 2]; <= 0 or NaN -> 0, > 2 clamps to 2.
+    // Scaling by 2^S (0 <= S <= 61) is exact in float: a normal w stays normal, a denormal w
+    // only moves its bits up, and w * 2^S <= 2^62 stays finite.  One round-to-nearest-even
+    // conversion of the exact product is then the rounded integer.
     if (!(w > 0.0f)) return 0ull;
     if (w > 2.0f) w = 2.0f;
-    const uint32_t bits = __float_as_uint(w);
-    const int e = (int)(bits >> 23);
-    const uint32_t man = bits & 0x7fffffu;
-    const unsigned long long m = e ? (unsigned long long)(man | 0x800000u) : (unsigned long long)man;
-    const int sh = (e ? e - 150 : -149) + S;  // value = m * 2^(sh)
-    if (sh >= 0) return m << sh;
-    const int r = -sh;
-    if (r > 40) return 0ull;
-    const unsigned long long q = m >> r;
-    const unsigned long long rem = m & ((1ull << r) - 1ull);
-    const unsigned long long half = 1ull << (r - 1);
-    return q + ((rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull);
+    return __float2ull_rn(__fmul_rn(w, __int_as_float((127 + S) << 23)));
 }
 
 // 96-bit products of a 64-bit and a 32-bit factor (every product here is below 2^86:
