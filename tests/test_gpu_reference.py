@@ -121,7 +121,9 @@ def test_against_reference_build(dogm, oracle, pyref, scene):
             # particles (common.h:24-32): their error grows with the total weight, which is ~1 on
             # the first frame and J (thousands) after a resampling; it is never more accurate
             assert e_ours <= max(e_ref, 2e-6), "frame %d %s: reference closer to FP64" % (k, name)
-            assert e_ref <= 1e-2, "frame %d %s: reference build vs FP64 %g" % (k, name, e_ref)
+            # sanity bound that the reference build ran at all (observed up to 1.02e-2: its
+            # frame-1 input varies run to run through the Q5 race)
+            assert e_ref <= 5e-2, "frame %d %s: reference build vs FP64 %g" % (k, name, e_ref)
         occ = ok & (co["start_idx"] >= 0)
         scale = 1.0 + f64[:, 11] ** 2 + f64[:, 12] ** 2 + np.abs(f64[:, 13]) + np.abs(f64[:, 14])
         for name in MOMENT_FIELDS:
