@@ -17,7 +17,8 @@ namespace dogm_gb300 {
 // Column scan: for each digit b, O[t][b] = base(b) + sum_{t' < t} H[t'][b], in place.
 // Work item = (grid, group of 32 digits); 32 warps split the tiles into contiguous chunks.
 // ---------------------------------------------------------------------------------------
-constexpr int kScanWarps = 32;
+constexpr int kScanWarps = 32;  // one warp per lane of the transposed chunk scan
+static_assert(kScanWarps == 32, "the chunk scan transposes a 32 x 32 matrix");
 constexpr int kScanBatch = 8;
 constexpr int kScanKeep = 16;  // tiles per warp kept in registers (N up to 2M particles)
 constexpr int kCtilePer = kMaxCellTiles / (kScanWarps * 32);
@@ -135,9 +136,24 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict
         if (lane == 0) red[warp] = part;
         chunk[warp][lane] = s;
         __syncthreads();
-        uint32_t pre = lanepre - own;
-        for (int w = 0; w < kScanWarps; ++w) pre += red[w];
-        for (int w = 0; w < warp; ++w) pre += chunk[w][lane];
+        // the block's sum of the parts: one load per lane and a warp reduction
+        uint32_t base_all = red[lane];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) base_all += __shfl_xor_sync(0xffffffffu, base_all, o);
+        // the counts of this lane's digit in the chunks of the warps before this one: warp w
+        // scans digit w across the 32 chunks (one per lane; the padded rows keep the transposed
+        // reads free of bank conflicts) and writes the exclusive prefixes back in place
+        const uint32_t c = chunk[lane][warp];
+        uint32_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        __syncthreads();
+        chunk[lane][warp] = inc - c;
+        __syncthreads();
+        uint32_t pre = lanepre - own + base_all + chunk[warp][lane];
         if (b < nb) {
             if (keep) {
 #pragma unroll
