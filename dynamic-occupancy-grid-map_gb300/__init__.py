@@ -38,7 +38,7 @@ STATUS_NAMES = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "CUDA err
 # C ABI symbols declared in include/dogm_gb300.h (checked by the CPU test suite).
 ABI_SYMBOLS = [
     "dogm_default_options", "dogm_create", "dogm_destroy", "dogm_update", "dogm_update_batch", "dogm_synchronize",
-    "dogm_get_grid_cells", "dogm_get_grid_cells_device", "dogm_get_measurement_cells", "dogm_get_particles",
+    "dogm_get_grid_cells", "dogm_get_grid_cells_device", "dogm_get_grid_cells_async", "dogm_get_measurement_cells", "dogm_get_particles",
     "dogm_get_grid_size", "dogm_get_resolution", "dogm_get_position_x", "dogm_get_position_y", "dogm_get_yaw",
     "dogm_get_iteration", "dogm_get_particle_count", "dogm_get_new_born_particle_count", "dogm_particle_prediction",
     "dogm_update_pose", "dogm_update_pose_noalloc", "dogm_initialize_particles", "dogm_set_measurement_cells", "dogm_set_particles",
@@ -127,6 +127,7 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_update": ([vp, vp, f, f, f, f, i], i),
         "dogm_update_batch": ([vp, i, vp, vp, vp, vp, vp, i], i), "dogm_synchronize": ([vp], i),
         "dogm_get_grid_cells": ([vp, vp, sz], i), "dogm_get_grid_cells_device": ([vp, vp, sz], i),
+        "dogm_get_grid_cells_async": ([vp, vp, sz], i),
         "dogm_get_measurement_cells": ([vp, vp, sz], i), "dogm_get_particles": ([vp, vp, vp, vp, vp, sz], i),
         "dogm_get_grid_size": ([vp], i), "dogm_get_resolution": ([vp], f), "dogm_get_position_x": ([vp], f),
         "dogm_get_position_y": ([vp], f), "dogm_get_yaw": ([vp], f), "dogm_get_iteration": ([vp], i),
@@ -293,6 +294,15 @@ class DOGM:
     def get_grid_cells(self, out: np.ndarray | None = None) -> np.ndarray:
         out = np.empty(self.cell_count, GRID_CELL_DTYPE) if out is None else out
         check(load().dogm_get_grid_cells(self.h, _ptr(out), self.cell_count), "dogm_get_grid_cells")
+        return out
+
+    def get_grid_cells_async(self, out: np.ndarray) -> np.ndarray:
+        """Queues the copy of the current grid into `out` (GRID_CELL_DTYPE, grid_size^2 entries,
+        ideally a PinnedArray's array); it overlaps the next update and is complete after
+        synchronize()."""
+        if out.dtype != GRID_CELL_DTYPE or out.size != self.cell_count or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous GRID_CELL_DTYPE array of grid_size^2 cells")
+        check(load().dogm_get_grid_cells_async(self.h, _ptr(out), self.cell_count), "dogm_get_grid_cells_async")
         return out
 
     def get_measurement_cells(self) -> np.ndarray:

@@ -139,6 +139,14 @@ struct dogm_handle {
     dogm_dynamic_cell* dyn_out = nullptr;
     int dyn_cap = 0;
     unsigned int* dyn_scratch = nullptr;
+    // asynchronous grid readback (dogm_get_grid_cells_async), created on first use: a second
+    // cell-record buffer that the updates alternate with, a copy stream, and per buffer the
+    // event after its last queued copy (0: the primary buffer, 1: cells_alt)
+    dogm_grid_cell* cells_primary = nullptr;
+    dogm_grid_cell* cells_alt = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t frame_ready = nullptr;
+    cudaEvent_t copy_done[2] = {nullptr, nullptr};
 };
 
 namespace {
@@ -549,7 +557,29 @@ dogm_status dogm_destroy(dogm_handle* h) {
     for (void* p : {(void*)h->rp_init, (void*)h->rp_predict, (void*)h->rp_birth, (void*)h->rp_resample,
                     (void*)h->dyn_out, (void*)h->dyn_scratch})
         if (p) cudaFree(p);
+    if (h->cells_alt) cudaFree(h->desc.cells == h->cells_primary ? h->cells_alt : h->desc.cells);
+    for (cudaEvent_t e : {h->frame_ready, h->copy_done[0], h->copy_done[1]})
+        if (e) cudaEventDestroy(e);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     delete h;
+    return DOGM_OK;
+}
+
+// With asynchronous readback in use, each update writes the cell-record buffer the previous
+// update did not, after the copy last queued from it has finished (on `stream`).  Records are
+// rewritten whole every frame, so the results do not depend on the buffer.
+static dogm_status alternate_cells(dogm_handle* h, cudaStream_t stream) {
+    if (!h->cells_alt) return DOGM_OK;
+    std::swap(h->desc.cells, h->cells_alt);
+    const int b = h->desc.cells == h->cells_primary ? 0 : 1;
+    DOGM_CUDA(cudaStreamWaitEvent(stream, h->copy_done[b], 0));
+    return DOGM_OK;
+}
+
+// Makes `stream` wait for every queued asynchronous copy of the handle's cell records.
+static dogm_status wait_readback(dogm_handle* h, cudaStream_t stream) {
+    for (cudaEvent_t e : h->copy_done)
+        if (e) DOGM_CUDA(cudaStreamWaitEvent(stream, e, 0));
     return DOGM_OK;
 }
 
@@ -578,6 +608,8 @@ dogm_status dogm_update(dogm_handle* h, const dogm_measurement_cell* meas, float
     const dogm_measurement_cell* src;
     int copy;
     st = prepare_measurement(h, meas, device, c.stream, &src, &copy);
+    if (st != DOGM_OK) return st;
+    st = alternate_cells(h, c.stream);
     if (st != DOGM_OK) return st;
     const bool init = !h->first_measurement_received;
     int shifted, xm, ym;
@@ -630,6 +662,8 @@ dogm_status dogm_update_batch(dogm_handle* const* hs, int n, const dogm_measurem
         int copy;
         dogm_status st = prepare_measurement(h, meas ? meas[i] : nullptr, device, c->stream, &src, &copy);
         if (st != DOGM_OK) return st;
+        st = alternate_cells(h, c->stream);
+        if (st != DOGM_OK) return st;
         init_mask[i] = h->first_measurement_received ? 0 : 1;
         any_init |= init_mask[i] != 0;
         int shifted, xm, ym;
@@ -655,6 +689,8 @@ dogm_status dogm_update_batch(dogm_handle* const* hs, int n, const dogm_measurem
 dogm_status dogm_synchronize(dogm_handle* h) {
     if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
     DeviceGuard dg(h->device);
+    dogm_status st = wait_readback(h, h->ctx.stream);  // queued asynchronous copies finish too
+    if (st != DOGM_OK) return st;
     dogm_handle* hs[1] = {h};
     return finish_frame(h->ctx, hs, 1);
 }
@@ -666,6 +702,34 @@ dogm_status dogm_get_grid_cells(dogm_handle* h, dogm_grid_cell* host_out, size_t
     DOGM_CUDA(cudaMemcpyAsync(host_out, h->desc.cells, sizeof(dogm_grid_cell) * n, cudaMemcpyDeviceToHost,
                               h->ctx.stream));
     DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
+    return DOGM_OK;
+}
+
+dogm_status dogm_get_grid_cells_async(dogm_handle* h, dogm_grid_cell* host_out, size_t n) {
+    if (!h || !host_out) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (n != (size_t)h->C) return fail(DOGM_ERR_INVALID_ARGUMENT, "n must equal grid_size^2");
+    DeviceGuard dg(h->device);
+    if (!h->cells_alt) {
+        dogm_grid_cell* alt = nullptr;
+        dogm_status st = dalloc(h, &alt, (size_t)h->C);
+        if (st != DOGM_OK) return st;
+        h->allocations.pop_back();  // owned through cells_alt / desc.cells, freed in dogm_destroy
+        if (cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->frame_ready, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->copy_done[0], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->copy_done[1], cudaEventDisableTiming) != cudaSuccess) {
+            cudaFree(alt);
+            return fail(DOGM_ERR_CUDA, "readback stream or event creation failed");
+        }
+        h->cells_primary = h->desc.cells;
+        h->cells_alt = alt;
+    }
+    const int b = h->desc.cells == h->cells_primary ? 0 : 1;
+    DOGM_CUDA(cudaEventRecord(h->frame_ready, h->ctx.stream));
+    DOGM_CUDA(cudaStreamWaitEvent(h->copy_stream, h->frame_ready, 0));
+    DOGM_CUDA(cudaMemcpyAsync(host_out, h->desc.cells, sizeof(dogm_grid_cell) * n, cudaMemcpyDeviceToHost,
+                              h->copy_stream));
+    DOGM_CUDA(cudaEventRecord(h->copy_done[b], h->copy_stream));
     return DOGM_OK;
 }
 
@@ -1373,6 +1437,8 @@ dogm_status slot_launch(BatchSlot* s, const SlotFrame* fr, int n) {
         const dogm_measurement_cell* src;
         int copy;
         st = prepare_measurement(h, fr[i].meas, fr[i].device, c.stream, &src, &copy);
+        if (st != DOGM_OK) return st;
+        st = alternate_cells(h, c.stream);
         if (st != DOGM_OK) return st;
         init_mask[i] = h->first_measurement_received ? 0 : 1;
         any_init |= init_mask[i] != 0;

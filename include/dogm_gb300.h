@@ -115,7 +115,8 @@ dogm_status dogm_update_batch(dogm_handle* const* hs, int n, const dogm_measurem
                               const float* new_x, const float* new_y, const float* new_yaw, const float* dt,
                               int device);
 
-/* Waits for all work queued on the handle's stream (only needed with sync_each_update=0). */
+/* Waits for all work queued on the handle's stream (only needed with sync_each_update=0) and
+ * for the copies queued by dogm_get_grid_cells_async. */
 dogm_status dogm_synchronize(dogm_handle* h);
 
 /* ---- readback (dogm/src/dogm.cu:133-159) ---------------------------------------------- */
@@ -124,6 +125,14 @@ dogm_status dogm_synchronize(dogm_handle* h);
 dogm_status dogm_get_grid_cells(dogm_handle* h, dogm_grid_cell* host_out, size_t n);
 /* Same into a device buffer of the handle's device (no host round trip). */
 dogm_status dogm_get_grid_cells_device(dogm_handle* h, dogm_grid_cell* dev_out, size_t n);
+/* Queues the copy of the current grid (n == grid_size^2 cells) to host_out on a copy stream of
+ * the handle and returns: the copy overlaps the next update's measurement copy and kernels.
+ * From the first call on the handle keeps a second cell-record buffer (C x 64 bytes) and its
+ * updates alternate between the two, each waiting for the copy last queued from the buffer it
+ * writes; results are bit-identical to the synchronous path.  host_out holds the grid once
+ * dogm_synchronize(h) returns; it must stay valid until then and should be pinned
+ * (dogm_host_alloc) for the copy to run asynchronously. */
+dogm_status dogm_get_grid_cells_async(dogm_handle* h, dogm_grid_cell* host_out, size_t n);
 
 /* Replaces DOGM::getMeasurementCells. */
 dogm_status dogm_get_measurement_cells(dogm_handle* h, dogm_measurement_cell* host_out, size_t n);
