@@ -391,6 +391,10 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
     __shared__ unsigned long long red[2 * (kThreads / 32)];
     __shared__ int s_bnd[kCellTile + 1];  // s_bnd[c]: first slot of cell c of the tile; [kCellTile]: end
     __shared__ int s_nuA[kCellTile];
+    // the tile's cells that receive newborns, compacted so that all threads share their work
+    __shared__ uint16_t s_list[kCellTile];
+    __shared__ float2 s_bp[kCellTile];
+    __shared__ int s_wcnt[kThreads / 32];
     const int total = batch_total(bt, kStBirth);
     const int lane = threadIdx.x & 31;
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
@@ -400,7 +404,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
         const int base = lt * kCellTile;
         const unsigned long long T = g.fs->qb_total;
         unsigned long long q[kCellIpt];
-        float rb[kCellIpt], pA[kCellIpt];
+        float rb[kCellIpt];
         float2 bp[kCellIpt];
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
@@ -413,7 +417,6 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
             rb[j] = bp[j].x;
-            pA[j] = bp[j].y;
             q[j] = quantize(rb[j], g.q_shift);
             v += q[j];
         }
@@ -433,30 +436,59 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
             s_bnd[threadIdx.x * kCellIpt + j] = bnd[j];
         }
         if (threadIdx.x == kThreads - 1) s_bnd[kCellTile] = bnd[kCellIpt];
+        // cells with newborns: count per thread, exclusive scan over the block
+        uint32_t mask = 0u;
+#pragma unroll
+        for (int j = 0; j < kCellIpt; ++j)
+            if (bnd[j + 1] > bnd[j] && base + (int)threadIdx.x * kCellIpt + j < g.C) mask |= 1u << j;
+        const int cnt = __popc(mask);
+        int wpos = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, wpos, o);
+            if (lane >= o) wpos += y;
+        }
+        if (lane == 31) s_wcnt[threadIdx.x >> 5] = wpos;
+        __syncthreads();
+        int pos = wpos - cnt, n_list = 0;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) {
+            const int c = s_wcnt[w];
+            if (w < (int)(threadIdx.x >> 5)) pos += c;
+            n_list += c;
+        }
+#pragma unroll
+        for (int j = 0; j < kCellIpt; ++j)
+            if (mask & (1u << j)) {
+                s_list[pos] = (uint16_t)(threadIdx.x * kCellIpt + j);
+                s_bp[pos] = bp[j];
+                ++pos;
+            }
         __syncthreads();
         const int lo_tile = s_bnd[0], hi_tile = s_bnd[kCellTile];
         const long long N = g.N;
         const long long rt0 = (N + lo_tile) / kResTile;
         unsigned long long racc[kRunTiles] = {0ull, 0ull, 0ull, 0ull};
         unsigned long long jq = 0ull;
-#pragma unroll
-        for (int j = 0; j < kCellIpt; ++j) {
-            const int k = base + threadIdx.x * kCellIpt + j;
-            const int nnew = bnd[j + 1] - bnd[j];
-            if (nnew > 0 && k < g.C) {
-                const int nuA = (int)roundf(__fmul_rn((float)nnew, pA[j]));
-                const int nuUA = nnew - nuA;
-                const float wA = nuA > 0 ? __fdiv_rn(__fmul_rn(pA[j], rb[j]), (float)nuA) : 0.0f;
-                const float wUA = nuUA > 0 ? __fdiv_rn(__fmul_rn(__fsub_rn(1.0f, pA[j]), rb[j]), (float)nuUA) : 0.0f;
-                g.cells[k].w_A = wA;
-                g.cells[k].w_UA = wUA;
-                s_nuA[threadIdx.x * kCellIpt + j] = nuA;
-                const int nA = min(max(nuA, 0), nnew);
-                const unsigned long long qA = quantize(wA, g.q_shift), qU = quantize(wUA, g.q_shift);
-                jq += (unsigned long long)nA * qA + (unsigned long long)(nnew - nA) * qU;
-                add_joint_range(racc, rt0, g.res_sum, N + bnd[j], N + bnd[j] + nA, qA);
-                add_joint_range(racc, rt0, g.res_sum, N + bnd[j] + nA, N + bnd[j + 1], qU);
-            }
+        // w_A / w_UA of each listed cell (init_new_particles.cu:145-153) and its joint weights
+        for (int i = threadIdx.x; i < n_list; i += kThreads) {
+            const int lc = s_list[i];
+            const int k = base + lc;
+            const int b0 = s_bnd[lc], b1 = s_bnd[lc + 1];
+            const int nnew = b1 - b0;
+            const float rbj = s_bp[i].x, pAj = s_bp[i].y;
+            const int nuA = (int)roundf(__fmul_rn((float)nnew, pAj));
+            const int nuUA = nnew - nuA;
+            const float wA = nuA > 0 ? __fdiv_rn(__fmul_rn(pAj, rbj), (float)nuA) : 0.0f;
+            const float wUA = nuUA > 0 ? __fdiv_rn(__fmul_rn(__fsub_rn(1.0f, pAj), rbj), (float)nuUA) : 0.0f;
+            g.cells[k].w_A = wA;
+            g.cells[k].w_UA = wUA;
+            s_nuA[lc] = nuA;
+            const int nA = min(max(nuA, 0), nnew);
+            const unsigned long long qA = quantize(wA, g.q_shift), qU = quantize(wUA, g.q_shift);
+            jq += (unsigned long long)nA * qA + (unsigned long long)(nnew - nA) * qU;
+            add_joint_range(racc, rt0, g.res_sum, N + b0, N + b0 + nA, qA);
+            add_joint_range(racc, rt0, g.res_sum, N + b0 + nA, N + b1, qU);
         }
 #pragma unroll
         for (int i = 0; i < kRunTiles; ++i) {
