@@ -39,6 +39,7 @@ struct HeavyRef {
     int item, first, end;  // a joint item with more copies than one thread writes
 };
 constexpr int kOwnCopies = 8;
+constexpr int kWarpCopies = 256;  // output slots a warp writes together (8 stores of 32)
 constexpr int kMaxHeavy = 256;
 
 struct ResSmem {
@@ -177,15 +178,37 @@ __global__ void __launch_bounds__(kThreads, 6) k_resample(Batch* __restrict__ bt
         if (threadIdx.x == kThreads - 1) sm.lw[pad_idx(kResTile)] = (uint32_t)lo_s;
         __syncthreads();
 
-        // ---- 3: copies, consecutive items on consecutive lanes (coalesced stores) --------
+        // ---- 3: copies.  The 32 consecutive items of a warp own one contiguous range of
+        // output slots; a warp whose range is short writes it together, 32 consecutive slots
+        // per store, each lane finding the owner of its slot (the last lane whose first slot
+        // is <= it; items without copies share their first slot with the next item).  A warp
+        // with a long range writes per item, and items with many copies go to the block.
         float4* __restrict__ P_state = g.P_state;
         uint32_t* __restrict__ P_key = g.P_key;
         int* __restrict__ dbg_src = g.dbg_src;
+        const int lane = threadIdx.x & 31;
 #pragma unroll 2
         for (int r = 0; r < kResIpt; ++r) {
             const int j = r * kThreads + threadIdx.x;
             const int first = (int)sm.lw[pad_idx(j)], end = (int)sm.lw[pad_idx(j + 1)];
-            if (end > first) {
+            const int wf = __shfl_sync(0xffffffffu, first, 0), we = __shfl_sync(0xffffffffu, end, 31);
+            if (we - wf <= kWarpCopies) {  // warp-uniform
+                const int j0 = j - lane;
+                for (int s0 = wf; s0 < we; s0 += 32) {
+                    const int slot = s0 + lane;
+                    int owner = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const int f = __shfl_sync(0xffffffffu, first, owner + step);
+                        if (f <= slot) owner += step;
+                    }
+                    if (slot < we) {
+                        P_state[slot] = sm.st[j0 + owner];
+                        P_key[slot] = sm.kw[j0 + owner];
+                        if (dbg_src) dbg_src[slot] = base + j0 + owner;
+                    }
+                }
+            } else if (end > first) {
                 bool own = end - first <= kOwnCopies;
                 if (!own) {
                     const int h = atomicAdd(&sm.nheavy, 1);
