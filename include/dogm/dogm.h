@@ -81,6 +81,19 @@ public:
         return cells;
     }
 
+    // Not in the reference: queues the copy of the current grid into `out` (grid_size^2 cells,
+    // pinned host memory for a real overlap) and returns; the copy overlaps the next
+    // updateGrid.  `out` holds the grid once synchronize() returns.
+    void getGridCellsAsync(GridCell* out) const
+    {
+        const size_t n = static_cast<size_t>(getGridSize()) * static_cast<size_t>(getGridSize());
+        checkStatus(dogm_get_grid_cells_async(handle, reinterpret_cast<dogm_grid_cell*>(out), n),
+                    "DOGM::getGridCellsAsync");
+    }
+
+    // Not in the reference: waits for queued updates and asynchronous copies.
+    void synchronize() const { checkStatus(dogm_synchronize(handle), "DOGM::synchronize"); }
+
     // dogm.h:95
     std::vector<MeasurementCell> getMeasurementCells() const
     {
