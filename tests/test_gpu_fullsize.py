@@ -1,0 +1,65 @@
+"""GPU: the benchmark's full size (120 m at 0.1 m = 1200^2 cells, 2e6 persistent + 2e5 newborn
+particles, ego motion with yaw) against the FP32 oracle with the GPU's draws replayed —
+keys, permutation, ranges, masses, weights, newborns and resample indices bit-exact, moments
+within the stated tolerance — and, with the in-kernel Philox draws, the size-independent
+properties: the sorted cell keys are non-decreasing, the cell ranges partition the sorted
+particles, every particle lies in the grid's cells, masses are valid, and two handles with
+the same seed agree bit for bit."""
+import numpy as np
+import pytest
+
+from test_gpu_parity import run_pair
+
+pytestmark = pytest.mark.gpu
+
+
+def large_scene(scene, frames):
+    cfg = dict(scene.CONFIGS["large"])
+    sc = scene.Scene(cfg, seed=1)
+    return cfg, [sc.frame(k) for k in range(frames)]
+
+
+def test_full_size_replay_bit_exact(dogm, oracle, scene):
+    cfg, frames = large_scene(scene, 3)
+    p = dogm.make_params(**scene.params_dict(cfg))
+    run_pair(dogm, oracle, scene, p, len(frames), lambda k, gs: frames[k][0], lambda k: (frames[k][1], frames[k][2]))
+
+
+def test_full_size_properties_and_determinism(dogm, scene):
+    cfg, frames = large_scene(scene, 4)
+    p = dogm.make_params(**scene.params_dict(cfg))
+    a = dogm.DOGM(p, seed=21)
+    b = dogm.DOGM(p, seed=21)
+    a.debug_enable(True)
+    for m, x, y, yaw in frames:
+        a.update_grid(m, x, y, yaw, 0.1)
+        b.update_grid(m, x, y, yaw, 0.1)
+        cells = a.get_grid_cells()
+        assert cells.tobytes() == b.get_grid_cells().tobytes()
+        gs, n = a.grid_size, a.particle_count
+        assert gs == 1200 and cells.size == gs * gs
+        dbg = a.debug_export()
+        key = dbg["sorted_cell"]
+        assert key.size == n and np.all(np.diff(key) >= 0) and key.min() >= 0 and key.max() < gs * gs
+        # ranges: occupied cells hold exactly the sorted positions with their key, in order
+        occ = cells["start_idx"] >= 0
+        st, en = cells["start_idx"][occ], cells["end_idx"][occ]
+        assert np.all(en >= st) and st[0] == 0 and en[-1] == n - 1
+        assert np.array_equal(st[1:], en[:-1] + 1)
+        assert np.array_equal(np.flatnonzero(occ), key[st])
+        assert np.array_equal(np.bincount(key, minlength=gs * gs)[occ], en - st + 1)
+        # masses
+        # (rho_p = occ - rho_b is a float difference, as in mass_update.cu:87-88, so the
+        # persistent mass may sit a rounding step below zero)
+        for f in ("occ_mass", "free_mass", "pers_occ_mass", "new_born_occ_mass"):
+            assert np.all(cells[f] >= -1e-6) and np.all(cells[f] <= 1.0 + 1e-6), (f, cells[f].min(), cells[f].max())
+        assert np.all(cells["occ_mass"] + cells["free_mass"] <= 1.0 + 1e-5)
+        assert np.all(np.abs(cells["pers_occ_mass"] + cells["new_born_occ_mass"] - cells["occ_mass"]) <= 1e-5)
+        # resampling: every output slot comes from an existing joint particle
+        src = dbg["resample_src"]
+        assert src.size == n and src.min() >= 0 and src.max() < n + dbg["n_birth"]
+        assert np.all(np.diff(src) >= 0)  # systematic resampling keeps the joint order
+    pa, pb = a.get_particles(), b.get_particles()
+    assert all(np.array_equal(pa[f], pb[f]) for f in pa)
+    a.close()
+    b.close()
