@@ -237,7 +237,8 @@ dogm_status dogm_device_alloc(void** ptr, size_t bytes);
 dogm_status dogm_device_free(void* ptr);
 dogm_status dogm_memcpy(void* dst, const void* src, size_t bytes, int kind /* cudaMemcpyKind */);
 
-/* Device bytes a handle with these parameters holds (admission control). */
+/* Device bytes a handle with these parameters holds (admission control); a handle that uses
+ * dogm_get_grid_cells_async holds 64 * grid_size^2 bytes more. */
 size_t dogm_state_bytes(const dogm_params* params);
 
 /* ---- serving loop ----------------------------------------------------------------------
