@@ -718,6 +718,9 @@ dogm_status dogm_get_grid_cells_async(dogm_handle* h, dogm_grid_cell* host_out, 
             cudaEventCreateWithFlags(&h->frame_ready, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->copy_done[0], cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&h->copy_done[1], cudaEventDisableTiming) != cudaSuccess) {
+            for (cudaEvent_t* e : {&h->frame_ready, &h->copy_done[0], &h->copy_done[1]})
+                if (*e) { cudaEventDestroy(*e); *e = nullptr; }
+            if (h->copy_stream) { cudaStreamDestroy(h->copy_stream); h->copy_stream = nullptr; }
             cudaFree(alt);
             return fail(DOGM_ERR_CUDA, "readback stream or event creation failed");
         }
