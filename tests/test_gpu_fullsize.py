@@ -1,5 +1,6 @@
 """GPU: the benchmark's full size (120 m at 0.1 m = 1200^2 cells, 2e6 persistent + 2e5 newborn
-particles, ego motion with yaw) against the FP32 oracle with the GPU's draws replayed —
+particles, ego motion with yaw) — and the small (250^2, 3e5 + 3e4) and precision (2048^2,
+8e6 + 8e5) workloads — against the FP32 oracle with the GPU's draws replayed —
 keys, permutation, ranges, masses, weights, newborns and resample indices bit-exact, moments
 within the stated tolerance — and, with the in-kernel Philox draws, the size-independent
 properties: the sorted cell keys are non-decreasing, the cell ranges partition the sorted
@@ -23,6 +24,15 @@ def test_full_size_replay_bit_exact(dogm, oracle, scene):
     cfg, frames = large_scene(scene, 3)
     p = dogm.make_params(**scene.params_dict(cfg))
     run_pair(dogm, oracle, scene, p, len(frames), lambda k, gs: frames[k][0], lambda k: (frames[k][1], frames[k][2]))
+
+
+@pytest.mark.parametrize("workload,frames", [("small", 8), ("precision", 2)])
+def test_other_workloads_replay_bit_exact(dogm, oracle, scene, workload, frames):
+    cfg = dict(scene.CONFIGS[workload])
+    sc = scene.Scene(cfg, seed=2)
+    fr = [sc.frame(k) for k in range(frames)]
+    p = dogm.make_params(**scene.params_dict(cfg))
+    run_pair(dogm, oracle, scene, p, frames, lambda k, gs: fr[k][0], lambda k: (fr[k][1], fr[k][2]))
 
 
 def test_full_size_properties_and_determinism(dogm, scene):
