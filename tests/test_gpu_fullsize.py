@@ -73,3 +73,29 @@ def test_full_size_properties_and_determinism(dogm, scene):
     assert all(np.array_equal(pa[f], pb[f]) for f in pa)
     a.close()
     b.close()
+
+
+def test_batched_workload_alone_equals_batch(dogm, scene):
+    """The batched workload's 64 uneven grids (sides log-uniform in [128, 1024] cells, 1.5
+    particles per cell, 10 % newborns) updated in one launch per stage give, grid by grid, the
+    bits of the same grids updated alone."""
+    cfgs = scene.stream_configs(64, seed=2)
+    frames = []
+    for i, c in enumerate(cfgs):
+        sc = scene.Scene(c, seed=2000 + i)
+        frames.append([sc.frame(k)[0] for k in range(2)])
+    params = [dogm.make_params(**scene.params_dict(c)) for c in cfgs]
+    alone = [dogm.DOGM(p, seed=100 + i, stream_id=i) for i, p in enumerate(params)]
+    batch = [dogm.DOGM(p, seed=100 + i, stream_id=i) for i, p in enumerate(params)]
+    zeros = [0.0] * len(cfgs)
+    for k in range(2):
+        for g, f in zip(alone, frames):
+            g.update_grid(f[k], 0.0, 0.0, 0.0, 0.1)
+        dogm.update_batch(batch, [f[k] for f in frames], zeros, zeros, zeros, [0.1] * len(cfgs))
+        for i, (a, b) in enumerate(zip(alone, batch)):
+            assert a.get_grid_cells().tobytes() == b.get_grid_cells().tobytes(), "grid %d frame %d" % (i, k)
+    for a, b in zip(alone, batch):
+        pa, pb = a.get_particles(), b.get_particles()
+        assert all(np.array_equal(pa[f], pb[f]) for f in pa)
+        a.close()
+        b.close()
