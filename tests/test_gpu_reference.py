@@ -118,6 +118,13 @@ def test_against_reference_build(dogm, oracle, pyref, scene, size, res, n, b):
         # ranges of every cell between its two keys (up to a grid row): > 99.5 % of the cells
         # agree at 256^2 / 1.5e5 particles, 96 % at 1200^2 / 2e6
         assert ok.mean() > (0.995 if gs < 1000 else 0.9)
+        # the outermost ring of cells holds the particles just outside the grid (keys clamped,
+        # weight 0, predict.cu:41-48); a particle within rounding of the edge is in the grid in
+        # one precision and out in the other, which moves a light cell's newborn mass by half its
+        # occupancy with the range unchanged, so the ring is left out of the FP64 comparison
+        inner = np.zeros((gs, gs), bool)
+        inner[1:-1, 1:-1] = True
+        ok &= inner.ravel()
         names = dogm.GRID_CELL_FIELDS
         for name in MASS_FIELDS:
             j = names.index(name)
