@@ -98,7 +98,7 @@ struct CellSmem {
     Run wagg[kCellThreads / 32];  // each warp's run, then (wpre) the runs before each warp
     Run wpre[kCellThreads / 32];
     unsigned long long red[kCellThreads / 32], red2[kCellThreads / 32];
-    int tile;
+    int tiles[2];  // the block's current tile and the one claimed for the next iteration
 };
 static_assert(offsetof(CellSmem, meas) % 16 == 0, "16-byte cp.async destination");
 static_assert(offsetof(CellSmem, stage) % 16 == 0, "16-byte staged records");
@@ -163,9 +163,14 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             for (int i = tid; i < g.tiles[kStCell]; i += stride) g.ctile_cnt[i] = 0u;
         }
     }
-    for (;;) {
-        const int t = claim_tile(bt, kStCell, &sm.tile);
+    // tiles are claimed one ahead: thread 0 takes the next tile while the block works on this
+    // one, so a claim costs no barrier of its own (the body's barriers publish it)
+    if (threadIdx.x == 0) sm.tiles[0] = (int)atomicAdd(&bt->counters[kStCell], 1u);
+    __syncthreads();
+    for (int it = 0;; it ^= 1) {
+        const int t = sm.tiles[it];
         if (t >= total) break;
+        if (threadIdx.x == 0) sm.tiles[it ^ 1] = (int)atomicAdd(&bt->counters[kStCell], 1u);
         const int gi = grid_of_tile(bt, kStCell, t);
         const GridDesc& g = bt->g[gi];
         const int lt = (int)g.ctile_order[t - bt->prefix[gi][kStCell]];  // full tiles first
