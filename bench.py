@@ -432,7 +432,7 @@ def run_batched(dogm, scene, n_streams: int = 64, rounds: int = 30, warm: int = 
 
 
 def run_serving(dogm, scene, n_streams: int = 200, rate_hz: float = 10.0, seconds: float = 10.0,
-                saturate_frames: int = 8, budget: int = 150 * 10**9) -> dict:
+                saturate_frames: int = 24, budget: int = 150 * 10**9) -> dict:
     """Serving: n_streams sensor streams with Poisson frame arrivals (rate_hz each) submitted
     to dogm_server_* under an HBM budget, in batched (continuous batching) and per-stream
     (one dogm_update per frame) mode.  Latency = result ready minus submission; measurement
