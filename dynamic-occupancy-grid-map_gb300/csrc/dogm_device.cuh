@@ -204,8 +204,8 @@ __device__ __forceinline__ int grid_of_tile(const Batch* bt, int stage, int t) {
     return lo;
 }
 
-// Dynamic tile claim (tiles are taken in increasing order, which keeps decoupled
-// look-back deadlock free).  Every thread of the block gets the same tile.
+// Dynamic tile claim: the next index of the stage's work counter (reset with every frame's
+// descriptors).  Every thread of the block gets the same tile.
 __device__ __forceinline__ int claim_tile(Batch* bt, int stage, int* smem_slot) {
     if (threadIdx.x == 0) *smem_slot = (int)atomicAdd(&bt->counters[stage], 1u);
     __syncthreads();

@@ -44,7 +44,7 @@ constexpr uint32_t kAssocBit = 1u << 31;
 // Philox counter word 2: which draw family.
 enum DrawStage : uint32_t { kDrawInit = 1, kDrawPredict = 2, kDrawBirth = 3, kDrawResample = 4 };
 
-// Stages that claim tiles from a work counter (look-back ordering) or iterate statically.
+// Stages of the update; each has a tile count per grid and a work counter for dynamic claims.
 enum Stage : int {
     kStPredict = 0, kStScan0, kStSort0, kStScan1, kStSort1, kStCell, kStBirth, kStResample, kStInitScan,
     kStInitExpand, kNumStages
@@ -109,7 +109,7 @@ struct GridDesc {
     // replay inputs (NULL: Philox) and debug outputs (NULL: off)
     const float2* rp_init; const float4* rp_predict; const float2* rp_birth; const unsigned long long* rp_resample;
     int* dbg_perm; int* dbg_src;
-    // tiles per stage (sort_tiles sizes the look-back arrays)
+    // tiles per stage (sort_tiles sizes the per-tile digit counts)
     int tiles[kNumStages];
     int sort_tiles;
     int pad1;

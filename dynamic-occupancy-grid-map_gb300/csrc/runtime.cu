@@ -382,7 +382,7 @@ dogm_status finish_frame(Ctx& c, dogm_handle* const* hs, int n) {
     c.h_status[0] = c.h_status[1] = 0;
     if (st & kStatusTimeout) {
         for (int i = 0; i < n; ++i) hs[i]->need_clear = true;
-        return fail(DOGM_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up (look-back predecessor never published)");
+        return fail(DOGM_ERR_DEVICE_TIMEOUT, "a bounded device-side wait gave up");
     }
     if (st & kStatusBounds) {
         for (int i = 0; i < n; ++i) hs[i]->need_clear = true;
