@@ -37,6 +37,8 @@ PKG = "dynamic-occupancy-grid-map_gb300"
 
 METRIC = "ms/update and HBM GB/s at 2M particles/1.44M cells; batched frames/s, p50/p99"
 WORKLOAD = "large"
+WORKLOAD_DESC = ("large: 120 x 120 m at 0.1 m (1200^2 = 1.44e6 cells), 2e6 persistent + 2e5 newborn particles, "
+                 "ego 10 m/s")
 # Per-unit algorithmic bytes of the whole update (compulsory traffic of a single-read,
 # single-write pipeline): 152 B per particle, 29 B per newborn, 108 B per cell.
 ALG_PER_PARTICLE, ALG_PER_NEWBORN, ALG_PER_CELL = 152, 29, 108
@@ -68,10 +70,33 @@ def load_cudart():
             lib.cudaEventRecord.argtypes = [C.c_void_p, C.c_void_p]
             lib.cudaEventSynchronize.argtypes = [C.c_void_p]
             lib.cudaEventElapsedTime.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+            lib.cudaMalloc.argtypes = [C.c_void_p, C.c_size_t]
+            lib.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+            lib.cudaFree.argtypes = [C.c_void_p]
             return lib
         except OSError:
             continue
     raise RuntimeError("libcudart not found")
+
+
+class CudartBuffer:
+    """Device buffer through libcudart alone (the reference arm maps nothing of this library)."""
+
+    def __init__(self, rt, nbytes: int):
+        self.rt, self.nbytes = rt, int(nbytes)
+        p = C.c_void_p()
+        assert rt.cudaMalloc(C.byref(p), C.c_size_t(self.nbytes)) == 0, "cudaMalloc"
+        self.ptr = p.value
+
+    def upload(self, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr)
+        assert a.nbytes <= self.nbytes
+        assert self.rt.cudaMemcpy(C.c_void_p(self.ptr), C.c_void_p(a.ctypes.data), C.c_size_t(a.nbytes), 1) == 0
+
+    def free(self) -> None:
+        if self.ptr:
+            self.rt.cudaFree(C.c_void_p(self.ptr))
+            self.ptr = 0
 
 
 class Events:
@@ -114,6 +139,10 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the timed region starts once the sampler is delivering
+            t_end = time.perf_counter() + 5.0
+            while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
 
@@ -145,6 +174,17 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peak_gbs() -> tuple[float, str]:
+    """HBM copy bandwidth of this GPU pool: the measured figure when the pool's measurement
+    file is present, else the earlier GB300 measurement of 6.8 TB/s."""
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        return float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
 
 
 def make_frames(count: int, seed: int = 0):
@@ -229,20 +269,46 @@ def run_gb300(args, rank: int, world: int):
         g.update_grid(dbufs[fr(k)].ptr, x, y, yaw, 0.1, device=True)
     g.synchronize()
 
+    # the timed region: R back-to-back blocks of the same K steps, R chosen so that the region
+    # lasts at least --min-seconds (the clock sampler then sees it); value = mean per update
+    def timed_block(r):
+        # block r continues the forth-and-back frame sequence, so the ego keeps moving
+        for k in range(t0_ + r * K, t0_ + (r + 1) * K):
+            m, x, y, yaw = frames[fr(k)]
+            g.update_grid(dbufs[fr(k)].ptr, x, y, yaw, 0.1, device=True)
+
+    a, b_ = ev.new(), ev.new()
+    ev.record(a)
+    timed_block(0)
+    ev.record(b_)
+    block_ms = reduce_max(ev.elapsed(a, b_), world)
+    repeats = max(1, int(np.ceil(args.min_seconds * 1e3 / max(block_ms, 1e-3))))
+    g.synchronize()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")) if world > 1 else 0)
-    barrier(world)
     clocks.start()
+    barrier(world)
     e0, e1 = ev.new(), ev.new()
+    wall0 = time.perf_counter()
     ev.record(e0)
-    for k in range(t0_, t0_ + K):
-        m, x, y, yaw = frames[fr(k)]
-        g.update_grid(dbufs[fr(k)].ptr, x, y, yaw, 0.1, device=True)
+    for r in range(repeats):
+        timed_block(1 + r)
     ev.record(e1)
     total_ms = ev.elapsed(e0, e1)
+    wall_s = time.perf_counter() - wall0
     g.synchronize()
     clk = clocks.stop()
-    launches = g.last_launch_count() * K
+    launches = g.last_launch_count() * K * repeats
     total_ms = reduce_max(total_ms, world)
+
+    # synchronous updates, each waited for on the host like the reference's updateGrid
+    # (dogm.cu:130): host wall clock per update, measurement grids in HBM
+    sync_ms = []
+    for k in range(e0_, e0_ + min(K, 100)):
+        m, x, y, yaw = frames[fr(k)]
+        w0 = time.perf_counter()
+        g.update_grid(dbufs[fr(k)].ptr, x, y, yaw, 0.1, device=True)
+        g.synchronize()
+        sync_ms.append((time.perf_counter() - w0) * 1e3)
 
     # end to end through the C ABI with host buffers (pinned), grid read back every step
     pins = {}
@@ -303,36 +369,33 @@ def run_gb300(args, rank: int, world: int):
     sort_tiles = -(-N // 4096)
     sb = stage_bytes(N, B, C_, n_occ, n_bcells, sort_tiles, 1 << d0, 1 << (bits - d0))
     dom = max(stages, key=lambda k: stages[k])
-    peaks = {}
-    try:
-        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    peak, peak_src = peak_gbs()
     achieved = sb[dom] / (stages[dom] * 1e-3) / 1e9
-    traffic = read_traffic(dom)
 
-
-    ms = total_ms / K / world
+    ms = total_ms / (K * repeats)
     alg = ALG_PER_PARTICLE * N + ALG_PER_NEWBORN * B + ALG_PER_CELL * C_
     line = {
         "metric": METRIC, "value": round(ms, 4), "unit": "ms/update", "n_gpus": world, "steps": K, "warmup": W,
-        "ms_per_step": round(total_ms / K, 4), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "timed_region": {"repeats_of_k_steps": repeats, "updates": K * repeats, "device_s": round(total_ms / 1e3, 3),
+                         "host_wall_s": round(wall_s, 3)},
         "dtype": "f32", "data": "synthetic (seeded scene: 40 vehicles + 30 pedestrians, 2160-beam lidar, "
                                 "inverse sensor model; no public dataset exists for this workload)",
-        "config": {"workload": "large: 120 x 120 m at 0.1 m (1200^2 = 1.44e6 cells), 2e6 persistent + 2e5 newborn "
-                               "particles, ego 10 m/s", "cells": C_, "particles": N, "newborn": B,
+        "config": {"workload": WORKLOAD_DESC, "cells": C_, "particles": N, "newborn": B,
                    "l2": "inputs larger than L2 (per-update working set > 300 MB vs 129 MB L2); no flush",
                    "parallelism": "replicas" if world > 1 else "single",
                    "autotune": tune.as_dict() if tune is not None else "off"},
         "hbm_gbs_whole_update": round(alg / (ms * 1e-3) / 1e9, 1),
         "updates_per_s": round(1e3 / ms, 1),
+        "sync_update_ms": {"median": round(statistics.median(sync_ms), 4), "mean": round(statistics.fmean(sync_ms), 4),
+                           "updates": len(sync_ms),
+                           "method": "host wall clock around one update and its synchronisation (as the reference's "
+                                     "synchronous updateGrid), measurement grid in HBM"},
         "stage_ms": {k: round(v, 4) for k, v in stages.items()},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 3), "peak_source": peak_src, "traffic": traffic,
-                     "algorithmic_bytes": sb[dom]},
+                     "frac": round(achieved / peak, 3), "peak_source": peak_src, "traffic": None,
+                     "algorithmic_bytes": sb[dom],
+                     "traffic_note": "DRAM bytes come from a separate ncu capture, not from this run"},
         "e2e": {"value": round(e2e_ms / K / world, 4), "unit": "ms/update", "h2d_bytes_per_step": C_ * 16,
                 "d2h_bytes_per_step": C_ * 64, "readback": "asynchronous (dogm_get_grid_cells_async)",
                 "sync_readback_ms": round(e2e_sync_ms / K / world, 4)},
@@ -386,9 +449,11 @@ def _stream_pool(dogm, scene, n: int, seed: int, pinned: bool):
 
 def run_batched(dogm, scene, n_streams: int = 64, rounds: int = 30, warm: int = 3) -> dict:
     """Batched uneven grids: n_streams independent grids updated per frame by one launch per
-    stage (dogm_update_batch, CUDA graph) against one dogm_update per grid on its own CUDA
-    stream; measurement grids resident in HBM; host wall clock over `rounds` frames of all
-    grids (synchronised at both ends)."""
+    stage (dogm_update_batch, CUDA graph) against two per-stream baselines: one dogm_update per
+    grid on its own CUDA stream as a CUDA graph launch with no host wait between grids (the
+    strongest per-stream form), and per-stream plain launches (every kernel launched one by one,
+    each update waited for, as the reference's updateGrid).  Measurement grids resident in HBM;
+    host wall clock over `rounds` frames of all grids (synchronised at both ends)."""
     params, cells, bufs, _ = _stream_pool(dogm, scene, n_streams, seed=2, pinned=False)
     grids = [dogm.DOGM(p, seed=1000 + i, stream_id=i, sync_each_update=False) for i, p in enumerate(params)]
     zeros = [0.0] * n_streams
@@ -398,16 +463,24 @@ def run_batched(dogm, scene, n_streams: int = 64, rounds: int = 30, warm: int = 
         dogm.update_batch(grids, [bufs[i][r % 2].ptr for i in range(n_streams)], zeros, zeros, zeros, dts,
                           device=True)
 
-    def plain(r):
+    def per_stream_graph(r):
         for i, g in enumerate(grids):
             g.update_grid(bufs[i][r % 2].ptr, 0.0, 0.0, 0.0, 0.1, device=True)
+
+    def per_stream_plain(r):
+        for i, g in enumerate(grids):
+            g.update_grid(bufs[i][r % 2].ptr, 0.0, 0.0, 0.0, 0.1, device=True)
+            g.synchronize()
 
     def sync():
         for g in grids:
             g.synchronize()
 
     out = {}
-    for name, step in (("batched", batched), ("per_stream", plain)):
+    for name, step in (("batched", batched), ("per_stream_graph", per_stream_graph),
+                       ("per_stream_plain", per_stream_plain)):
+        for g in grids:
+            g.set_launch_mode(plain=(name == "per_stream_plain"))
         for r in range(warm):
             step(r)
         sync()
@@ -424,11 +497,20 @@ def run_batched(dogm, scene, n_streams: int = 64, rounds: int = 30, warm: int = 
             d.free()
     total_cells = sum(cells)
     total_particles = sum(p.particle_count for p in params)
-    return {"frames_per_s": round(out["batched"], 1), "per_stream_frames_per_s": round(out["per_stream"], 1),
-            "speedup": round(out["batched"] / out["per_stream"], 2), "streams": n_streams, "rounds": rounds,
-            "cells": total_cells, "particles": total_particles,
+    newborn = sum(p.new_born_particle_count for p in params)
+    alg = ALG_PER_PARTICLE * total_particles + ALG_PER_NEWBORN * newborn + ALG_PER_CELL * total_cells
+    peak = peak_gbs()[0]
+    gbs = alg * out["batched"] / n_streams / 1e9
+    return {"frames_per_s": round(out["batched"], 1),
+            "per_stream_graph_frames_per_s": round(out["per_stream_graph"], 1),
+            "per_stream_plain_frames_per_s": round(out["per_stream_plain"], 1),
+            "speedup_vs_per_stream_graph": round(out["batched"] / out["per_stream_graph"], 2),
+            "speedup_vs_per_stream_plain": round(out["batched"] / out["per_stream_plain"], 2),
+            "hbm_gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 3),
+            "streams": n_streams, "rounds": rounds, "cells": total_cells, "particles": total_particles,
             "config": "%d grids, side log-uniform [128, 1024] cells at 0.1-0.2 m, 1.5 particles per cell, "
-                      "10%% newborns; measurement grids in HBM; host wall clock" % n_streams}
+                      "10%% newborns; measurement grids in HBM; host wall clock; per-stream plain = kernels "
+                      "launched one by one and each update waited for (the reference's updateGrid)" % n_streams}
 
 
 def run_serving(dogm, scene, n_streams: int = 200, rate_hz: float = 10.0, seconds: float = 10.0,
@@ -447,7 +529,8 @@ def run_serving(dogm, scene, n_streams: int = 200, rate_hz: float = 10.0, second
             t += rng.exponential(1.0 / rate_hz)
     arrivals.sort()
     out = {}
-    for mode_name, mode in (("batched", dogm.SERVE_BATCHED), ("per_stream", dogm.SERVE_PER_STREAM)):
+    for mode_name, mode in (("batched", dogm.SERVE_BATCHED), ("per_stream", dogm.SERVE_PER_STREAM),
+                            ("per_stream_plain", dogm.SERVE_PER_STREAM_PLAIN)):
         srv = dogm.Server(hbm_budget_bytes=budget, mode=mode, max_batch=64, max_inflight=2)
         sids = [srv.open_stream(p, seed=2000 + i, stream_id=i) for i, p in enumerate(params)]
         frame_no = [0] * n_streams
@@ -495,9 +578,10 @@ def run_serving(dogm, scene, n_streams: int = 200, rate_hz: float = 10.0, second
             "resident_gb": round(st["resident_bytes"] / 1e9, 2),
         }
     block.free()
-    return {"batched": out["batched"], "per_stream": out["per_stream"],
-            "saturated_speedup": round(out["batched"]["saturated_frames_per_s"] /
-                                       out["per_stream"]["saturated_frames_per_s"], 2),
+    sat = {k: v["saturated_frames_per_s"] for k, v in out.items()}
+    return {"batched": out["batched"], "per_stream": out["per_stream"], "per_stream_plain": out["per_stream_plain"],
+            "saturated_speedup": round(sat["batched"] / sat["per_stream"], 2),
+            "saturated_speedup_vs_plain": round(sat["batched"] / sat["per_stream_plain"], 2),
             "config": "%d streams, Poisson %.0f Hz each (%.0f frames/s offered) for %.0f s, grids as the batched "
                       "workload, %.0f GB HBM budget; latency = submit to result on the device; saturation = %d "
                       "frames queued per stream" % (n_streams, rate_hz, n_streams * rate_hz, seconds, budget / 1e9,
@@ -525,19 +609,6 @@ def run_meas_grid(dogm, gs_len: float = 120.0, res: float = 0.1, beams: int = 21
     return out
 
 
-def read_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if present."""
-    path = os.path.join(REPO, "profiles", "ncu_traffic.md")
-    try:
-        for ln in open(path):
-            parts = [p.strip() for p in ln.strip().strip("|").split("|")]
-            if len(parts) >= 2 and parts[0] == kernel:
-                return int(float(parts[1]))
-    except (OSError, ValueError):
-        pass
-    return None
-
-
 def run_reference(args, rank: int, world: int):
     if rank != 0:
         return None
@@ -551,8 +622,9 @@ def run_reference(args, rank: int, world: int):
     spec.loader.exec_module(b)
     b.build_oracle()
     b.build_ref_harness()
-    dogm = importlib.import_module(PKG)
-    p = dogm.make_params(**importlib.import_module(PKG + ".scene").params_dict(cfg))
+    # parameters as a plain record: the reference arm loads nothing of this library
+    import types
+    p = types.SimpleNamespace(**importlib.import_module(PKG + ".scene").params_dict(cfg))
     ref = pyoracle.ReferencePipeline(p, threads=0)
     for k in range(W + 1):
         m, x, y, yaw = frames[pingpong(k, len(frames))]
@@ -566,17 +638,17 @@ def run_reference(args, rank: int, world: int):
     line = {"impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/update", "n_gpus": world,
             "steps": K, "warmup": W, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "large: 120 x 120 m at 0.1 m (1200^2 cells), 2e6 + 2e5 particles",
+            "config": {"workload": WORKLOAD_DESC,
                        "implementation": "the reference's pipeline (dogm/src/dogm.cu:115-131) transcribed to C "
                                          "with OpenMP; the reference itself is CUDA-only and has no CPU path"},
             "cpu_baseline": {"value": round(ms, 3), "unit": "ms/update", "cores": ref.threads_used, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(ms, 3), "unit": "ms/update", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    line["reference_cuda"] = reference_cuda(dogm, p, frames, W, min(K, 100))
+    line["reference_cuda"] = reference_cuda(p, frames, W, min(K, 100))
     return line
 
 
-def reference_cuda(dogm, p, frames, warm: int, steps: int) -> dict:
+def reference_cuda(p, frames, warm: int, steps: int) -> dict:
     """The reference's own CUDA build on this GPU: its kernels (cubins compiled from
     dogm/src/kernel/) in the restated updateGrid sequence (oracle/ref/ref_harness.cu).  Each
     update is synchronous, like the reference's (dogm.cu:130): host wall clock per update,
@@ -586,9 +658,10 @@ def reference_cuda(dogm, p, frames, warm: int, steps: int) -> dict:
     why = pyref.missing()
     if why:
         return {"unavailable": why}
+    rt = load_cudart()
     bufs = []
     for m, *_ in frames:
-        d = dogm.DeviceBuffer(m.nbytes)
+        d = CudartBuffer(rt, m.nbytes)
         d.upload(m)
         bufs.append(d)
     ref = pyref.ReferenceDOGM(p)
@@ -647,6 +720,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true", help="skip the batched and serving workloads")
     ap.add_argument("--no-autotune", action="store_true", help="time the built-in launch shape")
+    ap.add_argument("--min-seconds", type=float, default=1.0,
+                    help="the timed region repeats the K steps until it lasts at least this long")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="seconds of Poisson arrivals per serving mode (the serving workload names 60)")
     args = ap.parse_args()

@@ -50,7 +50,7 @@ ABI_SYMBOLS = [
     "dogm_server_default_config", "dogm_server_create", "dogm_server_destroy", "dogm_server_open_stream",
     "dogm_server_close_stream", "dogm_server_submit", "dogm_server_pause", "dogm_server_poll", "dogm_server_drain",
     "dogm_server_get_stats", "dogm_server_stream_state", "dogm_server_stream_handle", "dogm_server_now_ns",
-    "dogm_get_tune", "dogm_set_tune", "dogm_autotune",
+    "dogm_get_tune", "dogm_set_tune", "dogm_autotune", "dogm_set_launch_mode",
     "dogm_meas_grid_create", "dogm_meas_grid_destroy", "dogm_meas_grid_generate", "dogm_meas_grid_size",
     "dogm_meas_grid_polar", "dogm_meas_grid_fan", "dogm_extract_dynamic_cells", "dogm_extract_dynamic_cells_device",
     "dogm_snapshot_bytes", "dogm_snapshot", "dogm_restore",
@@ -100,7 +100,7 @@ class Tune(C.Structure):
                 "ms_tuned": round(self.ms_tuned, 4), "ms_default": round(self.ms_default, 4)}
 
 
-SERVE_BATCHED, SERVE_PER_STREAM = 0, 1
+SERVE_BATCHED, SERVE_PER_STREAM, SERVE_PER_STREAM_PLAIN = 0, 1, 2
 STREAM_WAITING, STREAM_ACTIVE, STREAM_CLOSED = 0, 1, 2
 
 
@@ -142,6 +142,7 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_lower_bound_f32": ([vp, i, vp, i, vp, i, vp], i), "dogm_host_alloc": ([vp, sz], i),
         "dogm_host_free": ([vp], i), "dogm_device_alloc": ([vp, sz], i), "dogm_device_free": ([vp], i),
         "dogm_memcpy": ([vp, vp, sz, i], i), "dogm_state_bytes": ([vp], sz), "dogm_last_launch_count": ([vp], i),
+        "dogm_set_launch_mode": ([vp, i], i),
         "dogm_last_error": ([], C.c_char_p), "dogm_get_stream": ([vp], vp), "dogm_profile_enable": ([vp, i], i),
         "dogm_stage_times": ([vp, vp, i], i), "dogm_stage_name": ([i], C.c_char_p), "dogm_status_string": ([i], C.c_char_p), "dogm_abi_version": ([], i),
         "dogm_server_default_config": ([vp], i), "dogm_server_create": ([vp, vp], i), "dogm_server_destroy": ([vp], i),
@@ -336,6 +337,10 @@ class DOGM:
 
     def get_iteration(self) -> int:
         return load().dogm_get_iteration(self.h)
+
+    def set_launch_mode(self, plain: bool) -> None:
+        """Plain kernel launches per update (as the reference) instead of a CUDA graph."""
+        check(load().dogm_set_launch_mode(self.h, 1 if plain else 0), "dogm_set_launch_mode")
 
     def last_launch_count(self) -> int:
         return load().dogm_last_launch_count(self.h)

@@ -1,8 +1,5 @@
 // Particle-side kernels: frame begin, prediction (with the fused ego shift), first-frame
 // particle initialisation, the stand-alone shift stage and Philox draw export.
-#include <map>
-#include <mutex>
-
 #include "dogm_device.cuh"
 
 namespace dogm_gb300 {
@@ -355,36 +352,32 @@ cudaError_t launch_shift_stage(const GridDesc& g, int x_move, int y_move, const 
 // ---------------------------------------------------------------------------------------
 static __device__ __align__(256) unsigned char g_shift_scratch[kShiftScratchBytes];
 
-namespace {
-std::mutex g_shift_scratch_mu;
-std::map<int, void*> g_shift_scratch_ptr;  // device ordinal -> device address of g_shift_scratch
-}  // namespace
+// Device address of g_shift_scratch in the current device's context.  In host code the
+// array's name is only a host-side stand-in, so the address is asked for with that device
+// current.  It is looked up on every call rather than cached: the lookup allocates nothing,
+// and a context created anew (after cudaDeviceReset) loads the module again at another
+// address, which a cache keyed by the device ordinal would miss.
+cudaError_t shift_scratch_address(void** out) {
+    *out = nullptr;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_shift_scratch);
+    if (e != cudaSuccess) return e;
+    *out = p;
+    return cudaSuccess;
+}
 
 cudaError_t shift_scratch_setup() {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    std::lock_guard<std::mutex> lock(g_shift_scratch_mu);
-    if (g_shift_scratch_ptr.count(dev)) return cudaSuccess;
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_shift_scratch);
-    if (e != cudaSuccess) return e;
-    g_shift_scratch_ptr[dev] = p;
-    return cudaSuccess;
+    void* p;
+    return shift_scratch_address(&p);
 }
 
 cudaError_t launch_shift_stage_noalloc(const GridDesc& g, int x_move, int y_move, const LaunchCfg& cfg) {
     const size_t bytes = sizeof(dogm_grid_cell) * (size_t)g.C;
     if (bytes > kShiftScratchBytes) return cudaErrorInvalidValue;  // the caller checks first
-    cudaError_t e = shift_scratch_setup();
+    void* scratch = nullptr;
+    cudaError_t e = shift_scratch_address(&scratch);
     if (e != cudaSuccess) return e;
-    int dev = -1;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    dogm_grid_cell* old_cells;
-    {
-        std::lock_guard<std::mutex> lock(g_shift_scratch_mu);
-        old_cells = static_cast<dogm_grid_cell*>(g_shift_scratch_ptr[dev]);
-    }
+    dogm_grid_cell* old_cells = static_cast<dogm_grid_cell*>(scratch);
     k_shift_particles<<<cfg.num_sms * 4, kThreads, 0, cfg.stream>>>(g.P_state, g.N, (float)x_move, (float)y_move);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     e = cudaMemcpyAsync(old_cells, g.cells, bytes, cudaMemcpyDeviceToDevice, cfg.stream);

@@ -64,6 +64,8 @@ struct Ctx {
     // programmatic dependent launch between the frame's kernels (environment DOGM_PDL=0 turns
     // it off, for comparison)
     bool pdl = true;
+    // steady-state frames as CUDA graph launches (dogm_set_launch_mode; plain launches otherwise)
+    bool use_graphs = true;
 
     // Captured graphs hold the launch widths: drop them when the widths change.
     void drop_graphs() {
@@ -334,7 +336,7 @@ struct HostCopy {
 dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launches,
                       const std::vector<HostCopy>* after = nullptr) {
     cudaError_t e;
-    const bool plain = any_init || any_clear || c.profile;
+    const bool plain = any_init || any_clear || c.profile || !c.use_graphs;
     if (plain) {
         // first frame of some grid (init runs between begin and predict), a frame after a
         // failed one (full counter reset first) or per-stage timing
@@ -785,6 +787,13 @@ int dogm_get_particle_count(const dogm_handle* h) { return h ? h->N : 0; }
 int dogm_get_new_born_particle_count(const dogm_handle* h) { return h ? h->B : 0; }
 int dogm_last_launch_count(const dogm_handle* h) { return h ? h->last_launches : 0; }
 
+dogm_status dogm_set_launch_mode(dogm_handle* h, int mode) {
+    if (!h || (mode != DOGM_LAUNCH_GRAPH && mode != DOGM_LAUNCH_PLAIN))
+        return fail(DOGM_ERR_INVALID_ARGUMENT, "bad handle or launch mode");
+    h->ctx.use_graphs = mode == DOGM_LAUNCH_GRAPH;
+    return DOGM_OK;
+}
+
 // ---- stage calls -----------------------------------------------------------------------
 
 dogm_status dogm_particle_prediction(dogm_handle* h, float dt) {
@@ -815,6 +824,10 @@ dogm_status dogm_update_pose(dogm_handle* h, float new_x, float new_y, float new
     int shifted, xm, ym;
     pose_update(h, new_x, new_y, new_yaw, &shifted, &xm, &ym);
     if (!shifted) return DOGM_OK;
+    // the shift rewrites the cell records in place: copies queued from them by
+    // dogm_get_grid_cells_async finish first
+    dogm_status st = wait_readback(h, h->ctx.stream);
+    if (st != DOGM_OK) return st;
     LaunchCfg cfg{h->ctx.num_sms, h->ctx.stream};
     DOGM_CUDA(launch_shift_stage(h->desc, xm, ym, cfg));
     DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));
@@ -840,6 +853,8 @@ dogm_status dogm_update_pose_noalloc(dogm_handle* h, float new_x, float new_y, f
     int shifted, xm, ym;
     pose_update(h, new_x, new_y, new_yaw, &shifted, &xm, &ym);
     if (!shifted) return DOGM_OK;
+    dogm_status st = wait_readback(h, h->ctx.stream);  // as dogm_update_pose
+    if (st != DOGM_OK) return st;
     LaunchCfg cfg{h->ctx.num_sms, h->ctx.stream};
     DOGM_CUDA(launch_shift_stage_noalloc(h->desc, xm, ym, cfg));
     DOGM_CUDA(cudaStreamSynchronize(h->ctx.stream));

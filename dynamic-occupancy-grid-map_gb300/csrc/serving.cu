@@ -109,8 +109,9 @@ dogm_status create_handle(dogm_server* s, Stream* st, std::unique_lock<std::mute
     lk.unlock();
     dogm_status rc = dogm_create(&st->params, &opt, &h);
     cudaEvent_t ev = nullptr;
-    if (rc == DOGM_OK && s->cfg.mode == DOGM_SERVE_PER_STREAM &&
-        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+    const bool per_stream = s->cfg.mode == DOGM_SERVE_PER_STREAM || s->cfg.mode == DOGM_SERVE_PER_STREAM_PLAIN;
+    if (rc == DOGM_OK && s->cfg.mode == DOGM_SERVE_PER_STREAM_PLAIN) rc = dogm_set_launch_mode(h, DOGM_LAUNCH_PLAIN);
+    if (rc == DOGM_OK && per_stream && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
         dogm_destroy(h);
         h = nullptr;
         rc = fail(DOGM_ERR_CUDA, "cudaEventCreate failed");
@@ -230,7 +231,8 @@ bool dogm_server::launch(std::unique_lock<std::mutex>& lk) {
     std::sort(ready.begin(), ready.end(),
               [](const Stream* a, const Stream* b) { return a->q.front().t_submit < b->q.front().t_submit; });
     bool any = false;
-    if (cfg.mode == DOGM_SERVE_PER_STREAM) {
+    if (cfg.mode == DOGM_SERVE_PER_STREAM || cfg.mode == DOGM_SERVE_PER_STREAM_PLAIN) {
+        const bool plain = cfg.mode == DOGM_SERVE_PER_STREAM_PLAIN;
         for (Stream* st : ready) {
             st->cur = st->q.front();
             st->q.pop_front();
@@ -245,6 +247,9 @@ bool dogm_server::launch(std::unique_lock<std::mutex>& lk) {
                 rc = fail(DOGM_ERR_CUDA, "readback copy failed");
             if (rc == DOGM_OK && cudaEventRecord(st->ev, cs) != cudaSuccess)
                 rc = fail(DOGM_ERR_CUDA, "cudaEventRecord failed");
+            // plain mode: the frame is waited for before the next one starts, as the reference
+            if (rc == DOGM_OK && plain && cudaEventSynchronize(st->ev) != cudaSuccess)
+                rc = fail(DOGM_ERR_CUDA, "cudaEventSynchronize failed");
             const int64_t t = now_ns();
             lk.lock();
             launches += 1;
@@ -344,7 +349,8 @@ dogm_status dogm_server_default_config(dogm_server_config* cfg) {
 dogm_status dogm_server_create(const dogm_server_config* cfg, dogm_server** out) {
     if (!cfg || !out) return fail(DOGM_ERR_INVALID_ARGUMENT, "cfg/out is NULL");
     *out = nullptr;
-    if (cfg->mode != DOGM_SERVE_BATCHED && cfg->mode != DOGM_SERVE_PER_STREAM)
+    if (cfg->mode != DOGM_SERVE_BATCHED && cfg->mode != DOGM_SERVE_PER_STREAM &&
+        cfg->mode != DOGM_SERVE_PER_STREAM_PLAIN)
         return fail(DOGM_ERR_INVALID_ARGUMENT, "unknown serve mode");
     if (cfg->max_batch < 1 || cfg->max_batch > kMaxBatch)
         return fail(DOGM_ERR_INVALID_ARGUMENT, "max_batch must be in [1, 256]");

@@ -169,8 +169,11 @@ dogm_status dogm_update_pose(dogm_handle* h, float new_x, float new_y, float new
  * dogm_update_pose takes a temporary buffer for the copy of the previous cell records.  Here
  * that copy goes to a fixed 16 MiB device array built into the library, one per device, so
  * grids of at most 262,144 cells (for example 512 x 512) are accepted; a larger grid returns
- * DOGM_ERR_INVALID_ARGUMENT and leaves the handle unchanged.  The first call on a device looks
- * up the array's address: make that first call before any stream capture.  All calls on a
+ * DOGM_ERR_INVALID_ARGUMENT and leaves the handle unchanged.  Every call looks up the array's
+ * address in the current context (a lookup, not an allocation), so a context created anew after
+ * cudaDeviceReset is handled; the first call on a device may load the library's device code into
+ * that context: make that first call before any stream capture.  Like dogm_update_pose, it
+ * waits for grid copies queued by dogm_get_grid_cells_async before it moves the cells.  All calls on a
  * device share the one array, so calls whose work overlaps on the GPU (several host threads at
  * once) race on it and must be serialised by the caller. */
 dogm_status dogm_update_pose_noalloc(dogm_handle* h, float new_x, float new_y, float new_yaw);
@@ -256,8 +259,12 @@ size_t dogm_state_bytes(const dogm_params* params);
  * stream's own CUDA stream (the plain-launch comparison).  All calls are thread-safe. */
 
 typedef enum dogm_serve_mode {
-    DOGM_SERVE_BATCHED = 0,   /* continuous batching over launch slots                       */
-    DOGM_SERVE_PER_STREAM = 1 /* one dogm_update per frame on the stream's own CUDA stream     */
+    DOGM_SERVE_BATCHED = 0,    /* continuous batching over launch slots                      */
+    DOGM_SERVE_PER_STREAM = 1, /* one dogm_update per frame on the stream's own CUDA stream,
+                                  a CUDA graph launch, frames of several streams in flight    */
+    DOGM_SERVE_PER_STREAM_PLAIN = 2 /* one dogm_update per frame with plain kernel launches,
+                                  each waited for before the next frame starts (the
+                                  reference's synchronous updateGrid, dogm/src/dogm.cu:115-131) */
 } dogm_serve_mode;
 
 typedef struct dogm_server_config {
@@ -538,6 +545,13 @@ dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int
 
 /* Number of kernel launches the last update issued, and the text of the last error. */
 int dogm_last_launch_count(const dogm_handle* h);
+
+/* How a handle's steady-state updates are launched (no counterpart in the reference, whose
+ * updateGrid issues every kernel itself): DOGM_LAUNCH_GRAPH (default) replays one captured CUDA
+ * graph per update; DOGM_LAUNCH_PLAIN issues the kernels one by one, as the reference does.  The
+ * results are the same bits either way. */
+typedef enum dogm_launch_mode { DOGM_LAUNCH_GRAPH = 0, DOGM_LAUNCH_PLAIN = 1 } dogm_launch_mode;
+dogm_status dogm_set_launch_mode(dogm_handle* h, int mode);
 const char* dogm_last_error(void);
 const char* dogm_status_string(dogm_status s);
 int dogm_abi_version(void);

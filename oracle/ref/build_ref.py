@@ -18,6 +18,7 @@ oracle/ref/eval_harness.cu into oracle/_ref/libref_eval.so, a host library for t
 this machine (it does not run on the Arm GPU machine, where the tests that need it skip).
 
     python oracle/ref/build_ref.py            # where the reference sources are present
+    DOGM_REFERENCE_DIR=<checkout> python oracle/ref/build_ref.py
 """
 from __future__ import annotations
 
@@ -30,7 +31,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
-REFERENCE = "/root/reference/dogm"
+# where the reference's sources lie: DOGM_REFERENCE_DIR (the repository's root), by default the
+# read-only checkout this recipe was written against
+REFERENCE = os.path.join(os.environ.get("DOGM_REFERENCE_DIR", "/root/reference"), "dogm")
 KERNEL_FILES = ["ego_motion_compensation", "init", "init_new_particles", "mass_update", "particle_to_grid", "predict",
                 "resampling", "statistical_moments", "update_persistent_particles"]
 FLAGS = ["-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "--expt-extended-lambda",

@@ -50,6 +50,32 @@ def test_noalloc_pose_update_matches_allocating_one(dogm, scene):
         g.close()
 
 
+@pytest.mark.parametrize("call", ["update_pose_noalloc", "update_pose"])
+def test_pose_shift_waits_for_queued_grid_readback(dogm, scene, call):
+    """A grid copy queued by get_grid_cells_async before a shift must deliver the grid as it
+    was before the shift: the shift rewrites the cell records in place, so it has to wait for
+    the copy (a torn copy would mix pre- and post-shift records)."""
+    p = dogm.make_params(size=50.0, resolution=0.2, particle_count=100000, new_born_particle_count=10000)
+    g = dogm.DOGM(p, seed=501)   # 250 x 250 cells: 4 MB of records per copy
+    for k in range(2):
+        g.update_grid(scene.random_measurements(g.grid_size, seed=600 + k), 0.0, 0.0, 0.0, 0.1)
+    before = g.get_grid_cells()
+    outs = [dogm.PinnedArray(before.shape, dogm.GRID_CELL_DTYPE) for _ in range(2)]
+    try:
+        for i, (x, y) in enumerate([(1.3, -0.9), (2.9, 0.7)]):
+            g.get_grid_cells_async(outs[i].array)
+            getattr(g, call)(x, y, 0.0)
+            g.synchronize()
+            assert outs[i].array.tobytes() == before.tobytes(), "copy %d torn by the shift" % i
+            after = g.get_grid_cells()
+            assert after.tobytes() != before.tobytes()   # the shift did move the records
+            before = after
+    finally:
+        for o in outs:
+            o.free()
+        g.close()
+
+
 def test_noalloc_pose_update_refuses_grids_over_its_limit(dogm):
     p = dogm.make_params(size=60.0, resolution=0.1, particle_count=1000, new_born_particle_count=100)
     g = dogm.DOGM(p, seed=1)   # 600 x 600 = 360,000 cells > 262,144
