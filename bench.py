@@ -44,20 +44,17 @@ WORKLOAD_DESC = ("large: 120 x 120 m at 0.1 m (1200^2 = 1.44e6 cells), 2e6 persi
 ALG_PER_PARTICLE, ALG_PER_NEWBORN, ALG_PER_CELL = 152, 29, 108
 
 
-def stage_bytes(N: int, B: int, C_: int, n_occ: int, n_birth_cells: int, sort_tiles: int, nb0: int,
-                nb1: int) -> dict:
+def stage_bytes(N: int, B: int, C_: int, n_occ: int, n_birth_cells: int, sort_tiles: int, buckets: int) -> dict:
     """Algorithmic bytes per launch of each kernel (what it must read and write once)."""
     return {
-        "predict": 40 * N + 4 * sort_tiles * nb0,  # state R/W 16+16, key R/W 4+4; digit counts W
-        "sort_scan0": 8 * sort_tiles * nb0,      # digit counts R, offsets W
-        "sort_pass0": 12 * N + 4 * sort_tiles * nb0,  # key R 4, (key, index) W 8; offsets R
-        "sort_scan1": 4 * N + 12 * sort_tiles * nb1,  # pass-1 digit counts: keys R, counts W; scan R/W
-        "sort_pass1": 44 * N,                    # (key, index) R 8, state gather R 16, state+key W 20
-        "cells": 20 * N + 112 * C_,              # key 4 + state 16 R; meas 16 + free 4 R;
-                                                 # record 64 + free 4 + rho_b 4 + w 4 + meas copy 16 W
-        "newborn": 4 * C_ + 32 * n_birth_cells,   # newborn mass R; w_A/w_UA + newborn-cell list W
-        "resample": 24 * N + 20 * N,             # key 4 + state 16 + weight 4 R; state+key 20 W
-                                                 # (newborns are created in registers)
+        "predict": 40 * N + 4 * sort_tiles * buckets,  # state R/W 16+16, key R/W 4+4; bucket counts W
+        "sort_scan": 8 * sort_tiles * buckets,      # bucket counts R, offsets W
+        "sort_scatter": 40 * N + 4 * sort_tiles * buckets,  # state+key R 20, W 20 (bucketed); offsets R
+        "cells": 40 * N + 112 * C_,                 # bucketed state+key R 20, sorted W 20; meas 16 + free 4
+                                                    # R; record 64 + free 4 + rho_b 4 + w 4 + meas copy 16 W
+        "newborn": 4 * C_ + 32 * n_birth_cells,     # newborn mass R; w_A/w_UA + newborn-cell list W
+        "resample": 24 * N + 20 * N,                # key 4 + state 16 + weight 4 R; state+key 20 W
+                                                    # (newborns are created in registers)
     }
 
 
@@ -260,7 +257,7 @@ def run_gb300(args, rank: int, world: int):
         d = dogm.DeviceBuffer(m.nbytes)
         d.upload(m)
         dbufs.append(d)
-    # launch widths and the radix split chosen by the autotuner on this GPU (a scratch handle
+    # launch widths chosen by the autotuner on this GPU (a scratch handle
     # fed the first frame; kept only when faster than the defaults)
     tune = g.autotune(dbufs[0].ptr, reps=10, device=True) if not args.no_autotune else None
     # first measurement (initialisation) + warm-up (graph capture for both mirrors)
@@ -364,10 +361,8 @@ def run_gb300(args, rank: int, world: int):
     cells = g.get_grid_cells()
     n_occ = int((cells["start_idx"] >= 0).sum())
     n_bcells = int(((cells["w_A"] > 0) | (cells["w_UA"] > 0)).sum())
-    bits = max(1, (C_ - 1).bit_length())
-    d0 = (bits + 1) // 2
     sort_tiles = -(-N // 4096)
-    sb = stage_bytes(N, B, C_, n_occ, n_bcells, sort_tiles, 1 << d0, 1 << (bits - d0))
+    sb = stage_bytes(N, B, C_, n_occ, n_bcells, sort_tiles, -(-C_ // 1024))
     dom = max(stages, key=lambda k: stages[k])
     peak, peak_src = peak_gbs()
     achieved = sb[dom] / (stages[dom] * 1e-3) / 1e9

@@ -16,10 +16,8 @@ namespace dogm_gb300 {
 // ---- tile shapes (elements per tile; 256-thread blocks everywhere) ---------------------
 constexpr int kThreads = 256;
 constexpr int kPredictTile = 4096;   // particles per predict tile (16 per thread)
-constexpr int kSortIpt = 16;         // keys per thread in a sort pass
+constexpr int kSortIpt = 16;         // keys per thread in the bucket scatter
 constexpr int kSortTile = kThreads * kSortIpt;
-constexpr int kSortMaxBits = 11;     // radix digit width <= 11 -> <= 2048 bins
-constexpr int kSortMaxBins = 1 << kSortMaxBits;
 constexpr int kSegIpt = 4;           // sorted particles per thread in a chunk of the cell pass
 constexpr int kSegTile = kThreads * kSegIpt;
 constexpr int kCellIpt = 4;          // cells per thread in the cell passes
@@ -27,11 +25,11 @@ constexpr int kCellTile = kThreads * kCellIpt;
 constexpr int kResIpt = 4;           // joint particles per thread in resampling
 constexpr int kResTile = kThreads * kResIpt;
 
-static_assert(kPredictTile == kSortTile, "predict writes the pass-0 digit counts of the sort tiles");
+static_assert(kPredictTile == kSortTile, "predict writes the bucket counts of the scatter tiles");
 
-constexpr int kMaxKeyBits = 22;      // grid_size <= 2048 -> cells < 2^22 -> 2 radix passes
+constexpr int kMaxKeyBits = 22;      // grid_size <= 2048 -> cells < 2^22
 constexpr int kCellTileBits = 10;
-constexpr int kMaxCellTiles = (1 << kMaxKeyBits) >> kCellTileBits;
+constexpr int kMaxCellTiles = (1 << kMaxKeyBits) >> kCellTileBits;  // buckets of the particle sort
 static_assert(kCellTile == (1 << kCellTileBits), "cell tiles are indexed by cell >> kCellTileBits");
 static_assert(kResTile % 32 == 0, "32 aligned sorted positions lie in one resample tile");
 constexpr int kMaxParticles = (1 << 24) - 1;  // keys, counts and slot indices stay below 2^24
@@ -45,9 +43,10 @@ constexpr uint32_t kAssocBit = 1u << 31;
 enum DrawStage : uint32_t { kDrawInit = 1, kDrawPredict = 2, kDrawBirth = 3, kDrawResample = 4 };
 
 // Stages of the update; each has a tile count per grid and a work counter for dynamic claims.
+// The particle sort is one stable bucket scatter by cell tile (kStScan: bucket offsets, kStSort:
+// the scatter) followed by a stable counting sort of each bucket inside the cell pass.
 enum Stage : int {
-    kStPredict = 0, kStScan0, kStSort0, kStScan1, kStSort1, kStCell, kStBirth, kStResample, kStInitScan,
-    kStInitExpand, kNumStages
+    kStPredict = 0, kStScan, kStSort, kStCell, kStBirth, kStResample, kStInitScan, kStInitExpand, kNumStages
 };
 
 
@@ -69,8 +68,9 @@ constexpr uint32_t kStatusBounds = 2u;   // an index check refused a write
 struct GridDesc {
     // sizes
     int N, B, C, gs;
-    int d0_bits, d1_bits;   // radix digit widths (d0 low digit)
     int q_shift;            // fixed point: weight w -> round(w * 2^q_shift)
+    int ctiles;             // cell tiles = buckets of the particle sort
+    int bucket_stride;      // words per row of the per-tile bucket counts (ctiles rounded up to 4)
     int pad0;
     unsigned long long gs_div;  // floor(2^42 / gs) + 1: k / gs == (k * gs_div) >> 42 for k < 2^22
     // filter parameters
@@ -83,9 +83,10 @@ struct GridDesc {
     uint32_t frame;         // iteration number (Philox counter word 1)
     uint32_t stream_id;     // Philox counter word 3
     uint32_t seed_lo, seed_hi;
-    // particles (persistent: P, sort temporaries: T, sorted: S, newborn: Bp)
+    // particles (persistent: P, bucketed by cell tile: T, sorted: S, newborn: Bp)
     float4* P_state; uint32_t* P_key;
-    uint2* T_pair;          // pass-0 output: {key word, index of the particle in P}
+    float4* T_state; uint32_t* T_key;  // stable bucket scatter of P by cell tile
+    int* T_idx;             // debug: index in P of each bucketed particle (NULL: off)
     float4* S_state; uint32_t* S_key;
     float4* B_state; uint32_t* B_key; float* B_w;  // newborns: key words always, state/weight for debug export
     // cells
@@ -96,8 +97,7 @@ struct GridDesc {
     float2* rho_b;          // per cell {newborn mass, p_A} of this frame (the newborn kernel's input)
     float* w_cell;          // per cell weight of an in-grid persistent particle after reweighting
     // scratch
-    uint32_t* hist;         // 2 x kSortMaxBins digit histograms
-    uint32_t* hsort;        // 2 x sort_tiles x kSortMaxBins: per-tile digit counts, then offsets
+    uint32_t* hsort;        // sort_tiles x bucket_stride: per-tile bucket counts, then offsets
     uint32_t* ctile_cnt;    // per cell tile: particles whose cell lies in it (counted by predict)
     uint32_t* ctile_start;  // per cell tile + 1: first sorted position of the tile (exclusive scan)
     uint32_t* ctile_order;  // cell tiles in claim order: tiles with many particles first
@@ -167,14 +167,14 @@ inline int launch_blocks(const LaunchCfg& cfg, int default_mult) {
 
 cudaError_t prepare_kernels();  // per device, before the first launch
 cudaError_t prepare_cells();
+cudaError_t prepare_sort();
 cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCfg& cfg);
 cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg);
-cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg);
-cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg);
-cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cfg);
-// pass-1 digit counts of every pass-0 output tile (k_sort_hist), then their column scan
-cudaError_t launch_sort_offsets1(const Batch* d_batch, const LaunchCfg& cfg);
+// bucket offsets (column scan of the per-tile bucket counts) and the stable bucket scatter;
+// max_ctiles: the largest bucket count of the batch's grids (sizes the scatter's shared memory)
+cudaError_t launch_sort_scan(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_sort_scatter(const Batch* d_batch, int max_ctiles, const LaunchCfg& cfg);
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg);
@@ -189,10 +189,10 @@ cudaError_t launch_draws(const GridDesc& g, int iteration, float2* init_u, float
 cudaError_t launch_lower_bound(const float* accum, int n_accum, const float* q, int n_q, int* out, int clamp_last,
                                cudaStream_t s);
 
-// Kernel launches per steady-state update (for the launch-count claim): predict, 2 x (digit
-// scan, sort pass), cells, newborn, resample.  A grid's first frame, and a frame after a
-// failed one, adds the frame-begin reset.
-constexpr int kLaunchesPerFrame = 9;
+// Kernel launches per steady-state update (for the launch-count claim): predict, bucket scan,
+// bucket scatter, cells, newborn, resample.  A grid's first frame, and a frame after a failed
+// one, adds the frame-begin reset.
+constexpr int kLaunchesPerFrame = 6;
 constexpr int kLaunchesInit = 2;
 
 // ---- batch slots (runtime.cu): the launch contexts of the serving loop (serving.cu) ------

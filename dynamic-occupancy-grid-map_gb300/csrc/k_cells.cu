@@ -1,7 +1,8 @@
 // Cell-side kernels.
-//  k_cells    : one pass over all cells and the sorted particles in them; fuses the
-//               particle-to-cell segmented reduction, the mass update, reweighting,
-//               moments, ego shift of the free mass and the measurement copy.
+//  k_cells    : one pass over all cells and the particles in them; fuses the second half of
+//               the particle sort (a stable counting sort of the tile's bucket by cell), the
+//               particle-to-cell segmented reduction, the mass update, reweighting, moments,
+//               ego shift of the free mass and the measurement copy.
 //  k_newborn  : newborn allocation over an exact scan of the newborn masses
 //               (init_new_particles.cu:126-155, dogm.cu:323-348): records w_A / w_UA and
 //               the key word of every newborn slot; the newborn particles themselves are
@@ -65,8 +66,12 @@ __device__ __forceinline__ Run run_shfl_up(const Run& a, int o) {
 }
 
 // ---------------------------------------------------------------------------------------
-// Fused per-cell update over one tile of kCellTile cells and the sorted particles that lie
-// in it, positions [ctile_start[t], ctile_start[t + 1]).
+// Fused per-cell update over one tile of kCellTile cells and the particles that lie in it,
+// positions [ctile_start[t], ctile_start[t + 1]) of the bucketed (T) and sorted (S) arrays.
+//   S  stable counting sort of the bucket by cell, T -> S: per-cell counts, their exclusive
+//      scan, then, chunk by chunk in bucket order, each particle's rank among the earlier
+//      particles of its cell (warp ranks by match_any, per-warp counts, offsets across warps).
+//      The writes land in the tile's own window of S, which stays in L2 for phase A.
 //   A  segmented reduction of those particles into per-cell shared sums (sorted range,
 //      in-grid count, sum(v), sum(v^2), sum(vx*vy)).  Each thread walks its own share of
 //      consecutive particles: a cell whose particles start and end inside the thread is
@@ -85,23 +90,40 @@ __device__ __forceinline__ Run run_shfl_up(const Run& a, int o) {
 constexpr int kCellThreads = 512;  // two cells per thread: a tile finishes in half the time
 static_assert(kCellTile % kCellThreads == 0, "whole cells per thread");
 
+constexpr int kCellWarps = kCellThreads / 32;
+constexpr int kBucketIpt = 8;  // bucket particles per thread in a chunk of the counting sort
+constexpr int kBucketChunk = kCellThreads * kBucketIpt;
+
 struct CellSmem {
-    dogm_measurement_cell meas[kCellTile];  // prefetched (cp.async) while A runs
+    dogm_measurement_cell meas[kCellTile];  // prefetched (cp.async) while S and A run
     float free_prev[kCellTile];             // previous free mass, ego shift applied
     int start[kCellTile];   // sorted position of the first particle (-1: none)
     int end[kCellTile];     // sorted position of the last particle
     int n_in[kCellTile];    // in-grid particles
-    float vx[kCellTile], vy[kCellTile], vxx[kCellTile], vyy[kCellTile], vxy[kCellTile];
-    // per warp: its 32 cell records (2 KB), staged so that the warp stores them as 512
-    // contiguous bytes per instruction instead of four 16-byte pieces at 64-byte stride
-    float4 stage[kCellThreads / 32][32 * 4];
+    union {
+        struct {            // A and B: per-cell sums
+            float vx[kCellTile], vy[kCellTile], vxx[kCellTile], vyy[kCellTile], vxy[kCellTile];
+        } sum;
+        struct {            // S: particles per cell, then running offsets (two chunks in turn)
+            uint32_t cnt[kCellTile];
+            uint32_t off[2][kCellTile];
+        } srt;
+    } u1;
+    union {
+        // B, per warp: its 32 cell records (2 KB), staged so that the warp stores them as 512
+        // contiguous bytes per instruction instead of four 16-byte pieces at 64-byte stride
+        float4 stage[kCellWarps][32 * 4];
+        // S: per-warp particle counts per cell in the current chunk, then offsets across warps
+        uint16_t whist[kCellWarps][kCellTile];
+    } u2;
+    int scan[kCellWarps];
     Run wagg[kCellThreads / 32];  // each warp's run, then (wpre) the runs before each warp
     Run wpre[kCellThreads / 32];
     unsigned long long red[kCellThreads / 32], red2[kCellThreads / 32];
     int tiles[2];  // the block's current tile and the one claimed for the next iteration
 };
 static_assert(offsetof(CellSmem, meas) % 16 == 0, "16-byte cp.async destination");
-static_assert(offsetof(CellSmem, stage) % 16 == 0, "16-byte staged records");
+static_assert(offsetof(CellSmem, u2) % 16 == 0, "16-byte staged records");
 static_assert(sizeof(dogm_grid_cell) == 64, "a record is four float4");
 
 // Record chunk j of lane l is staged at float4 slot 4 l + (j ^ ((l >> 1) & 3)): for each j the
@@ -139,11 +161,136 @@ __device__ __forceinline__ void put_cell(CellSmem& sm, const GridDesc& g, uint32
     }
     sm.end[cl] = last;
     sm.n_in[cl] = (int)(r.fn & ~kRunHead);
-    sm.vx[cl] = r.vx;
-    sm.vy[cl] = r.vy;
-    sm.vxx[cl] = r.vxx;
-    sm.vyy[cl] = r.vyy;
-    sm.vxy[cl] = r.vxy;
+    sm.u1.sum.vx[cl] = r.vx;
+    sm.u1.sum.vy[cl] = r.vy;
+    sm.u1.sum.vxx[cl] = r.vxx;
+    sm.u1.sum.vyy[cl] = r.vyy;
+    sm.u1.sum.vxy[cl] = r.vxy;
+}
+
+// S: the stable counting sort of one bucket (bucketed positions [p0, p1) of T, whose cells lie
+// in [base, base + kCellTile)) into the same positions of S.  Ends with a barrier.
+__device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int base, int p0, int p1) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) sm.u1.srt.cnt[c] = 0u;
+    __syncthreads();
+    // 1: particles per cell (a key outside the tile can only come from inconsistent counts)
+    for (int i0 = p0; i0 < p1; i0 += kCellThreads * 4) {
+        uint32_t kw[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int i = i0 + r * kCellThreads + (int)threadIdx.x;
+            kw[r] = i < p1 ? g.T_key[i] : 0xffffffffu;
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const uint32_t c = kw[r] == 0xffffffffu ? 0xffffffffu : (kw[r] & kCellMask) - (uint32_t)base;
+            const uint32_t d = c < (uint32_t)kCellTile ? c : 0xffffffffu;
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            if (d != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&sm.u1.srt.cnt[d], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    // 2: exclusive scan of the counts: the first position of each cell in the bucket
+    {
+        constexpr int kPer = kCellTile / kCellThreads;
+        const int c0 = threadIdx.x * kPer;
+        uint32_t v[kPer], s = 0u;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            v[j] = sm.u1.srt.cnt[c0 + j];
+            s += v[j];
+        }
+        uint32_t x = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) sm.scan[warp] = (int)x;
+        __syncthreads();
+        uint32_t e = x - s;
+        for (int w = 0; w < warp; ++w) e += (uint32_t)sm.scan[w];
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            sm.u1.srt.off[0][c0 + j] = e;
+            e += v[j];
+        }
+    }
+    // 3: chunks in bucket order; warp w takes chunk positions [w * 256, (w + 1) * 256)
+    int cur = 0;
+    for (int c0 = p0; c0 < p1; c0 += kBucketChunk, cur ^= 1) {
+        uint4* wz = reinterpret_cast<uint4*>(&sm.u2.whist[0][0]);
+        for (int i = threadIdx.x; i < (int)(sizeof(sm.u2.whist) / sizeof(uint4)); i += kCellThreads)
+            wz[i] = make_uint4(0u, 0u, 0u, 0u);
+        __syncthreads();
+        const int wbase = c0 + warp * (32 * kBucketIpt);
+        uint32_t key[kBucketIpt];
+        uint16_t rank[kBucketIpt];
+#pragma unroll
+        for (int k = 0; k < kBucketIpt; ++k) {
+            const int i = wbase + k * 32 + lane;
+            key[k] = i < p1 ? g.T_key[i] : 0xffffffffu;
+        }
+#pragma unroll
+        for (int k = 0; k < kBucketIpt; ++k) {
+            const uint32_t c = key[k] == 0xffffffffu ? 0xffffffffu : (key[k] & kCellMask) - (uint32_t)base;
+            const uint32_t d = c < (uint32_t)kCellTile ? c : 0xffffffffu;
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            uint16_t before = 0;
+            if (d != 0xffffffffu) before = sm.u2.whist[warp][d];
+            rank[k] = (uint16_t)(before + __popc(peers & lt_mask));
+            __syncwarp();
+            if (d != 0xffffffffu && lane == __ffs(peers) - 1) sm.u2.whist[warp][d] = (uint16_t)(before + __popc(peers));
+            __syncwarp();
+        }
+        __syncthreads();
+        // per cell: offsets of the warps within the chunk, and the cell's offset for the next chunk
+        for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) {
+            uint32_t acc = 0u;
+#pragma unroll
+            for (int w = 0; w < kCellWarps; ++w) {
+                const uint32_t n = sm.u2.whist[w][c];
+                sm.u2.whist[w][c] = (uint16_t)acc;
+                acc += n;
+            }
+            sm.u1.srt.off[cur ^ 1][c] = sm.u1.srt.off[cur][c] + acc;
+        }
+        __syncthreads();
+        // scatter to the sorted positions; per half of the items every state load is issued
+        // before the first store
+        constexpr int kHalf = kBucketIpt / 2;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float4 st[kHalf];
+            int out[kHalf];
+#pragma unroll
+            for (int j = 0; j < kHalf; ++j) {
+                const int k = h * kHalf + j;
+                const int i = wbase + k * 32 + lane;
+                const uint32_t c = (key[k] & kCellMask) - (uint32_t)base;
+                out[j] = -1;
+                if (i < p1 && c < (uint32_t)kCellTile)
+                    out[j] = p0 + (int)(sm.u1.srt.off[cur][c] + sm.u2.whist[warp][c] + rank[k]);
+                st[j] = g.T_state[i < p1 ? i : p1 - 1];
+            }
+#pragma unroll
+            for (int j = 0; j < kHalf; ++j) {
+                const int k = h * kHalf + j;
+                const int i = wbase + k * 32 + lane;
+                if (i >= p1) continue;
+                if (out[j] < p0 || out[j] >= p1) {  // only inconsistent counts get here
+                    flag_status(g, kStatusBounds);
+                    continue;
+                }
+                g.S_key[out[j]] = key[k];
+                g.S_state[out[j]] = st[j];
+                if (g.dbg_perm) g.dbg_perm[out[j]] = g.T_idx[i];
+            }
+        }
+        __syncthreads();
+    }
 }
 
 __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ bt) {
@@ -153,13 +300,12 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
     const int total = batch_total(bt, kStCell);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     {
-        // the next frame's counters start at zero: predict adds the digit and cell-tile
-        // counts; their readers (the digit scans) finished before this kernel
+        // the next frame's bucket totals start at zero: predict adds them; their readers (the
+        // bucket scan) finished before this kernel
         const int stride = gridDim.x * blockDim.x;
         const int tid = blockIdx.x * blockDim.x + threadIdx.x;
         for (int gi = 0; gi < bt->n_grids; ++gi) {
             const GridDesc& g = bt->g[gi];
-            for (int i = tid; i < 2 * kSortMaxBins; i += stride) g.hist[i] = 0u;
             for (int i = tid; i < g.tiles[kStCell]; i += stride) g.ctile_cnt[i] = 0u;
         }
     }
@@ -199,12 +345,15 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             else sm.free_prev[cl] = 0.0f;
         }
         for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) sm.start[c] = -1;
-        __syncthreads();
+
+        // ---- S: stable counting sort of the tile's bucket into S -------------------------
+        const int np = p1 - p0;
+        if (np > 0) sort_bucket(sm, g, base, p0, p1);  // block-uniform; ends with a barrier
+        else __syncthreads();
 
         // ---- A: segmented reduction of the tile's particles ------------------------------
         // thread t walks its own consecutive share [i_beg, i_end) of the tile's particles, so
         // a full tile costs one block scan however many particles it holds
-        const int np = p1 - p0;
         if (np > 0) {  // block-uniform
             const int per = (np + kCellThreads - 1) / kCellThreads;
             const int i_beg = min(p1, p0 + (int)threadIdx.x * per), i_end = min(p1, i_beg + per);
@@ -297,7 +446,7 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             const int k = base + cl;
             const int warp_first = base + r * kCellThreads + warp * 32;  // the warp's 32 cells
             if (warp_first >= g.C) break;                                // warp-uniform
-            float4* stage = sm.stage[warp];
+            float4* stage = sm.u2.stage[warp];
             if (k < g.C) {
             const bool occupied = sm.start[cl] >= 0;  // end, count and sums are set only then
             const int start = occupied ? sm.start[cl] : -1, end = occupied ? sm.end[cl] : -1;
@@ -317,11 +466,11 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                                __fmul_rn(__fmul_rn(__fsub_rn(1.0f, m.p_A), muUA), o.w_norm));
                 if (o.rho_p > 0.0f) {
                     const float inv = __fdiv_rn(1.0f, o.rho_p);
-                    mx = __fmul_rn(inv, __fmul_rn(wp, sm.vx[cl]));
-                    my = __fmul_rn(inv, __fmul_rn(wp, sm.vy[cl]));
-                    vx = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.vxx[cl])), __fmul_rn(mx, mx));
-                    vy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.vyy[cl])), __fmul_rn(my, my));
-                    cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.vxy[cl])), __fmul_rn(mx, my));
+                    mx = __fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vx[cl]));
+                    my = __fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vy[cl]));
+                    vx = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vxx[cl])), __fmul_rn(mx, mx));
+                    vy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vyy[cl])), __fmul_rn(my, my));
+                    cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vxy[cl])), __fmul_rn(mx, my));
                 }
             }
             stage[stage_slot(lane, 0)] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);

@@ -12,11 +12,10 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     for (int gi = 0; gi < bt->n_grids; ++gi) {
         const GridDesc& g = bt->g[gi];
-        for (int i = tid; i < 2 * kSortMaxBins; i += stride) g.hist[i] = 0u;
         for (int i = tid; i < g.tiles[kStCell]; i += stride) g.ctile_cnt[i] = 0u;
         for (int i = tid; i < 2 * g.tiles[kStCell]; i += stride) g.cell_sum[i] = 0ull;
         for (int i = tid; i < g.tiles[kStResample]; i += stride) g.res_sum[i] = 0ull;
-        // (the per-tile digit counts of both passes are written whole each frame)
+        // (the per-tile bucket counts are written whole each frame)
         if (tid == 0) {
             g.fs->status = 0u;
             g.fs->qb_total = 0ull;
@@ -34,7 +33,9 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
 // evaluated as x' = (x + dt*vx) + n_x (the grouping of the reference's mat4 x vec4);
 // the weight is not stored per particle: every persistent particle carries the common
 // weight w_res, so the predicted weight is p_S * w_res, or 0 out of the grid (bit 30).
-// mode 0: full frame (shift + digit histograms); mode 1: stage call (no histograms).
+// Each 4096-particle tile also counts its particles per bucket of the sort (cell tile): the
+// row of the tile is written whole, the grid's totals are added to ctile_cnt.
+// mode 0: full frame (shift + bucket counts); mode 1: stage call (no counts).
 // ---------------------------------------------------------------------------------------
 // 512 threads per 4096-particle tile (8 particles each): the kernel is issue-bound, and twice
 // the warps of a 256-thread block keep about 50 warps per SM in flight over the frame's tiles.
@@ -43,9 +44,7 @@ static_assert(kPredictTile % kPredictThreads == 0, "whole particles per thread")
 
 __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restrict__ bt, int mode) {
     grid_dependency_begin();
-    __shared__ uint32_t h0[kSortMaxBins];
-    __shared__ uint32_t h1[kSortMaxBins];
-    __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (ranges of the cell pass)
+    __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (bucket of the sort)
     const int total = batch_total(bt, kStPredict);
     if (mode == 0) {
         // this frame's exact sums start at zero: the cell and newborn passes add into them
@@ -67,11 +66,8 @@ __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restric
         const int gi = grid_of_tile(bt, kStPredict, t);
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][kStPredict];
-        const int nb0 = 1 << g.d0_bits, nb1 = 1 << g.d1_bits;
         if (mode == 0) {
-            for (int i = threadIdx.x; i < nb0; i += kPredictThreads) h0[i] = 0u;
-            for (int i = threadIdx.x; i < nb1; i += kPredictThreads) h1[i] = 0u;
-            for (int i = threadIdx.x; i < g.tiles[kStCell]; i += kPredictThreads) h2[i] = 0u;
+            for (int i = threadIdx.x; i < g.ctiles; i += kPredictThreads) h2[i] = 0u;
             __syncthreads();
         }
         const float gsm1 = (float)(g.gs - 1);
@@ -117,27 +113,20 @@ __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restric
                 g.P_key[i] = key | (out ? kOutBit : 0u) | (kw & kAssocBit);
             }
             if (mode == 0) {
-                const uint32_t peers = __match_any_sync(0xffffffffu, key);
-                if (valid && lane == __ffs(peers) - 1) {
-                    const uint32_t cnt = __popc(peers);
-                    atomicAdd(&h0[key & (nb0 - 1)], cnt);
-                    atomicAdd(&h1[key >> g.d0_bits], cnt);
-                    atomicAdd(&h2[key >> kCellTileBits], cnt);
-                }
+                const uint32_t bucket = valid ? key >> kCellTileBits : 0xffffffffu;
+                const uint32_t peers = __match_any_sync(0xffffffffu, bucket);
+                if (valid && lane == __ffs(peers) - 1) atomicAdd(&h2[bucket], (uint32_t)__popc(peers));
             }
         }
         if (mode == 0) {
             __syncthreads();
-            // this tile's digit-0 counts (upsweep of sort pass 0: predict and sort tiles coincide)
-            uint32_t* row = g.hsort + (size_t)lt * kSortMaxBins;
-            for (int i = threadIdx.x; i < nb0; i += kPredictThreads) {
-                row[i] = h0[i];
-                if (h0[i]) atomicAdd(&g.hist[i], h0[i]);
+            // this tile's bucket counts (predict and scatter tiles coincide), row written whole
+            uint32_t* row = g.hsort + (size_t)lt * g.bucket_stride;
+            for (int i = threadIdx.x; i < g.ctiles; i += kPredictThreads) {
+                const uint32_t c = h2[i];
+                row[i] = c;
+                if (c) atomicAdd(&g.ctile_cnt[i], c);
             }
-            for (int i = threadIdx.x; i < nb1; i += kPredictThreads)
-                if (h1[i]) atomicAdd(&g.hist[kSortMaxBins + i], h1[i]);
-            for (int i = threadIdx.x; i < g.tiles[kStCell]; i += kPredictThreads)
-                if (h2[i]) atomicAdd(&g.ctile_cnt[i], h2[i]);
             __syncthreads();
         }
     }

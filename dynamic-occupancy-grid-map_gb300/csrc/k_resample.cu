@@ -83,13 +83,24 @@ __global__ void __launch_bounds__(kThreads, 6) k_resample(Batch* __restrict__ bt
             }
         }
         cp_async_wait_all();
+        {
+            // every cell-weight load of the thread is issued before the first shared store
+            uint32_t kw[kResIpt];
+            float w[kResIpt];
 #pragma unroll
-        for (int r = 0; r < kResIpt; ++r) {
-            const int j = r * kThreads + threadIdx.x;
-            if (base + j < N) {
-                const uint32_t kw = sm.kw[j];
-                sm.lw[pad_idx(j)] = __float_as_uint((kw & kOutBit) ? 0.0f : g.w_cell[kw & kCellMask]);
-                sm.kw[j] = kw & ~kOutBit;
+            for (int r = 0; r < kResIpt; ++r) {
+                const int j = r * kThreads + threadIdx.x;
+                kw[r] = base + j < N ? sm.kw[j] : 0u;
+            }
+#pragma unroll
+            for (int r = 0; r < kResIpt; ++r) w[r] = g.w_cell[min((int)(kw[r] & kCellMask), C - 1)];
+#pragma unroll
+            for (int r = 0; r < kResIpt; ++r) {
+                const int j = r * kThreads + threadIdx.x;
+                if (base + j < N) {
+                    sm.lw[pad_idx(j)] = __float_as_uint((kw[r] & kOutBit) ? 0.0f : w[r]);
+                    sm.kw[j] = kw[r] & ~kOutBit;
+                }
             }
         }
         // newborn items, created here, and the empty tail of the last tile

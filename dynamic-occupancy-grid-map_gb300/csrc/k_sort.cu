@@ -1,21 +1,23 @@
-// Stable particle-to-cell sort: two LSD radix passes over the cell index (<= 11-bit digits),
-// reduce-then-scan.  Replaces thrust::sort_by_key with a zip payload (dogm/src/dogm.cu:262-281).
-//   upsweep    pass 0: per-tile digit histograms written by predict (same 4096-particle tiles);
-//              pass 1: k_sort_hist counts each tile of the pass-0 output in shared memory and
-//              writes its row whole (no global atomics, no zeroing between frames)
-//   k_sort_scan  column scan of the [tile][digit] histogram -> the global output offset of
-//              every (tile, digit) pair (digit base from predict's global histogram)
-//   k_sort_pass  stable warp ranking inside the tile, scatter to offset + rank; pass 0 moves
-//              {key, index} pairs (one 8-byte store per particle), pass 1 also gathers the
-//              predicted particle state, so the payload moves once.
-// Stability makes the permutation identical to the reference's stable sort.
+// Stable particle-to-cell sort, first half: a stable bucket scatter of the predicted particles
+// by cell tile (the 1024-cell tiles of the cell pass).  The second half, a stable counting sort
+// of each bucket by cell, runs inside the cell pass (k_cells.cu), which then holds the bucket in
+// shared memory anyway.  Together they give exactly the permutation of a stable sort by cell
+// index and replace thrust::sort_by_key with its zip payload (dogm/src/dogm.cu:262-281).
+//   predict      per 4096-particle tile, the particles per bucket (row written whole) and the
+//                particles per bucket over the whole grid (ctile_cnt)
+//   k_sort_scan  column scan of the [tile][bucket] counts -> the output offset of every
+//                (tile, bucket) pair; one block also scans ctile_cnt into the first sorted
+//                position of every bucket and orders the buckets for the cell pass
+//   k_sort_scatter  stable warp ranking inside the tile, scatter of {state, key} to
+//                offset + rank: the payload moves once, read in order and written in runs
+//                (consecutive particles of the resampled set lie in few buckets)
 #include "dogm_device.cuh"
 
 namespace dogm_gb300 {
 
 // ---------------------------------------------------------------------------------------
-// Column scan: for each digit b, O[t][b] = base(b) + sum_{t' < t} H[t'][b], in place.
-// Work item = (grid, group of 32 digits); 32 warps split the tiles into contiguous chunks.
+// Column scan: for each bucket b, O[t][b] = base(b) + sum_{t' < t} H[t'][b], in place.
+// Work item = (grid, group of 32 buckets); 32 warps split the tiles into contiguous chunks.
 // ---------------------------------------------------------------------------------------
 constexpr int kScanWarps = 32;  // one warp per lane of the transposed chunk scan
 static_assert(kScanWarps == 32, "the chunk scan transposes a 32 x 32 matrix");
@@ -28,10 +30,10 @@ static_assert(kCtilePer * kScanWarps * 32 == kMaxCellTiles, "one block scans eve
 // the first sorted position of cell tile i, ctile_start[n] = N.  Also the claim order of the
 // cell pass: tiles by decreasing bit length of their particle count (the fullest, slowest
 // tiles start first; the last tiles claimed are the quickest), in any order within a class.
-// Run by one block as the last work item of the pass-1 digit scan (after predict, before
-// the cell pass).  scratch: >= 64 words.
+// Run by one block as the last work item of the bucket scan (after predict, before the
+// scatter and the cell pass).  scratch: >= 64 words.
 __device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) {
-    const int n = g.tiles[kStCell];
+    const int n = g.ctiles;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int i0 = threadIdx.x * kCtilePer;
     uint32_t* cls_count = scratch;       // 16 classes
@@ -80,27 +82,26 @@ __device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) 
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict__ bt, int pass) {
+__global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict__ bt) {
     grid_dependency_begin();
     __shared__ uint32_t chunk[kScanWarps][33];
     __shared__ uint32_t red[kScanWarps];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int stage = pass ? kStScan1 : kStScan0;
-    const int total = batch_total(bt, stage);
+    const int total = batch_total(bt, kStScan);
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
-        const int gi = grid_of_tile(bt, stage, t);
+        const int gi = grid_of_tile(bt, kStScan, t);
         const GridDesc& g = bt->g[gi];
-        const int group = t - bt->prefix[gi][stage];
-        if (pass == 1 && group == g.tiles[kStScan1] - 1) {  // block-uniform
+        const int group = t - bt->prefix[gi][kStScan];
+        if (group == g.tiles[kStScan] - 1) {  // block-uniform
             ctile_scan(g, red, &chunk[0][0]);
             continue;
         }
-        const int nb = 1 << (pass ? g.d1_bits : g.d0_bits);
+        const int nb = g.ctiles;
         const int b = group * 32 + lane;
-        const uint32_t* hist = g.hist + pass * kSortMaxBins;
+        const size_t stride = (size_t)g.bucket_stride;
         // each warp owns a contiguous chunk of tiles; up to kScanKeep counts per lane stay in
         // registers between the sum and the rewrite (one load round), more are reloaded
-        uint32_t* H = g.hsort + (size_t)pass * g.sort_tiles * kSortMaxBins;
+        uint32_t* H = g.hsort;
         const int T = g.sort_tiles;
         const int per = (T + kScanWarps - 1) / kScanWarps;
         const int t0 = warp * per, t1 = min(T, t0 + per);
@@ -109,24 +110,22 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict
         uint32_t s = 0;
         if (keep) {
 #pragma unroll
-            for (int i = 0; i < kScanKeep; ++i)
-                v[i] = (b < nb && t0 + i < t1) ? H[(size_t)(t0 + i) * kSortMaxBins + b] : 0u;
+            for (int i = 0; i < kScanKeep; ++i) v[i] = (b < nb && t0 + i < t1) ? H[(t0 + i) * stride + b] : 0u;
 #pragma unroll
             for (int i = 0; i < kScanKeep; ++i) s += v[i];
         } else if (b < nb) {
             for (int tb = t0; tb < t1; tb += kScanBatch) {
                 uint32_t w[kScanBatch];
 #pragma unroll
-                for (int i = 0; i < kScanBatch; ++i)
-                    w[i] = (tb + i < t1) ? H[(size_t)(tb + i) * kSortMaxBins + b] : 0u;
+                for (int i = 0; i < kScanBatch; ++i) w[i] = (tb + i < t1) ? H[(tb + i) * stride + b] : 0u;
 #pragma unroll
                 for (int i = 0; i < kScanBatch; ++i) s += w[i];
             }
         }
-        // digit base: sum of the global histogram over digits < b (loads issued alongside)
+        // bucket base: particles in buckets < b over the whole grid (loads issued alongside)
         uint32_t part = 0;
-        for (int i = threadIdx.x; i < group * 32; i += blockDim.x) part += hist[i];
-        const uint32_t own = (b < nb) ? hist[b] : 0u;
+        for (int i = threadIdx.x; i < group * 32; i += blockDim.x) part += g.ctile_cnt[i];
+        const uint32_t own = (b < nb) ? g.ctile_cnt[b] : 0u;
         for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
         uint32_t lanepre = own;
         for (int o = 1; o < 32; o <<= 1) {
@@ -140,9 +139,9 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict
         uint32_t base_all = red[lane];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) base_all += __shfl_xor_sync(0xffffffffu, base_all, o);
-        // the counts of this lane's digit in the chunks of the warps before this one: warp w
-        // scans digit w across the 32 chunks (one per lane; the padded rows keep the transposed
-        // reads free of bank conflicts) and writes the exclusive prefixes back in place
+        // the counts of this lane's bucket in the chunks of the warps before this one: warp w
+        // scans bucket w across the 32 chunks (one per lane; the padded rows keep the
+        // transposed reads free of bank conflicts) and writes the exclusive prefixes back
         const uint32_t c = chunk[lane][warp];
         uint32_t inc = c;
 #pragma unroll
@@ -158,18 +157,17 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict
             if (keep) {
 #pragma unroll
                 for (int i = 0; i < kScanKeep; ++i) {
-                    if (t0 + i < t1) H[(size_t)(t0 + i) * kSortMaxBins + b] = pre;
+                    if (t0 + i < t1) H[(t0 + i) * stride + b] = pre;
                     pre += v[i];
                 }
             } else {
                 for (int tb = t0; tb < t1; tb += kScanBatch) {
                     uint32_t w[kScanBatch];
 #pragma unroll
-                    for (int i = 0; i < kScanBatch; ++i)
-                        w[i] = (tb + i < t1) ? H[(size_t)(tb + i) * kSortMaxBins + b] : 0u;
+                    for (int i = 0; i < kScanBatch; ++i) w[i] = (tb + i < t1) ? H[(tb + i) * stride + b] : 0u;
 #pragma unroll
                     for (int i = 0; i < kScanBatch; ++i) {
-                        if (tb + i < t1) H[(size_t)(tb + i) * kSortMaxBins + b] = pre;
+                        if (tb + i < t1) H[(tb + i) * stride + b] = pre;
                         pre += w[i];
                     }
                 }
@@ -180,106 +178,110 @@ __global__ void __launch_bounds__(kScanWarps * 32) k_sort_scan(Batch* __restrict
 }
 
 // ---------------------------------------------------------------------------------------
-// Downsweep: one tile of 4096 keys per block iteration.
+// Bucket scatter: one tile of 4096 particles per block iteration, 512 threads (8 particles
+// each), warp-striped: item k of lane l of warp w is tile position w * 256 + k * 32 + l.
+// Shared memory (dynamic, W = the batch's largest bucket count rounded up to 8):
+//   whist  u16 [16][W]  per-warp bucket counts, then each warp's offset within the tile
+//   gbase  u32 [W]      output offset of each bucket for this tile (from the column scan)
 // ---------------------------------------------------------------------------------------
-struct SortSmem {
-    uint16_t whist[kThreads / 32][kSortMaxBins];  // per-warp digit counts, then warp offsets
-    uint32_t gbase[kSortMaxBins];                  // global offset of each digit for this tile
-    uint16_t rank[kSortTile];                      // rank of each key among its warp's equal digits
-};
+constexpr int kScatterThreads = 512;
+constexpr int kScatterWarps = kScatterThreads / 32;
+constexpr int kScatterIpt = kSortTile / kScatterThreads;
+static_assert(kScatterIpt * kScatterThreads == kSortTile, "whole particles per thread");
 
-// Four blocks per SM: a 2M-particle frame's 489 tiles run in one wave.
-template <bool FINAL>
-__global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ bt) {
+__host__ __device__ __forceinline__ int scatter_width(int max_ctiles) { return (max_ctiles + 7) & ~7; }
+__host__ __device__ __forceinline__ size_t scatter_smem(int W) {
+    return (size_t)kScatterWarps * W * sizeof(uint16_t) + (size_t)W * sizeof(uint32_t);
+}
+
+__global__ void __launch_bounds__(kScatterThreads, 2) k_sort_scatter(Batch* __restrict__ bt, int W) {
     grid_dependency_begin();
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    SortSmem& sm = *reinterpret_cast<SortSmem*>(smem_raw);
-    const int stage = FINAL ? kStSort1 : kStSort0;
-    const int pass = FINAL ? 1 : 0;
-    const int total = batch_total(bt, stage);
+    uint16_t* whist = reinterpret_cast<uint16_t*>(smem_raw);
+    uint32_t* gbase = reinterpret_cast<uint32_t*>(smem_raw + (size_t)kScatterWarps * W * sizeof(uint16_t));
+    const int total = batch_total(bt, kStSort);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt_mask = (1u << lane) - 1u;
+    uint16_t* my_hist = whist + warp * W;
 
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
-        const int gi = grid_of_tile(bt, stage, t);
+        const int gi = grid_of_tile(bt, kStSort, t);
         const GridDesc& g = bt->g[gi];
-        const int lt = t - bt->prefix[gi][stage];
-        const int bits = pass ? g.d1_bits : g.d0_bits;
-        const int shift = pass ? g.d0_bits : 0;
-        const int nb = 1 << bits;
-        const uint32_t* O = g.hsort + (size_t)pass * g.sort_tiles * kSortMaxBins + (size_t)lt * kSortMaxBins;
-        for (int i = threadIdx.x; i < nb; i += kThreads) sm.gbase[i] = O[i];
-        uint4* wz = reinterpret_cast<uint4*>(&sm.whist[0][0]);  // all warp counts, 16 bytes a store
-        for (int i = threadIdx.x; i < (int)(sizeof(sm.whist) / sizeof(uint4)); i += kThreads)
-            wz[i] = make_uint4(0u, 0u, 0u, 0u);
+        const int lt = t - bt->prefix[gi][kStSort];
+        const int nb = g.ctiles;
+        const uint32_t* O = g.hsort + (size_t)lt * g.bucket_stride;
+        for (int i = threadIdx.x; i < nb; i += kScatterThreads) gbase[i] = O[i];
+        uint4* wz = reinterpret_cast<uint4*>(whist);  // all warp counts, 16 bytes a store
+        for (int i = threadIdx.x; i < kScatterWarps * W / 8; i += kScatterThreads) wz[i] = make_uint4(0u, 0u, 0u, 0u);
         __syncthreads();
 
-        // load the tile warp-striped (item k of lane l: warp base + k*32 + l)
-        const int base = lt * kSortTile + warp * (32 * kSortIpt);
-        uint16_t* rank = sm.rank + warp * (32 * kSortIpt) + lane;  // item k at rank[k * 32]
-        // one base pointer per thread, items at constant offsets (k * 32 particles)
-        const uint32_t* src_kw = FINAL ? reinterpret_cast<const uint32_t*>(g.T_pair + base + lane) : g.P_key + base + lane;
-        constexpr int kw_stride = FINAL ? 64 : 32;  // words between a lane's items
-        uint32_t key[kSortIpt];
+        const int base = lt * kSortTile + warp * (32 * kScatterIpt);
+        uint32_t key[kScatterIpt];
+        uint16_t rank[kScatterIpt];
 #pragma unroll
-        for (int k = 0; k < kSortIpt; ++k)
-            key[k] = base + k * 32 + lane < g.N ? src_kw[k * kw_stride] : 0xffffffffu;
-        // stable rank within the warp: rounds in input order, peers by match_any
+        for (int k = 0; k < kScatterIpt; ++k) {
+            const int pos = base + k * 32 + lane;
+            key[k] = pos < g.N ? g.P_key[pos] : 0xffffffffu;
+        }
+        // stable rank within the warp: rounds in input order, peers by match_any (a key whose
+        // bucket lies outside the grid -- only injected state can hold one -- is not placed)
 #pragma unroll
-        for (int k = 0; k < kSortIpt; ++k) {
-            const bool valid = base + k * 32 + lane < g.N;
-            const uint32_t d = valid ? (((key[k] & kCellMask) >> shift) & (uint32_t)(nb - 1)) : 0xffffffffu;
+        for (int k = 0; k < kScatterIpt; ++k) {
+            const uint32_t b = (key[k] & kCellMask) >> kCellTileBits;
+            const bool valid = base + k * 32 + lane < g.N && b < (uint32_t)nb;
+            const uint32_t d = valid ? b : 0xffffffffu;
             const uint32_t peers = __match_any_sync(0xffffffffu, d);
             uint16_t before = 0;
-            if (valid) before = sm.whist[warp][d];
-            rank[k * 32] = (uint16_t)(before + __popc(peers & lt_mask));
+            if (valid) before = my_hist[d];
+            rank[k] = (uint16_t)(before + __popc(peers & lt_mask));
             __syncwarp();
-            if (valid && lane == __ffs(peers) - 1) sm.whist[warp][d] = (uint16_t)(before + __popc(peers));
+            if (valid && lane == __ffs(peers) - 1) my_hist[d] = (uint16_t)(before + __popc(peers));
             __syncwarp();
         }
         __syncthreads();
-        // per digit: exclusive offsets across the warps of the tile
-        for (int b = threadIdx.x; b < nb; b += kThreads) {
+        // per bucket: exclusive offsets across the warps of the tile
+        for (int b = threadIdx.x; b < nb; b += kScatterThreads) {
             uint32_t acc = 0;
 #pragma unroll
-            for (int w = 0; w < kThreads / 32; ++w) {
-                const uint32_t c = sm.whist[w][b];
-                sm.whist[w][b] = (uint16_t)acc;
+            for (int w = 0; w < kScatterWarps; ++w) {
+                const uint32_t c = whist[w * W + b];
+                whist[w * W + b] = (uint16_t)acc;
                 acc += c;
             }
         }
         __syncthreads();
 
-        // scatter to the global sorted position.  The final pass's arrays do not overlap:
-        // restrict lets the compiler issue the index loads and state gathers of several items
-        // before their stores.
-        const uint32_t* __restrict__ t_idx = src_kw + 1;  // .y words of the pass-0 pairs (final pass)
+        // scatter {state, key} (and, for debugging, the particle's index) to its bucket slot;
+        // per half of the items, every state load is issued before the first store (a load
+        // behind its own store's guard would wait for the one before it)
         const float4* __restrict__ p_state = g.P_state;
-        float4* __restrict__ s_state = g.S_state;
-        uint32_t* __restrict__ s_key = g.S_key;
-        uint2* __restrict__ t_pair = g.T_pair;
-        const int pos0 = base + lane;
+        float4* __restrict__ t_state = g.T_state;
+        uint32_t* __restrict__ t_key = g.T_key;
+        constexpr int kHalf = kScatterIpt / 2;
 #pragma unroll
-        for (int k = 0; k < kSortIpt; ++k) {
-            const int pos = base + k * 32 + lane;
-            const bool valid = pos < g.N;
-            uint32_t out = 0xffffffffu;
-            if (valid) {
-                const uint32_t d = ((key[k] & kCellMask) >> shift) & (uint32_t)(nb - 1);
-                out = sm.gbase[d] + sm.whist[warp][d] + rank[k * 32];
-                if (out >= (uint32_t)g.N) {  // only an inconsistent histogram can get here
-                    flag_status(g, kStatusBounds);
-                    out = 0xffffffffu;
-                }
+        for (int h = 0; h < 2; ++h) {
+            float4 st[kHalf];
+            uint32_t out[kHalf];
+#pragma unroll
+            for (int j = 0; j < kHalf; ++j) {
+                const int k = h * kHalf + j;
+                const int pos = base + k * 32 + lane;
+                const uint32_t d = (key[k] & kCellMask) >> kCellTileBits;
+                out[j] = 0xffffffffu;
+                if (pos < g.N && d < (uint32_t)nb) out[j] = gbase[d] + my_hist[d] + rank[k];
+                st[j] = p_state[pos < g.N ? pos : g.N - 1];
             }
-            if (out != 0xffffffffu) {
-                if (FINAL) {
-                    const uint32_t src = t_idx[k * kw_stride];  // particle index carried by pass 0
-                    s_key[out] = key[k];
-                    s_state[out] = __ldg(p_state + src);
-                    if (g.dbg_perm) g.dbg_perm[out] = (int)src;
-                } else {
-                    t_pair[out] = make_uint2(key[k], (uint32_t)(pos0 + k * 32));
+#pragma unroll
+            for (int j = 0; j < kHalf; ++j) {
+                const int k = h * kHalf + j;
+                const int pos = base + k * 32 + lane;
+                if (pos >= g.N) continue;
+                if (out[j] < (uint32_t)g.N) {
+                    t_key[out[j]] = key[k];
+                    t_state[out[j]] = st[j];
+                    if (g.T_idx) g.T_idx[out[j]] = pos;
+                } else {  // a bucket outside the grid, or an inconsistent histogram
+                    flag_status(g, kStatusBounds);
                 }
             }
         }
@@ -287,64 +289,19 @@ __global__ void __launch_bounds__(kThreads, 4) k_sort_pass(Batch* __restrict__ b
     }
 }
 
-// ---------------------------------------------------------------------------------------
-// Pass-1 digit counts: one tile of the pass-0 output per block iteration, counted in shared
-// memory; the row H1[tile][0 .. 2^d1) is written whole.
-// ---------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_sort_hist(Batch* __restrict__ bt) {
-    grid_dependency_begin();
-    __shared__ uint32_t cnt[kSortMaxBins];
-    const int total = batch_total(bt, kStSort1);
-    for (int t = blockIdx.x; t < total; t += gridDim.x) {
-        const int gi = grid_of_tile(bt, kStSort1, t);
-        const GridDesc& g = bt->g[gi];
-        const int lt = t - bt->prefix[gi][kStSort1];
-        const int nb1 = 1 << g.d1_bits;
-        const int shift1 = g.d0_bits;
-        for (int i = threadIdx.x; i < nb1; i += kThreads) cnt[i] = 0u;
-        const int base = lt * kSortTile;
-        const uint32_t* kw = reinterpret_cast<const uint32_t*>(g.T_pair + base + threadIdx.x);
-        uint32_t key[kSortIpt];
-#pragma unroll
-        for (int k = 0; k < kSortIpt; ++k)
-            key[k] = base + k * kThreads + (int)threadIdx.x < g.N ? kw[2 * k * kThreads] : 0xffffffffu;
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < kSortIpt; ++k)
-            if (base + k * kThreads + (int)threadIdx.x < g.N)
-                atomicAdd(&cnt[((key[k] & kCellMask) >> shift1) & (uint32_t)(nb1 - 1)], 1u);
-        __syncthreads();
-        uint32_t* H1 = g.hsort + (size_t)g.sort_tiles * kSortMaxBins + (size_t)lt * kSortMaxBins;
-        for (int i = threadIdx.x; i < nb1; i += kThreads) H1[i] = cnt[i];
-        __syncthreads();
-    }
+cudaError_t launch_sort_scan(const Batch* d_batch, const LaunchCfg& cfg) {
+    return launch_kernel(cfg, k_sort_scan, launch_blocks(cfg, 2), kScanWarps * 32, 0, const_cast<Batch*>(d_batch));
 }
 
-cudaError_t launch_sort_scan(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
-    return launch_kernel(cfg, k_sort_scan, launch_blocks(cfg, 2), kScanWarps * 32, 0, const_cast<Batch*>(d_batch), pass);
+cudaError_t prepare_sort() {
+    return cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)scatter_smem(scatter_width(kMaxCellTiles)));
 }
 
-cudaError_t launch_sort_pass(const Batch* d_batch, int pass, const LaunchCfg& cfg) {
-    const size_t smem = sizeof(SortSmem);  // 48 KB: no opt-in attribute needed
-    Batch* b = const_cast<Batch*>(d_batch);
-    if (pass == 0)
-        return launch_kernel(cfg, k_sort_pass<false>, launch_blocks(cfg, 4), kThreads, smem, b);
-    else
-        return launch_kernel(cfg, k_sort_pass<true>, launch_blocks(cfg, 4), kThreads, smem, b);
-}
-
-cudaError_t launch_sort_offsets1(const Batch* d_batch, const LaunchCfg& cfg) {
-    cudaError_t e = launch_kernel(cfg, k_sort_hist, launch_blocks(cfg, 4), kThreads, 0, const_cast<Batch*>(d_batch));
-    if (e != cudaSuccess) return e;
-    return launch_sort_scan(d_batch, 1, cfg);
-}
-
-cudaError_t launch_sort(const Batch* d_batch, const LaunchCfg& cfg) {
-    cudaError_t e;
-    if ((e = launch_sort_scan(d_batch, 0, cfg)) != cudaSuccess) return e;
-    if ((e = launch_sort_pass(d_batch, 0, cfg)) != cudaSuccess) return e;
-    if ((e = launch_sort_offsets1(d_batch, cfg)) != cudaSuccess) return e;
-    return launch_sort_pass(d_batch, 1, cfg);
+cudaError_t launch_sort_scatter(const Batch* d_batch, int max_ctiles, const LaunchCfg& cfg) {
+    const int W = scatter_width(max_ctiles);
+    return launch_kernel(cfg, k_sort_scatter, launch_blocks(cfg, 2), kScatterThreads, scatter_smem(W),
+                         const_cast<Batch*>(d_batch), W);
 }
 
 }  // namespace dogm_gb300

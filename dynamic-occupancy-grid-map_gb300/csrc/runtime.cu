@@ -39,9 +39,8 @@ int bitlen(unsigned long long v) {
 
 int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
 
-constexpr int kStages = 8;
-const char* const kStageNames[kStages] = {"predict",    "sort_scan0", "sort_pass0", "sort_scan1",
-                                          "sort_pass1", "cells",      "newborn",    "resample"};
+constexpr int kStages = 6;
+const char* const kStageNames[kStages] = {"predict", "sort_scan", "sort_scatter", "cells", "newborn", "resample"};
 
 // One launch context: a device copy of a Batch, two pinned host mirrors (the host fills one
 // while the device may still read the other, so frame k+1 is queued while frame k runs) and
@@ -66,6 +65,9 @@ struct Ctx {
     bool pdl = true;
     // steady-state frames as CUDA graph launches (dogm_set_launch_mode; plain launches otherwise)
     bool use_graphs = true;
+    // bucket-count class of the batch being built: the bucket scatter's shared memory is sized
+    // for 2048 buckets, or 4096 when a grid of the batch has more than 2048 cell tiles
+    int scatter_ctiles = 2048;
 
     // Captured graphs hold the launch widths: drop them when the widths change.
     void drop_graphs() {
@@ -167,7 +169,7 @@ dogm_status dalloc(dogm_handle* h, T** p, size_t count) {
 }
 
 struct Sizes {
-    int gs, N, B, C, key_bits, sort_tiles, cell_tiles, res_tiles, pred_tiles, scan0, scan1;
+    int gs, N, B, C, key_bits, sort_tiles, cell_tiles, res_tiles, pred_tiles, scan;
 };
 
 dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
@@ -186,19 +188,15 @@ dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
     s.sort_tiles = div_up(s.N, kSortTile);
     s.cell_tiles = div_up(s.C, kCellTile);
     s.res_tiles = div_up((long long)s.N + s.B, kResTile);
-    const int d0 = (s.key_bits + 1) / 2, d1 = s.key_bits - d0;
-    s.scan0 = div_up(1 << d0, 32);  // digit groups of the column scans
-    s.scan1 = div_up(1 << d1, 32) + 1;  // + the cell-tile start scan
+    s.scan = div_up(s.cell_tiles, 32) + 1;  // bucket groups of the column scan + the cell-tile start scan
     return DOGM_OK;
 }
 
 void set_tiles(GridDesc& g, const Sizes& s) {
     for (int i = 0; i < kNumStages; ++i) g.tiles[i] = 0;
     g.tiles[kStPredict] = s.pred_tiles;
-    g.tiles[kStScan0] = s.scan0;
-    g.tiles[kStSort0] = s.sort_tiles;
-    g.tiles[kStScan1] = s.scan1;
-    g.tiles[kStSort1] = s.sort_tiles;
+    g.tiles[kStScan] = s.scan;
+    g.tiles[kStSort] = s.sort_tiles;
     g.tiles[kStCell] = s.cell_tiles;
     g.tiles[kStBirth] = s.cell_tiles;
     g.tiles[kStResample] = s.res_tiles;
@@ -257,6 +255,9 @@ void build_batch(Ctx& c, dogm_handle* const* hs, int n, const std::vector<int>& 
     Batch& b = *c.h_batch[c.cur];
     b.n_grids = n;
     b.status = 0u;
+    c.scatter_ctiles = 2048;
+    for (int i = 0; i < n; ++i)
+        if (hs[i]->desc.ctiles > c.scatter_ctiles) c.scatter_ctiles = kMaxCellTiles;
     for (int s = 0; s < kNumStages; ++s) b.counters[s] = 0u;
     for (int s = 0; s < kNumStages; ++s) b.prefix[0][s] = 0;
     for (int i = 0; i < n; ++i) {
@@ -285,8 +286,8 @@ cudaError_t download_status(Ctx& c) {
                            c.stream);
 }
 
-// The steady-state frame: 9 kernels in 8 stages; with profiling, a CUDA event before each
-// stage and at the end.
+// The steady-state frame: 6 kernels; with profiling, a CUDA event before each stage and at the
+// end.
 cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
     LaunchCfg cfg{c.num_sms, c.stream};
     const bool prof = c.profile && !with_init;
@@ -303,13 +304,11 @@ cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
     if ((with_begin || with_init) && (e = launch_frame_begin(c.d_batch, 0, cfg)) != cudaSuccess) return e;
     if (with_init && (e = launch_init_particles(c.d_batch, cfg)) != cudaSuccess) return e;
     STAGE(0, launch_predict(c.d_batch, 0, cfg));
-    STAGE(1, launch_sort_scan(c.d_batch, 0, cfg));
-    STAGE(2, launch_sort_pass(c.d_batch, 0, cfg));
-    STAGE(3, launch_sort_offsets1(c.d_batch, cfg));
-    STAGE(4, launch_sort_pass(c.d_batch, 1, cfg));
-    STAGE(5, launch_cells(c.d_batch, cfg));
-    STAGE(6, launch_newborn(c.d_batch, cfg));
-    STAGE(7, launch_resample(c.d_batch, cfg));
+    STAGE(1, launch_sort_scan(c.d_batch, cfg));
+    STAGE(2, launch_sort_scatter(c.d_batch, c.scatter_ctiles, cfg));
+    STAGE(3, launch_cells(c.d_batch, cfg));
+    STAGE(4, launch_newborn(c.d_batch, cfg));
+    STAGE(5, launch_resample(c.d_batch, cfg));
 #undef STAGE
     if (prof && (e = cudaEventRecord(c.ev[kStages], c.stream)) != cudaSuccess) return e;
     return cudaSuccess;
@@ -323,6 +322,11 @@ int graph_bucket(int n) {
     int b = 1;
     while (b < n) b <<= 1;
     return std::min(b, kMaxBatch);
+}
+
+// A graph is keyed by its batch-size bucket, mirror and bucket-scatter class.
+int graph_key(int nb, int mirror, int scatter_ctiles) {
+    return (scatter_ctiles > 2048 ? 1 << 20 : 0) + nb * 2 + mirror;
 }
 
 // A device-to-host copy queued after a frame's kernels and before its completion event.
@@ -346,7 +350,7 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
         *launches = kLaunchesPerFrame + (any_init || any_clear ? 1 : 0) + (any_init ? kLaunchesInit : 0);
     } else {
         const int nb = graph_bucket(n);
-        const int key = nb * 2 + c.cur;
+        const int key = graph_key(nb, c.cur, c.scatter_ctiles);
         auto it = c.graphs.find(key);
         if (it == c.graphs.end()) {
             cudaGraph_t graph;
@@ -466,11 +470,11 @@ size_t dogm_state_bytes(const dogm_params* p) {
     if (derive_sizes(*p, s) != DOGM_OK) return 0;
     const size_t N = (size_t)s.N, B = (size_t)s.B, C = (size_t)s.C;
     size_t b = 0;
-    b += N * (16 + 4) + N * (4 + 4) + N * (16 + 4);    // P, T, S particles
+    b += 3 * N * (16 + 4);                            // P, T (bucketed), S (sorted) particles
     b += B * (16 + 4 + 4);                            // newborns
     // per cell: record 64, measurement copy 16, free mass 2 x 4, {newborn mass, p_A} 8, cell weight 4
     b += C * (sizeof(dogm_grid_cell) + sizeof(dogm_measurement_cell) + 2 * 4 + 8 + 4);
-    b += 2 * kSortMaxBins * 4 + (size_t)2 * s.sort_tiles * kSortMaxBins * 4;
+    b += (size_t)s.sort_tiles * (size_t)((s.cell_tiles + 3) & ~3) * 4;  // per-tile bucket counts
     b += (size_t)s.cell_tiles * (16 + 12) + 4 + (size_t)s.res_tiles * 8;
     b += sizeof(Batch);
     return b;
@@ -490,13 +494,13 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     h->gs = s.gs; h->N = s.N; h->B = s.B; h->C = s.C;
     auto cleanup = [&](dogm_status s2) { dogm_destroy(h); return s2; };
     if ((st = ctx_init(h->ctx, h->device)) != DOGM_OK) return cleanup(st);
-    if (prepare_kernels() != cudaSuccess || prepare_cells() != cudaSuccess)
+    if (prepare_kernels() != cudaSuccess || prepare_cells() != cudaSuccess || prepare_sort() != cudaSuccess)
         return cleanup(fail(DOGM_ERR_CUDA, "kernel attribute setup failed"));
 
     GridDesc& g = h->desc;
     g.N = s.N; g.B = s.B; g.C = s.C; g.gs = s.gs;
-    g.d0_bits = (s.key_bits + 1) / 2;
-    g.d1_bits = s.key_bits - g.d0_bits;
+    g.ctiles = s.cell_tiles;
+    g.bucket_stride = (s.cell_tiles + 3) & ~3;
     g.q_shift = 61 - bitlen((unsigned long long)s.C);
     g.gs_div = (1ull << 42) / (unsigned long long)s.gs + 1ull;
     g.p_S = params->persistence_prob;
@@ -512,7 +516,7 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
 
 #define ALLOC(ptr, n) if ((st = dalloc(h, &(ptr), (n))) != DOGM_OK) return cleanup(st)
     ALLOC(g.P_state, s.N); ALLOC(g.P_key, s.N);
-    ALLOC(g.T_pair, s.N);
+    ALLOC(g.T_state, s.N); ALLOC(g.T_key, s.N);
     ALLOC(g.S_state, s.N); ALLOC(g.S_key, s.N);
     ALLOC(g.B_state, s.B); ALLOC(g.B_key, s.B); ALLOC(g.B_w, s.B);
     ALLOC(g.cells, s.C);
@@ -524,8 +528,7 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     ALLOC(fa, s.C); ALLOC(fb, s.C);
     g.free_old = fa; g.free_new = fb;
     ALLOC(g.rho_b, s.C); ALLOC(g.w_cell, s.C);
-    ALLOC(g.hist, 2 * kSortMaxBins);
-    ALLOC(g.hsort, (size_t)2 * s.sort_tiles * kSortMaxBins);
+    ALLOC(g.hsort, (size_t)s.sort_tiles * g.bucket_stride);
     ALLOC(g.ctile_cnt, s.cell_tiles); ALLOC(g.ctile_start, (size_t)s.cell_tiles + 1);
     ALLOC(g.ctile_order, s.cell_tiles);
     ALLOC(g.cell_sum, 2 * (size_t)s.cell_tiles);
@@ -948,10 +951,12 @@ dogm_status dogm_debug_enable(dogm_handle* h, int enable) {
     if (enable && !h->debug) {
         dogm_status st;
         if ((st = dalloc(h, &h->desc.dbg_perm, h->N)) != DOGM_OK) return st;
+        if ((st = dalloc(h, &h->desc.T_idx, h->N)) != DOGM_OK) return st;
         if ((st = dalloc(h, &h->desc.dbg_src, h->N)) != DOGM_OK) return st;
         h->debug = true;
     } else if (!enable) {
         h->desc.dbg_perm = nullptr;
+        h->desc.T_idx = nullptr;
         h->desc.dbg_src = nullptr;
         h->debug = false;
     }
@@ -1180,24 +1185,6 @@ dogm_status dogm_extract_dynamic_cells(dogm_handle* h, float min_occupancy, floa
 
 // ---- autotuning ----------------------------------------------------------------------------
 
-static int key_bits_of(const dogm_handle* h) { return std::max(1, bitlen((unsigned long long)(h->C - 1))); }
-
-// Radix split of the cell-key sort: low digit d0 (0: the default, half rounded up), high digit
-// key_bits - d0; both at most kSortMaxBits.  The digit-scan tile counts follow the split.
-static dogm_status apply_split(dogm_handle* h, int d0) {
-    const int kb = key_bits_of(h);
-    if (d0 == 0) d0 = (kb + 1) / 2;
-    const int d1 = kb - d0;
-    if (d0 < 1 || d0 > kSortMaxBits || d1 < 0 || d1 > kSortMaxBits || (d1 == 0 && kb > 1))
-        return fail(DOGM_ERR_INVALID_ARGUMENT, "radix_low_bits " + std::to_string(d0) + " does not split a " +
-                                                   std::to_string(kb) + "-bit cell key into two digits of <= 11 bits");
-    h->desc.d0_bits = d0;
-    h->desc.d1_bits = d1;
-    h->desc.tiles[kStScan0] = div_up(1 << d0, 32);
-    h->desc.tiles[kStScan1] = div_up(1 << d1, 32) + 1;  // + the cell-tile start scan
-    return DOGM_OK;
-}
-
 // ms per update over `reps` graph-launched updates on the resident measurement grid.
 static dogm_status time_updates(dogm_handle* h, int reps, float* ms) {
     Ctx& c = h->ctx;
@@ -1221,7 +1208,7 @@ static std::string tune_key(const dogm_handle* h) {
     std::string name = cudaGetDeviceProperties(&prop, h->device) == cudaSuccess ? prop.name : "unknown";
     for (char& ch : name)
         if (ch == '|' || ch == '\n') ch = '_';
-    return "dogm-tune v1|" + name + "|gs=" + std::to_string(h->gs) + "|N=" + std::to_string(h->N) +
+    return "dogm-tune v2|" + name + "|gs=" + std::to_string(h->gs) + "|N=" + std::to_string(h->N) +
            "|B=" + std::to_string(h->B);
 }
 
@@ -1229,23 +1216,19 @@ dogm_status dogm_get_tune(dogm_handle* h, dogm_tune* out) {
     if (!h || !out) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
     std::memset(out, 0, sizeof(*out));
     for (int i = 0; i < kStages; ++i) out->blocks_per_sm[i] = h->ctx.mult[i];
-    out->radix_low_bits = h->desc.d0_bits == (key_bits_of(h) + 1) / 2 ? 0 : h->desc.d0_bits;
     return DOGM_OK;
 }
 
 dogm_status dogm_set_tune(dogm_handle* h, const dogm_tune* t) {
     if (!h || !t) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
-    for (int i = 0; i < kStages; ++i)
-        if (t->blocks_per_sm[i] < 0 || t->blocks_per_sm[i] > 32)
-            return fail(DOGM_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 32]");
+    for (int i = 0; i < 8; ++i)
+        if (t->blocks_per_sm[i] < 0 || t->blocks_per_sm[i] > 32 || (i >= kStages && t->blocks_per_sm[i] != 0))
+            return fail(DOGM_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 32] for the 6 stages and 0 after them");
+    if (t->radix_low_bits != 0)
+        return fail(DOGM_ERR_INVALID_ARGUMENT, "radix_low_bits must be 0: the particle sort is one bucket pass");
     DeviceGuard dg(h->device);
     dogm_status st = dogm_synchronize(h);  // no frame of the old shape in flight
     if (st != DOGM_OK) return st;
-    const int d0_old = h->desc.d0_bits;
-    if ((st = apply_split(h, t->radix_low_bits)) != DOGM_OK) {
-        apply_split(h, d0_old);
-        return st;
-    }
     for (int i = 0; i < kStages; ++i) h->ctx.mult[i] = t->blocks_per_sm[i];
     h->ctx.drop_graphs();
     return DOGM_OK;
@@ -1297,24 +1280,7 @@ dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int
     float ms_def = 0.f;
     if ((st = time_updates(s, reps, &ms_def)) != DOGM_OK) return st;
 
-    // 1: radix split, whole-update time
-    const int kb = key_bits_of(s);
-    const int d0_def = (kb + 1) / 2;
-    int best_d0 = d0_def;
-    float best_ms = ms_def;
-    for (int d0 = std::max(1, kb - kSortMaxBits); d0 <= std::min(kSortMaxBits, kb - 1); ++d0) {
-        if (d0 == d0_def) continue;
-        if ((st = apply_split(s, d0)) != DOGM_OK) return st;
-        float ms = 0.f;
-        if ((st = time_updates(s, reps, &ms)) != DOGM_OK) return st;
-        if (ms < 0.99f * best_ms) {
-            best_ms = ms;
-            best_d0 = d0;
-        }
-    }
-    if ((st = apply_split(s, best_d0)) != DOGM_OK) return st;
-
-    // 2: each stage's width, timed by the per-stage events (plain launches)
+    // each stage's width, timed by the per-stage events (plain launches)
     static const int kCand[] = {1, 2, 3, 4, 6, 8};
     int best_mult[kStages] = {};
     s->ctx.profile = true;
@@ -1349,7 +1315,6 @@ dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int
     dogm_tune t{};
     if (ms_tuned < 0.995f * ms_def) {
         for (int i = 0; i < kStages; ++i) t.blocks_per_sm[i] = best_mult[i];
-        t.radix_low_bits = best_d0 == d0_def ? 0 : best_d0;
         t.ms_tuned = ms_tuned;
     } else {
         t.ms_tuned = ms_def;  // nothing beat the defaults
@@ -1420,7 +1385,7 @@ dogm_status slot_create(int device, BatchSlot** out) {
     BatchSlot* s = new BatchSlot();
     dogm_status st = ctx_init(s->ctx, device);
     if (st != DOGM_OK) { delete s; return st; }
-    if (prepare_kernels() != cudaSuccess || prepare_cells() != cudaSuccess) {
+    if (prepare_kernels() != cudaSuccess || prepare_cells() != cudaSuccess || prepare_sort() != cudaSuccess) {
         delete s;
         return fail(DOGM_ERR_CUDA, "kernel attribute setup failed");
     }
@@ -1494,7 +1459,8 @@ dogm_status slot_prewarm(BatchSlot* s, int max_n) {
     const int cur = c.cur;
     for (int m = 0; m < 2; ++m) {
         for (int nb = 1; nb <= graph_bucket(std::max(1, max_n)); nb <<= 1) {
-            const int key = nb * 2 + m;
+            c.scatter_ctiles = 2048;  // streams of the serving loop have at most 2048 cell tiles
+            const int key = graph_key(nb, m, c.scatter_ctiles);
             if (c.graphs.count(key)) continue;
             c.cur = m;
             cudaGraph_t graph;
