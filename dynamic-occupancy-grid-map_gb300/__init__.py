@@ -41,7 +41,9 @@ ABI_SYMBOLS = [
     "dogm_get_grid_cells", "dogm_get_grid_cells_device", "dogm_get_grid_cells_async", "dogm_get_measurement_cells", "dogm_get_particles",
     "dogm_get_grid_size", "dogm_get_resolution", "dogm_get_position_x", "dogm_get_position_y", "dogm_get_yaw",
     "dogm_get_iteration", "dogm_get_particle_count", "dogm_get_new_born_particle_count", "dogm_particle_prediction",
-    "dogm_update_pose", "dogm_update_pose_noalloc", "dogm_initialize_particles", "dogm_set_measurement_cells", "dogm_set_particles",
+    "dogm_update_pose", "dogm_update_pose_noalloc", "dogm_initialize_particles", "dogm_particle_assignment",
+    "dogm_grid_cell_occupancy_update", "dogm_update_persistent_particles", "dogm_initialize_new_particles",
+    "dogm_statistical_moments", "dogm_resampling", "dogm_set_measurement_cells", "dogm_set_particles",
     "dogm_set_replay", "dogm_clear_replay", "dogm_generate_draws", "dogm_debug_enable", "dogm_debug_export",
     "dogm_debug_joint_weights",
     "dogm_lower_bound_f32", "dogm_host_alloc", "dogm_host_free", "dogm_device_alloc", "dogm_device_free",
@@ -134,7 +136,10 @@ def load(path: str | None = None) -> C.CDLL:
         "dogm_get_particle_count": ([vp], i), "dogm_get_new_born_particle_count": ([vp], i),
         "dogm_particle_prediction": ([vp, f], i), "dogm_update_pose": ([vp, f, f, f], i),
         "dogm_update_pose_noalloc": ([vp, f, f, f], i),
-        "dogm_initialize_particles": ([vp], i), "dogm_set_measurement_cells": ([vp, vp, sz], i),
+        "dogm_initialize_particles": ([vp], i), "dogm_particle_assignment": ([vp], i),
+        "dogm_grid_cell_occupancy_update": ([vp, f], i), "dogm_update_persistent_particles": ([vp], i),
+        "dogm_initialize_new_particles": ([vp], i), "dogm_statistical_moments": ([vp], i),
+        "dogm_resampling": ([vp], i), "dogm_set_measurement_cells": ([vp, vp, sz], i),
         "dogm_set_particles": ([vp, vp, vp, vp, f, sz], i), "dogm_set_replay": ([vp, vp, vp, vp, vp], i),
         "dogm_clear_replay": ([vp], i), "dogm_generate_draws": ([vp, i, vp, vp, vp, vp], i),
         "dogm_debug_enable": ([vp, i], i), "dogm_debug_joint_weights": ([vp, vp, sz, vp], i),
@@ -406,6 +411,25 @@ class DOGM:
     def update_pose_noalloc(self, x: float, y: float, yaw: float) -> None:
         """update_pose without device allocation (grids of at most 262,144 cells)."""
         check(load().dogm_update_pose_noalloc(self.h, x, y, yaw), "dogm_update_pose_noalloc")
+
+    # stage methods after particlePrediction, in updateGrid's order (dogm/src/dogm.cu:119-127)
+    def particle_assignment(self) -> None:
+        check(load().dogm_particle_assignment(self.h), "dogm_particle_assignment")
+
+    def grid_cell_occupancy_update(self, dt: float) -> None:
+        check(load().dogm_grid_cell_occupancy_update(self.h, dt), "dogm_grid_cell_occupancy_update")
+
+    def update_persistent_particles(self) -> None:
+        check(load().dogm_update_persistent_particles(self.h), "dogm_update_persistent_particles")
+
+    def initialize_new_particles(self) -> None:
+        check(load().dogm_initialize_new_particles(self.h), "dogm_initialize_new_particles")
+
+    def statistical_moments(self) -> None:
+        check(load().dogm_statistical_moments(self.h), "dogm_statistical_moments")
+
+    def resampling(self) -> None:
+        check(load().dogm_resampling(self.h), "dogm_resampling")
 
     def initialize_particles(self) -> None:
         check(load().dogm_initialize_particles(self.h), "dogm_initialize_particles")

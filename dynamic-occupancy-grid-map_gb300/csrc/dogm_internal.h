@@ -62,6 +62,16 @@ struct FrameState {
     int n_birth;                   // newborns created this frame (B or 0)
     int pad;
 };
+// Parts of the cell pass (GridDesc::stage_mask).  The update runs them all in one pass; the
+// stage calls of the reference's public stage methods run one each and merge their fields into
+// the cell records (dogm/src/dogm.cu:262-384: particleAssignment, gridCellOccupancyUpdate,
+// updatePersistentParticles, statisticalMoments).
+constexpr uint32_t kPartRanges = 1u;    // start_idx / end_idx
+constexpr uint32_t kPartMasses = 2u;    // masses, free mass, newborn mass, measurement copy
+constexpr uint32_t kPartReweight = 4u;  // mu_A / mu_UA, reweighted weights, joint weight sums
+constexpr uint32_t kPartMoments = 8u;   // velocity mean / variance / covariance
+constexpr uint32_t kPartAll = 15u;
+
 constexpr uint32_t kStatusTimeout = 1u;  // a bounded wait gave up
 constexpr uint32_t kStatusBounds = 2u;   // an index check refused a write
 
@@ -80,6 +90,8 @@ struct GridDesc {
     int shift_x, shift_y;   // cells to shift (x_move, y_move of dogm.cu:177-178)
     int shifted;            // 1 when the pose moved by more than one cell this frame
     int copy_meas;          // 1: meas_src is a caller buffer to copy into meas_own
+    uint32_t stage_mask;    // parts of the cell pass to run (kPart*)
+    int weights_predicted;  // 1: w_res already holds p_S * w (stage calls: particlePrediction ran)
     uint32_t frame;         // iteration number (Philox counter word 1)
     uint32_t stream_id;     // Philox counter word 3
     uint32_t seed_lo, seed_hi;
@@ -170,12 +182,16 @@ cudaError_t prepare_cells();
 cudaError_t prepare_sort();
 cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCfg& cfg);
 cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg);
+// stage_mode 0: the update's predict (ego shift, motion, bucket counts, per-frame sums zeroed);
+// 1: the particlePrediction stage call (motion only); 2: the particleAssignment stage call
+// (bucket counts of the resident keys and per-frame sums zeroed, no motion)
 cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg);
 // bucket offsets (column scan of the per-tile bucket counts) and the stable bucket scatter;
 // max_ctiles: the largest bucket count of the batch's grids (sizes the scatter's shared memory)
 cudaError_t launch_sort_scan(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_sort_scatter(const Batch* d_batch, int max_ctiles, const LaunchCfg& cfg);
-cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg);
+// staged: a stage call, running the parts of GridDesc::stage_mask
+cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg, bool staged = false);
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg);
 cudaError_t launch_shift_stage(const GridDesc& g, int x_move, int y_move, const LaunchCfg& cfg);

@@ -169,31 +169,58 @@ __device__ __forceinline__ void put_cell(CellSmem& sm, const GridDesc& g, uint32
 }
 
 // S: the stable counting sort of one bucket (bucketed positions [p0, p1) of T, whose cells lie
-// in [base, base + kCellTile)) into the same positions of S.  Ends with a barrier.
+// in [base, base + kCellTile)) into the same positions of S.  The bucket is ranked in chunks of
+// at most kBucketChunk particles; within a chunk warp w takes the contiguous segment
+// [w * 32 R, (w + 1) * 32 R) in R rounds of 32 (R = the chunk's particles / 512, rounded up), so
+// that bucket order is (warp, round, lane) and per-warp counts give stable ranks.  A bucket of
+// one chunk is ranked in a single pass: its per-warp counts also give the per-cell totals.
+// Ends with a barrier.
+__device__ __forceinline__ int chunk_rounds(int n) { return min(kBucketIpt, (n + kCellThreads - 1) / kCellThreads); }
+
 __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int base, int p0, int p1) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) sm.u1.srt.cnt[c] = 0u;
-    __syncthreads();
-    // 1: particles per cell (a key outside the tile can only come from inconsistent counts)
-    for (int i0 = p0; i0 < p1; i0 += kCellThreads * 4) {
-        uint32_t kw[4];
+    const int np = p1 - p0;
+    const bool single = np <= kBucketChunk;  // block-uniform
+    uint32_t key[kBucketIpt];
+    uint16_t rank[kBucketIpt];
+
+    // the cell (within the tile) of key word kw, or ~0 for no particle; a key outside the
+    // tile can only come from inconsistent counts and is not placed
+    auto cell_of = [&](uint32_t kw) -> uint32_t {
+        const uint32_t c = kw == 0xffffffffu ? 0xffffffffu : (kw & kCellMask) - (uint32_t)base;
+        return c < (uint32_t)kCellTile ? c : 0xffffffffu;
+    };
+    auto load_chunk = [&](int c0, int R) {
+        const int wbase = c0 + warp * 32 * R;
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int i = i0 + r * kCellThreads + (int)threadIdx.x;
-            kw[r] = i < p1 ? g.T_key[i] : 0xffffffffu;
+        for (int k = 0; k < kBucketIpt; ++k) {
+            const int i = wbase + k * 32 + lane;
+            key[k] = (k < R && i < p1) ? g.T_key[i] : 0xffffffffu;
         }
+    };
+    auto zero_whist = [&]() {
+        uint4* wz = reinterpret_cast<uint4*>(&sm.u2.whist[0][0]);
+        for (int i = threadIdx.x; i < (int)(sizeof(sm.u2.whist) / sizeof(uint4)); i += kCellThreads)
+            wz[i] = make_uint4(0u, 0u, 0u, 0u);
+    };
+    // warp ranks of the loaded chunk: rank[k] = earlier same-cell particles of the warp
+    auto rank_chunk = [&](int R) {
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const uint32_t c = kw[r] == 0xffffffffu ? 0xffffffffu : (kw[r] & kCellMask) - (uint32_t)base;
-            const uint32_t d = c < (uint32_t)kCellTile ? c : 0xffffffffu;
+        for (int k = 0; k < kBucketIpt; ++k) {
+            if (k >= R) break;  // block-uniform
+            const uint32_t d = cell_of(key[k]);
             const uint32_t peers = __match_any_sync(0xffffffffu, d);
-            if (d != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&sm.u1.srt.cnt[d], (uint32_t)__popc(peers));
+            uint16_t before = 0;
+            if (d != 0xffffffffu) before = sm.u2.whist[warp][d];
+            rank[k] = (uint16_t)(before + __popc(peers & lt_mask));
+            __syncwarp();
+            if (d != 0xffffffffu && lane == __ffs(peers) - 1) sm.u2.whist[warp][d] = (uint16_t)(before + __popc(peers));
+            __syncwarp();
         }
-    }
-    __syncthreads();
-    // 2: exclusive scan of the counts: the first position of each cell in the bucket
-    {
+    };
+    // exclusive scan of cnt[] into off[0][] (the first position of each cell in the bucket)
+    auto scan_counts = [&]() {
         constexpr int kPer = kCellTile / kCellThreads;
         const int c0 = threadIdx.x * kPer;
         uint32_t v[kPer], s = 0u;
@@ -217,69 +244,32 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
             sm.u1.srt.off[0][c0 + j] = e;
             e += v[j];
         }
-    }
-    // 3: chunks in bucket order; warp w takes chunk positions [w * 256, (w + 1) * 256)
-    int cur = 0;
-    for (int c0 = p0; c0 < p1; c0 += kBucketChunk, cur ^= 1) {
-        uint4* wz = reinterpret_cast<uint4*>(&sm.u2.whist[0][0]);
-        for (int i = threadIdx.x; i < (int)(sizeof(sm.u2.whist) / sizeof(uint4)); i += kCellThreads)
-            wz[i] = make_uint4(0u, 0u, 0u, 0u);
-        __syncthreads();
-        const int wbase = c0 + warp * (32 * kBucketIpt);
-        uint32_t key[kBucketIpt];
-        uint16_t rank[kBucketIpt];
-#pragma unroll
-        for (int k = 0; k < kBucketIpt; ++k) {
-            const int i = wbase + k * 32 + lane;
-            key[k] = i < p1 ? g.T_key[i] : 0xffffffffu;
-        }
-#pragma unroll
-        for (int k = 0; k < kBucketIpt; ++k) {
-            const uint32_t c = key[k] == 0xffffffffu ? 0xffffffffu : (key[k] & kCellMask) - (uint32_t)base;
-            const uint32_t d = c < (uint32_t)kCellTile ? c : 0xffffffffu;
-            const uint32_t peers = __match_any_sync(0xffffffffu, d);
-            uint16_t before = 0;
-            if (d != 0xffffffffu) before = sm.u2.whist[warp][d];
-            rank[k] = (uint16_t)(before + __popc(peers & lt_mask));
-            __syncwarp();
-            if (d != 0xffffffffu && lane == __ffs(peers) - 1) sm.u2.whist[warp][d] = (uint16_t)(before + __popc(peers));
-            __syncwarp();
-        }
-        __syncthreads();
-        // per cell: offsets of the warps within the chunk, and the cell's offset for the next chunk
-        for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) {
-            uint32_t acc = 0u;
-#pragma unroll
-            for (int w = 0; w < kCellWarps; ++w) {
-                const uint32_t n = sm.u2.whist[w][c];
-                sm.u2.whist[w][c] = (uint16_t)acc;
-                acc += n;
-            }
-            sm.u1.srt.off[cur ^ 1][c] = sm.u1.srt.off[cur][c] + acc;
-        }
-        __syncthreads();
-        // scatter to the sorted positions; per half of the items every state load is issued
-        // before the first store
+    };
+    // the loaded chunk to its sorted positions; per half of the rounds every state load is
+    // issued before the first store
+    auto scatter_chunk = [&](int c0, int R, int cur) {
+        const int wbase = c0 + warp * 32 * R;
         constexpr int kHalf = kBucketIpt / 2;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
+            if (h * kHalf >= R) break;  // block-uniform
             float4 st[kHalf];
             int out[kHalf];
 #pragma unroll
             for (int j = 0; j < kHalf; ++j) {
                 const int k = h * kHalf + j;
                 const int i = wbase + k * 32 + lane;
-                const uint32_t c = (key[k] & kCellMask) - (uint32_t)base;
+                const uint32_t c = cell_of(key[k]);
                 out[j] = -1;
-                if (i < p1 && c < (uint32_t)kCellTile)
+                if (k < R && c != 0xffffffffu)
                     out[j] = p0 + (int)(sm.u1.srt.off[cur][c] + sm.u2.whist[warp][c] + rank[k]);
-                st[j] = g.T_state[i < p1 ? i : p1 - 1];
+                st[j] = g.T_state[(k < R && i < p1) ? i : p1 - 1];
             }
 #pragma unroll
             for (int j = 0; j < kHalf; ++j) {
                 const int k = h * kHalf + j;
                 const int i = wbase + k * 32 + lane;
-                if (i >= p1) continue;
+                if (k >= R || i >= p1) continue;
                 if (out[j] < p0 || out[j] >= p1) {  // only inconsistent counts get here
                     flag_status(g, kStatusBounds);
                     continue;
@@ -289,10 +279,81 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
                 if (g.dbg_perm) g.dbg_perm[out[j]] = g.T_idx[i];
             }
         }
+    };
+
+    if (single) {
+        // one pass: warp ranks and counts; the column prefix over the warps gives each warp's
+        // offset within its cell and the cell's total
+        const int R = chunk_rounds(np);
+        load_chunk(p0, R);
+        zero_whist();
+        __syncthreads();
+        rank_chunk(R);
+        __syncthreads();
+        for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) {
+            uint32_t acc = 0u;
+#pragma unroll
+            for (int w = 0; w < kCellWarps; ++w) {
+                const uint32_t n = sm.u2.whist[w][c];
+                sm.u2.whist[w][c] = (uint16_t)acc;
+                acc += n;
+            }
+            sm.u1.srt.cnt[c] = acc;
+        }
+        __syncthreads();
+        scan_counts();
+        __syncthreads();
+        scatter_chunk(p0, R, 0);
+        __syncthreads();
+        return;
+    }
+
+    // several chunks: particles per cell over the whole bucket first
+    for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) sm.u1.srt.cnt[c] = 0u;
+    __syncthreads();
+    for (int c0 = p0; c0 < p1; c0 += kBucketChunk) {
+        const int R = chunk_rounds(min(kBucketChunk, p1 - c0));
+        load_chunk(c0, R);
+#pragma unroll
+        for (int k = 0; k < kBucketIpt; ++k) {
+            if (k >= R) break;  // block-uniform
+            const uint32_t d = cell_of(key[k]);
+            const uint32_t peers = __match_any_sync(0xffffffffu, d);
+            if (d != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&sm.u1.srt.cnt[d], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    scan_counts();
+    // then chunk by chunk in bucket order, the cells' offsets carried from chunk to chunk
+    int cur = 0;
+    for (int c0 = p0; c0 < p1; c0 += kBucketChunk, cur ^= 1) {
+        const int R = chunk_rounds(min(kBucketChunk, p1 - c0));
+        load_chunk(c0, R);
+        zero_whist();
+        __syncthreads();
+        rank_chunk(R);
+        __syncthreads();
+        for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) {
+            uint32_t acc = 0u;
+            if (sm.u1.srt.cnt[c]) {  // cells without particles keep zero offsets
+#pragma unroll
+                for (int w = 0; w < kCellWarps; ++w) {
+                    const uint32_t n = sm.u2.whist[w][c];
+                    sm.u2.whist[w][c] = (uint16_t)acc;
+                    acc += n;
+                }
+            }
+            sm.u1.srt.off[cur ^ 1][c] = sm.u1.srt.off[cur][c] + acc;
+        }
+        __syncthreads();
+        scatter_chunk(c0, R, cur);
         __syncthreads();
     }
 }
 
+// STAGED: a stage call (GridDesc::stage_mask selects the parts); the update's instantiation runs
+// every part with no mask tests.
+template <bool STAGED>
 __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ bt) {
     grid_dependency_begin();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -438,7 +499,12 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
         }
 
         // ---- B: per-cell update ----------------------------------------------------------
-        const float c_pred = __fmul_rn(g.p_S, g.fs->w_res);  // predicted weight of an in-grid particle
+        // (a stage call runs one part of the pass: it starts from the records as they are and
+        // replaces only its own fields)
+        const uint32_t mask = STAGED ? g.stage_mask : kPartAll;
+        const bool all = !STAGED;
+        const float c_pred = g.weights_predicted ? g.fs->w_res                    // predicted weight of
+                                                 : __fmul_rn(g.p_S, g.fs->w_res);  // an in-grid particle
         unsigned long long qb = 0ull, jq = 0ull;
         cp_async_wait_all();  // this thread's own prefetches (B reads only its own cells' slots)
         for (int r = 0; r < kCellTile / kCellThreads; ++r) {
@@ -447,13 +513,22 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             const int warp_first = base + r * kCellThreads + warp * 32;  // the warp's 32 cells
             if (warp_first >= g.C) break;                                // warp-uniform
             float4* stage = sm.u2.stage[warp];
+            const int n_rec = min(32, g.C - warp_first);
+            float4* dst = reinterpret_cast<float4*>(g.cells + warp_first);
+            if (!all) {  // block-uniform: the warp's records as they are
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int rec = q * 8 + (lane >> 2), chunk = lane & 3;
+                    if (rec < n_rec) stage[stage_slot(rec, chunk)] = dst[rec * 4 + chunk];
+                }
+                __syncwarp();
+            }
             if (k < g.C) {
             const bool occupied = sm.start[cl] >= 0;  // end, count and sums are set only then
             const int start = occupied ? sm.start[cl] : -1, end = occupied ? sm.end[cl] : -1;
             const int n_in = occupied ? sm.n_in[cl] : 0;
             const float free_prev = sm.free_prev[cl];
             const dogm_measurement_cell m = sm.meas[cl];
-            if (g.copy_meas) g.meas_own[k] = m;
             const CellOut o = cell_masses(n_in, c_pred, free_prev, g.alpha, g.p_B, m.free_mass, m.occ_mass);
             float muA = 0.0f, muUA = 0.0f, wp = 0.0f;
             float mx = 0.0f, my = 0.0f, vx = 0.0f, vy = 0.0f, cxy = 0.0f;
@@ -464,7 +539,7 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                 muUA = o.m_occ_pred > 0.0f ? __fdiv_rn(o.rho_p, o.m_occ_pred) : 0.0f;
                 wp = __fadd_rn(__fmul_rn(__fmul_rn(m.p_A, muA), wu),
                                __fmul_rn(__fmul_rn(__fsub_rn(1.0f, m.p_A), muUA), o.w_norm));
-                if (o.rho_p > 0.0f) {
+                if (o.rho_p > 0.0f && (mask & kPartMoments)) {
                     const float inv = __fdiv_rn(1.0f, o.rho_p);
                     mx = __fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vx[cl]));
                     my = __fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vy[cl]));
@@ -473,24 +548,53 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                     cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vxy[cl])), __fmul_rn(mx, my));
                 }
             }
-            stage[stage_slot(lane, 0)] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
-            stage[stage_slot(lane, 1)] = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
-            stage[stage_slot(lane, 2)] = make_float4(muUA, 0.0f, 0.0f, mx);
-            stage[stage_slot(lane, 3)] = make_float4(my, vx, vy, cxy);
-            g.free_new[k] = o.free_up;
-            g.rho_b[k] = make_float2(o.rho_b, m.p_A);
-            g.w_cell[k] = wp;
-            qb += quantize(o.rho_b, g.q_shift);
-            const unsigned long long qw = n_in > 0 ? quantize(wp, g.q_shift) : 0ull;
-            if (qw) {
-                jq += (unsigned long long)n_in * qw;
-                add_persistent(g, start, end, n_in, qw);
+            if (all) {
+                stage[stage_slot(lane, 0)] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
+                stage[stage_slot(lane, 1)] = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
+                stage[stage_slot(lane, 2)] = make_float4(muUA, 0.0f, 0.0f, mx);
+                stage[stage_slot(lane, 3)] = make_float4(my, vx, vy, cxy);
+            } else {
+                float4 s0 = stage[stage_slot(lane, 0)], s1 = stage[stage_slot(lane, 1)];
+                float4 s2 = stage[stage_slot(lane, 2)], s3 = stage[stage_slot(lane, 3)];
+                if (mask & kPartRanges) {
+                    s0.x = __int_as_float(start);
+                    s0.y = __int_as_float(end);
+                }
+                if (mask & kPartMasses) {
+                    s0.z = o.rho_b; s0.w = o.rho_p;
+                    s1.x = o.free_up; s1.y = o.occ_up; s1.z = o.m_occ_pred;
+                    s2.y = 0.0f; s2.z = 0.0f;  // w_A / w_UA: the newborn stage sets them
+                }
+                if (mask & kPartReweight) {
+                    s1.w = muA;
+                    s2.x = muUA;
+                }
+                if (mask & kPartMoments) {
+                    s2.w = mx;
+                    s3 = make_float4(my, vx, vy, cxy);
+                }
+                stage[stage_slot(lane, 0)] = s0;
+                stage[stage_slot(lane, 1)] = s1;
+                stage[stage_slot(lane, 2)] = s2;
+                stage[stage_slot(lane, 3)] = s3;
+            }
+            if (mask & kPartMasses) {
+                if (g.copy_meas) g.meas_own[k] = m;
+                g.free_new[k] = o.free_up;
+                g.rho_b[k] = make_float2(o.rho_b, m.p_A);
+                qb += quantize(o.rho_b, g.q_shift);
+            }
+            if (mask & kPartReweight) {
+                g.w_cell[k] = wp;
+                const unsigned long long qw = n_in > 0 ? quantize(wp, g.q_shift) : 0ull;
+                if (qw) {
+                    jq += (unsigned long long)n_in * qw;
+                    add_persistent(g, start, end, n_in, qw);
+                }
             }
             }  // k < g.C
             // the warp's records, 512 contiguous bytes per store instruction
             __syncwarp();
-            const int n_rec = min(32, g.C - warp_first);
-            float4* dst = reinterpret_cast<float4*>(g.cells + warp_first);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int rec = q * 8 + (lane >> 2), chunk = lane & 3;
@@ -502,8 +606,10 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
         block_excl_scan_u64<kCellThreads>(qb, sm.red, &tile_qb);
         block_excl_scan_u64<kCellThreads>(jq, sm.red2, &tile_jq);
         if (threadIdx.x == 0) {
-            g.cell_sum[lt] = tile_qb;
-            atomicAdd(&g.fs->qb_total, tile_qb);
+            if (mask & kPartMasses) {
+                g.cell_sum[lt] = tile_qb;
+                atomicAdd(&g.fs->qb_total, tile_qb);
+            }
             if (tile_jq) atomicAdd(&g.fs->joint_total, tile_jq);
         }
     }
@@ -671,11 +777,15 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
 }
 
 cudaError_t prepare_cells() {
-    return cudaFuncSetAttribute(k_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CellSmem));
+    cudaError_t e = cudaFuncSetAttribute(k_cells<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CellSmem));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_cells<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CellSmem));
 }
 
-cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg) {
-    return launch_kernel(cfg, k_cells, launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), const_cast<Batch*>(d_batch));
+cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg, bool staged) {
+    Batch* b = const_cast<Batch*>(d_batch);
+    if (staged) return launch_kernel(cfg, k_cells<true>, launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), b);
+    return launch_kernel(cfg, k_cells<false>, launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), b);
 }
 
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg) {

@@ -35,7 +35,8 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
 // weight w_res, so the predicted weight is p_S * w_res, or 0 out of the grid (bit 30).
 // Each 4096-particle tile also counts its particles per bucket of the sort (cell tile): the
 // row of the tile is written whole, the grid's totals are added to ctile_cnt.
-// mode 0: full frame (shift + bucket counts); mode 1: stage call (no counts).
+// mode 0: full frame (shift + bucket counts); mode 1: particlePrediction stage call (no
+// counts); mode 2: particleAssignment stage call (bucket counts of the resident keys only).
 // ---------------------------------------------------------------------------------------
 // 512 threads per 4096-particle tile (8 particles each): the kernel is issue-bound, and twice
 // the warps of a 256-thread block keep about 50 warps per SM in flight over the frame's tiles.
@@ -46,7 +47,8 @@ __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restric
     grid_dependency_begin();
     __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (bucket of the sort)
     const int total = batch_total(bt, kStPredict);
-    if (mode == 0) {
+    const bool counts = mode != 1;
+    if (counts) {
         // this frame's exact sums start at zero: the cell and newborn passes add into them
         // after this kernel, and the last reader (the previous frame's resampling) is done
         const int stride = gridDim.x * blockDim.x;
@@ -66,7 +68,7 @@ __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restric
         const int gi = grid_of_tile(bt, kStPredict, t);
         const GridDesc& g = bt->g[gi];
         const int lt = t - bt->prefix[gi][kStPredict];
-        if (mode == 0) {
+        if (counts) {
             for (int i = threadIdx.x; i < g.ctiles; i += kPredictThreads) h2[i] = 0u;
             __syncthreads();
         }
@@ -78,9 +80,12 @@ __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restric
 #pragma unroll 4
         for (int k = 0; k < kPredictTile / kPredictThreads; ++k) {
             const int i = base + k * kPredictThreads + threadIdx.x;
-            const bool valid = i < g.N;
+            bool valid = i < g.N;
             uint32_t key = 0xffffffffu;
-            if (valid) {
+            if (valid && mode == 2) {
+                key = g.P_key[i] & kCellMask;
+                valid = key < (uint32_t)g.C;  // injected keys outside the grid are not counted
+            } else if (valid) {
                 float4 s = g.P_state[i];
                 const uint32_t kw = g.P_key[i];
                 if (shift) {
@@ -112,13 +117,13 @@ __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restric
                 g.P_state[i] = o;
                 g.P_key[i] = key | (out ? kOutBit : 0u) | (kw & kAssocBit);
             }
-            if (mode == 0) {
+            if (counts) {
                 const uint32_t bucket = valid ? key >> kCellTileBits : 0xffffffffu;
                 const uint32_t peers = __match_any_sync(0xffffffffu, bucket);
                 if (valid && lane == __ffs(peers) - 1) atomicAdd(&h2[bucket], (uint32_t)__popc(peers));
             }
         }
-        if (mode == 0) {
+        if (counts) {
             __syncthreads();
             // this tile's bucket counts (predict and scatter tiles coincide), row written whole
             uint32_t* row = g.hsort + (size_t)lt * g.bucket_stride;

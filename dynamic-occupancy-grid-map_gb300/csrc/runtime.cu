@@ -151,6 +151,7 @@ struct dogm_handle {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t frame_ready = nullptr;
     cudaEvent_t copy_done[2] = {nullptr, nullptr};
+    float stage_dt = 0.1f;  // dt of the last gridCellOccupancyUpdate stage call
 };
 
 namespace {
@@ -243,6 +244,8 @@ void fill_frame(dogm_handle* h, float dt, int shifted, int xm, int ym, const dog
     g.meas_src = meas_src;
     g.copy_meas = copy_meas;
     g.frame = (uint32_t)h->iteration;
+    g.stage_mask = kPartAll;      // the update runs every part of the cell pass
+    g.weights_predicted = 0;
     g.rp_init = h->rp_init;
     g.rp_predict = h->rp_predict;
     g.rp_birth = h->rp_birth;
@@ -818,6 +821,87 @@ dogm_status dogm_particle_prediction(dogm_handle* h, float dt) {
     fs.w_res = fs.w_res * h->params.persistence_prob;
     DOGM_CUDA(cudaMemcpy(&h->desc.fs->w_res, &fs.w_res, sizeof(float), cudaMemcpyHostToDevice));
     h->last_launches = 1;
+    return DOGM_OK;
+}
+
+}  // extern "C"
+
+// Runs stage launches on the handle's resident state (the reference's public stage methods):
+// the handle alone in a batch, kernels launched one by one and waited for; the cell pass runs
+// only the parts in `mask`, and the weights are taken as already predicted (particlePrediction
+// multiplies them by p_S, predict.cu:30).  Returns the launches' device status.
+template <class Launch>
+static dogm_status run_stage(dogm_handle* h, float dt, uint32_t mask, int n_launches, Launch launch) {
+    DeviceGuard dg(h->device);
+    Ctx& c = h->ctx;
+    DOGM_CUDA(cudaStreamSynchronize(c.stream));
+    c.pending[0] = c.pending[1] = false;  // the stream was synchronised above
+    dogm_status st = wait_readback(h, c.stream);  // the cell records may be rewritten
+    if (st != DOGM_OK) return st;
+    fill_frame(h, dt, 0, 0, 0, h->desc.meas_own, 0);
+    h->desc.stage_mask = mask;
+    h->desc.weights_predicted = 1;
+    dogm_handle* hs[1] = {h};
+    build_batch(c, hs, 1, std::vector<int>(1, 0));
+    h->desc.stage_mask = kPartAll;
+    h->desc.weights_predicted = 0;
+    DOGM_CUDA(upload_batch(c, 1));
+    LaunchCfg cfg{c.num_sms, c.stream};
+    DOGM_CUDA(launch(cfg));
+    DOGM_CUDA(download_status(c));
+    h->last_launches = n_launches;
+    return finish_frame(c, hs, 1);
+}
+
+extern "C" {
+
+dogm_status dogm_particle_assignment(dogm_handle* h) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    const bool clear = h->need_clear;  // first frame, or after a failed one: all counters reset
+    Ctx& c = h->ctx;
+    return run_stage(h, h->stage_dt, kPartRanges, 4 + (clear ? 1 : 0), [&](const LaunchCfg& cfg) {
+        cudaError_t e;
+        if (clear && (e = launch_frame_begin(c.d_batch, 1, cfg)) != cudaSuccess) return e;
+        if ((e = launch_predict(c.d_batch, 2, cfg)) != cudaSuccess) return e;
+        if ((e = launch_sort_scan(c.d_batch, cfg)) != cudaSuccess) return e;
+        if ((e = launch_sort_scatter(c.d_batch, c.scatter_ctiles, cfg)) != cudaSuccess) return e;
+        return launch_cells(c.d_batch, cfg, true);
+    });
+}
+
+dogm_status dogm_grid_cell_occupancy_update(dogm_handle* h, float dt) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    h->stage_dt = dt;  // freespace_discount^dt (dogm.cu:291) is also what the later parts use
+    Ctx& c = h->ctx;
+    return run_stage(h, dt, kPartMasses, 1, [&](const LaunchCfg& cfg) { return launch_cells(c.d_batch, cfg, true); });
+}
+
+dogm_status dogm_update_persistent_particles(dogm_handle* h) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    Ctx& c = h->ctx;
+    return run_stage(h, h->stage_dt, kPartReweight, 1, [&](const LaunchCfg& cfg) { return launch_cells(c.d_batch, cfg, true); });
+}
+
+dogm_status dogm_initialize_new_particles(dogm_handle* h) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    Ctx& c = h->ctx;
+    return run_stage(h, h->stage_dt, 0u, 1, [&](const LaunchCfg& cfg) { return launch_newborn(c.d_batch, cfg); });
+}
+
+dogm_status dogm_statistical_moments(dogm_handle* h) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    Ctx& c = h->ctx;
+    return run_stage(h, h->stage_dt, kPartMoments, 1, [&](const LaunchCfg& cfg) { return launch_cells(c.d_batch, cfg, true); });
+}
+
+dogm_status dogm_resampling(dogm_handle* h) {
+    if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
+    Ctx& c = h->ctx;
+    dogm_status st = run_stage(h, h->stage_dt, 0u, 1, [&](const LaunchCfg& cfg) { return launch_resample(c.d_batch, cfg); });
+    if (st != DOGM_OK) return st;
+    // the resampled particles are the current ones (the reference's particle_array =
+    // particle_array_next, dogm.cu:128), and the frame ends as an update's does
+    advance(h);
     return DOGM_OK;
 }
 

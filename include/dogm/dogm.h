@@ -1,10 +1,11 @@
 // dogm::DOGM — header-only C++ drop-in for the reference's class of the same name
 // (dogm/include/dogm/dogm.h:20-199), implemented over the C ABI in dogm_gb300.h.
 //
-// Same constructor, updateGrid, getters and public stage methods (particlePrediction,
-// initializeParticles).  The reference's remaining stage methods (particleAssignment,
-// gridCellOccupancyUpdate, updatePersistentParticles, initializeNewParticles,
-// statisticalMoments, resampling) run fused inside updateGrid and are not separate calls.
+// Same constructor, updateGrid, getters and public stage methods (initializeParticles,
+// particlePrediction, particleAssignment, gridCellOccupancyUpdate, updatePersistentParticles,
+// initializeNewParticles, statisticalMoments, resampling; dogm.h:150-157).  updateGrid runs the
+// stages fused; called one by one in the reference's order (dogm.cu:119-127) after
+// updatePose, they compute the same bits as updateGrid.
 // Error behaviour matches the reference's CHECK_ERROR (cuda_utils.h:13-24): print and
 // continue; define DOGM_GB300_THROW to throw std::runtime_error instead.
 #pragma once
@@ -127,9 +128,32 @@ public:
     float getPositionY() const { return dogm_get_position_y(handle); }
     int getIteration() const { return dogm_get_iteration(handle); }
 
-    // public stage methods (dogm.h:150-152)
+    // public stage methods (dogm.h:150-157), in the order updateGrid runs them (dogm.cu:119-127)
     void initializeParticles() { checkStatus(dogm_initialize_particles(handle), "DOGM::initializeParticles"); }
     void particlePrediction(float dt) { checkStatus(dogm_particle_prediction(handle, dt), "DOGM::particlePrediction"); }
+    void particleAssignment() { checkStatus(dogm_particle_assignment(handle), "DOGM::particleAssignment"); }
+    void gridCellOccupancyUpdate(float dt)
+    {
+        checkStatus(dogm_grid_cell_occupancy_update(handle, dt), "DOGM::gridCellOccupancyUpdate");
+    }
+    void updatePersistentParticles()
+    {
+        checkStatus(dogm_update_persistent_particles(handle), "DOGM::updatePersistentParticles");
+    }
+    void initializeNewParticles() { checkStatus(dogm_initialize_new_particles(handle), "DOGM::initializeNewParticles"); }
+    void statisticalMoments() { checkStatus(dogm_statistical_moments(handle), "DOGM::statisticalMoments"); }
+    // also makes the resampled particles the current ones, which the reference leaves to
+    // updateGrid's particle_array = particle_array_next (dogm.cu:128)
+    void resampling() { checkStatus(dogm_resampling(handle), "DOGM::resampling"); }
+
+    // private in the reference (dogm.h:145); public here so that a caller can run a whole
+    // update stage by stage from a host measurement grid
+    void updateMeasurementGrid(const MeasurementCell* measurement_grid)
+    {
+        const size_t n = static_cast<size_t>(getGridSize()) * static_cast<size_t>(getGridSize());
+        checkStatus(dogm_set_measurement_cells(handle, reinterpret_cast<const dogm_measurement_cell*>(measurement_grid), n),
+                    "DOGM::updateMeasurementGrid");
+    }
 
     // private in the reference (dogm.h:144); public here so stage tests can drive it
     void updatePose(float new_x, float new_y, float new_yaw)

@@ -182,6 +182,39 @@ dogm_status dogm_update_pose_noalloc(dogm_handle* h, float new_x, float new_y, f
  * measurement grid (set by a previous update, or by dogm_set_measurement_cells). */
 dogm_status dogm_initialize_particles(dogm_handle* h);
 
+/* The remaining stage methods, in the order DOGM::updateGrid runs them (dogm/src/dogm.cu:119-127).
+ * Each runs one part of the update on the handle's resident state and waits for it.  Called in
+ * this order once per frame -- after dogm_set_measurement_cells (and dogm_initialize_particles on
+ * the first frame), dogm_update_pose and dogm_particle_prediction -- they compute the same bits
+ * as dogm_update with the same inputs.  The particle weights are taken as they are, i.e. as
+ * dogm_particle_prediction left them (p_S times the previous weight). */
+
+/* Replaces DOGM::particleAssignment (dogm/src/dogm.cu:262-281): the stable particle-to-cell
+ * sort and the cells' start_idx / end_idx. */
+dogm_status dogm_particle_assignment(dogm_handle* h);
+
+/* Replaces DOGM::gridCellOccupancyUpdate (dogm/src/dogm.cu:283-298): predicted, free, occupied,
+ * persistent and newborn masses (freespace_discount^dt), written into the cell records. */
+dogm_status dogm_grid_cell_occupancy_update(dogm_handle* h, float dt);
+
+/* Replaces DOGM::updatePersistentParticles (dogm/src/dogm.cu:300-321): mu_A, mu_UA and the
+ * reweighted persistent weights. */
+dogm_status dogm_update_persistent_particles(dogm_handle* h);
+
+/* Replaces DOGM::initializeNewParticles (dogm/src/dogm.cu:323-348): newborn allocation over the
+ * cells' newborn masses, w_A / w_UA of the records. */
+dogm_status dogm_initialize_new_particles(dogm_handle* h);
+
+/* Replaces DOGM::statisticalMoments (dogm/src/dogm.cu:350-384): velocity mean, variance and
+ * covariance of the cell records. */
+dogm_status dogm_statistical_moments(dogm_handle* h);
+
+/* Replaces DOGM::resampling (dogm/src/dogm.cu:386-423) and the particle_array =
+ * particle_array_next copy of updateGrid (dogm/src/dogm.cu:128): systematic resampling over the
+ * exact joint-weight scan; the resampled set becomes the current particles and the frame ends
+ * (dogm_get_iteration counts it). */
+dogm_status dogm_resampling(dogm_handle* h);
+
 /* ---- state injection and draw replay (parity tests; not on the hot path) -------------- */
 
 /* Overwrites the resident measurement grid from host memory. */

@@ -7,6 +7,7 @@
 // the particles are first initialised from a measurement grid, then the same relations are
 // checked through the stage calls: pose bookkeeping + shift, and zero-noise prediction.
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "dogm/dogm.h"
@@ -137,11 +138,56 @@ static void update_grid()
     EXPECT_EQ(mc[44].occ_mass, 0.7f);
 }
 
+// The public stage methods called one by one in updateGrid's order (dogm.cu:116-128) compute
+// the same cells and particles as updateGrid.
+static void stages_equal_update_grid()
+{
+    dogm::DOGM::Params p = test_params();
+    p.particle_count = 20000;
+    p.new_born_particle_count = 2000;
+    p.stddev_process_noise_position = 0.1f;
+    p.stddev_process_noise_velocity = 2.0f;
+    p.freespace_discount = 0.01f;
+    dogm::DOGM fused(p), staged(p);
+    std::vector<dogm::MeasurementCell> meas(100, dogm::MeasurementCell{0.4f, 0.0f, 1.0f, 1.0f});
+    meas[44] = dogm::MeasurementCell{0.0f, 0.7f, 1.0f, 1.0f};
+    meas[57] = dogm::MeasurementCell{0.1f, 0.8f, 1.0f, 1.0f};
+    for (int k = 0; k < 4; ++k)
+    {
+        const float x = 1.5f * static_cast<float>(k), y = -1.2f * static_cast<float>(k);
+        fused.updateGrid(meas.data(), x, y, 0.0f, 0.1f, false);
+        staged.updateMeasurementGrid(meas.data());
+        if (k == 0)
+        {
+            staged.initializeParticles();
+        }
+        staged.updatePose(x, y, 0.0f);
+        staged.particlePrediction(0.1f);
+        staged.particleAssignment();
+        staged.gridCellOccupancyUpdate(0.1f);
+        staged.updatePersistentParticles();
+        staged.initializeNewParticles();
+        staged.statisticalMoments();
+        staged.resampling();
+        const auto a = fused.getGridCells();
+        const auto b = staged.getGridCells();
+        EXPECT_EQ(std::memcmp(a.data(), b.data(), a.size() * sizeof(dogm::GridCell)), 0);
+        auto pa = fused.getParticles();
+        auto pb = staged.getParticles();
+        EXPECT_EQ(std::memcmp(pa.state, pb.state, sizeof(pa.state[0]) * static_cast<size_t>(p.particle_count)), 0);
+        EXPECT_EQ(std::memcmp(pa.weight, pb.weight, sizeof(float) * static_cast<size_t>(p.particle_count)), 0);
+        pa.free();
+        pb.free();
+    }
+    EXPECT_EQ(staged.getIteration(), 4);
+}
+
 int main()
 {
     ego_motion_compensation();
     predict();
     update_grid();
+    stages_equal_update_grid();
     std::printf("dogm_spec: %d failure(s)\n", failures);
     return failures;
 }
