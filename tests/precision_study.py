@@ -15,6 +15,8 @@ and no divergence accumulates.  Reported per frame and over all frames:
     moment 1 + mx^2 + my^2 + |var_x| + |var_y|).
 
     python tests/precision_study.py [--frames 30] [--out report.json]   (needs the GPU)
+
+The record of the full 30-frame run is tests/precision_study_2048.json.
 Test infrastructure: imports the oracle; tests/test_gpu_precision.py runs a small case.
 """
 from __future__ import annotations
@@ -139,7 +141,16 @@ def main():
     scene = importlib.import_module(PKG + ".scene")
     import pyoracle
     pyoracle.load()
+    t0 = time.time()
     rep = run(dogm, pyoracle, scene, frames=args.frames, log=lambda s: print(s, flush=True))
+    import subprocess
+    try:
+        gpu = subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader", "-i", "0"],
+                             capture_output=True, text=True, timeout=10).stdout.strip()
+    except (OSError, subprocess.SubprocessError):
+        gpu = "unknown"
+    rep["summary"]["provenance"] = {"command": "python tests/precision_study.py " + " ".join(sys.argv[1:]),
+                                    "gpu": gpu, "wall_s": round(time.time() - t0, 1)}
     print(json.dumps(rep["summary"], indent=1))
     if args.out:
         with open(args.out, "w") as f:

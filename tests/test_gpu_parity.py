@@ -1,14 +1,17 @@
 """GPU parity: the CUDA path against the FP32 oracle (bit-exact except the per-cell velocity
-sums, whose summation order differs) and the FP64 oracle (stated tolerances), with the
-GPU's own Philox draws replayed into the oracle."""
+sums, whose summation order differs: 4e-6 of the cell's second moment) and the FP64 oracle
+(masses within 5e-7), with the GPU's own Philox draws replayed into the oracle."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 # Moments come from float sums in a different order, and var = E[v^2] - E[v]^2 cancels:
-# the tolerance is relative to the cell's second moment 1 + mx^2 + my^2 + |var_x| + |var_y|.
-MOMENT_TOL = 1e-4
+# the tolerance is relative to the cell's second moment 1 + mx^2 + my^2 + |var_x| + |var_y|
+# (observed at most 1.7e-6 over the cases below).
+MOMENT_TOL = 4e-6
+# masses against the FP64 oracle (observed at most 2.4e-7, the 30-frame precision study included)
+MASS_TOL_FP64 = 5e-7
 EXACT_FIELDS = slice(2, 11)   # new_born .. w_UA: bit-exact
 MOMENT_FIELDS = slice(11, 16)
 
@@ -25,9 +28,12 @@ def compare_frame(dogm, oracle, g, out, label):
         assert bad.size == 0, "%s field %s differs at %d cells, first %s: %r vs %r" % (
             label, names[j], bad.size, bad[:3], got[bad[:3]], exp[bad[:3]])
     scale = 1.0 + ref[:, 11] ** 2 + ref[:, 12] ** 2 + np.abs(ref[:, 13]) + np.abs(ref[:, 14])
+    worst = 0.0
     for j in range(11, 16):
         err = np.abs(cells[names[j]].astype(np.float64) - ref[:, j]) / scale
+        worst = max(worst, float(err.max()))
         assert err.max() <= MOMENT_TOL, "%s field %s rel err %g" % (label, names[j], err.max())
+    print("%s: moments vs FP32 oracle, max rel. err %.3e" % (label, worst))
     dbg = g.debug_export()
     assert np.array_equal(dbg["sorted_cell"], (out["S_key"] & oracle.CELL_MASK).astype(np.int32)), label + " keys"
     assert np.array_equal(dbg["sort_perm"], out["perm"]), label + " permutation"
@@ -133,7 +139,7 @@ def test_lower_bound_matches_searchsorted(dogm):
 
 
 def test_fp64_tolerance_first_frame(dogm, oracle, scene):
-    """Against the double restatement on identical inputs: masses within 2e-6 absolute."""
+    """Against the double restatement on identical inputs: masses within 5e-7 absolute."""
     p = dogm.make_params(size=25.6, resolution=0.1, particle_count=200000, new_born_particle_count=20000)
     g = dogm.DOGM(p, seed=9)
     o = oracle.OracleDOGM(p, np.float64)
@@ -150,5 +156,6 @@ def test_fp64_tolerance_first_frame(dogm, oracle, scene):
     assert same.mean() > 0.999
     for j in (2, 3, 4, 5, 6):
         err = np.abs(cells[names[j]].astype(np.float64) - out["cells"][:, j])[same]
-        assert err.max() <= 2e-6, (names[j], err.max())
+        print("%s vs FP64: max abs err %.3e" % (names[j], err.max()))
+        assert err.max() <= MASS_TOL_FP64, (names[j], err.max())
     g.close()

@@ -13,7 +13,7 @@ are replayed into the GB300 path, so:
     except where the reference's float allocation rounds a boundary differently;
   * masses and velocity moments of both builds are compared with the FP64 oracle on the same
     inputs: per-field error versus FP64 is reported, the GB300 path's must stay within the
-    stated FP32 tolerances (2e-6 on masses, 1e-4 of the second moment on moments) and be no
+    stated FP32 tolerances (5e-7 on masses, 2e-6 of the second moment on moments) and be no
     larger than the reference build's (whose float prefix-sum differences lose precision as the
     total particle weight grows, quirk Q4).
 """
@@ -117,7 +117,8 @@ def test_against_reference_build(dogm, oracle, pyref, scene, size, res, n, b):
         # a particle within float rounding of a border may change cell in double, which moves the
         # ranges of every cell between its two keys (up to a grid row): > 99.5 % of the cells
         # agree at 256^2 / 1.5e5 particles, 96 % at 1200^2 / 2e6
-        assert ok.mean() > (0.995 if gs < 1000 else 0.9)
+        report["frame %d cells with FP64 ranges" % k] = (float(ok.mean()), 0.0)
+        assert ok.mean() > (0.995 if gs < 1000 else 0.94)
         # the outermost ring of cells holds the particles just outside the grid (keys clamped,
         # weight 0, predict.cu:41-48); a particle within rounding of the edge is in the grid in
         # one precision and out in the other, which moves a light cell's newborn mass by half its
@@ -131,11 +132,11 @@ def test_against_reference_build(dogm, oracle, pyref, scene, size, res, n, b):
             e_ours = np.abs(co[name].astype(np.float64) - f64[:, j])[ok].max()
             e_ref = np.abs(cr[name].astype(np.float64) - f64[:, j])[ok].max()
             report["frame %d %s" % (k, name)] = (e_ours, e_ref)
-            assert e_ours <= 2e-6, "frame %d %s: GB300 vs FP64 %g" % (k, name, e_ours)
+            assert e_ours <= 5e-7, "frame %d %s: GB300 vs FP64 %g" % (k, name, e_ours)
             # the reference's per-cell sums are differences of a float prefix sum over all
             # particles (common.h:24-32): their error grows with the total weight, which is ~1 on
             # the first frame and J (thousands) after a resampling; it is never more accurate
-            assert e_ours <= max(e_ref, 2e-6), "frame %d %s: reference closer to FP64" % (k, name)
+            assert e_ours <= max(e_ref, 5e-7), "frame %d %s: reference closer to FP64" % (k, name)
             # sanity bound that the reference build ran at all (observed up to 1.02e-2 at 256^2: its
             # frame-1 input varies run to run through the Q5 race).  At 1200^2 / 2e6 its prefix-sum
             # differences after a resampling are off by more than 1 (masses leave [0, 1]), so there
@@ -156,7 +157,7 @@ def test_against_reference_build(dogm, oracle, pyref, scene, size, res, n, b):
             e_ours = (np.abs(co[name].astype(np.float64) - f64[:, j]) / scale)[occ].max()
             e_ref = (np.abs(cr[name].astype(np.float64) - f64[:, j]) / scale)[occ].max()
             report["frame %d %s" % (k, name)] = (e_ours, e_ref)
-            assert e_ours <= 1e-4, "frame %d %s: GB300 vs FP64 %g" % (k, name, e_ours)
+            assert e_ours <= 2e-6, "frame %d %s: GB300 vs FP64 %g" % (k, name, e_ours)
 
         # both continue from the reference's resampled particles (multinomial there,
         # systematic here), so the next frame starts from identical inputs again
