@@ -234,6 +234,11 @@ __device__ __forceinline__ void flag_status(const GridDesc& g, uint32_t bits) {
 }
 __device__ __forceinline__ void flag_timeout(const GridDesc& g) { flag_status(g, kStatusTimeout); }
 
+// Adds v to the exact joint-weight sum of resample tile t.
+__device__ __forceinline__ void add_res_sum(const GridDesc& g, long long t, unsigned long long v) {
+    atomicAdd(&g.res_sum[t], v);
+}
+
 // Block-wide exclusive scan of one 64-bit value per thread (NT threads).  Returns the
 // exclusive prefix; *total receives the block sum.  scratch: >= 8 entries.
 template <int NT = kThreads>

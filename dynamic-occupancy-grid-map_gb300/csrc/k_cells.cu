@@ -139,7 +139,7 @@ __device__ __forceinline__ void add_persistent(const GridDesc& g, int start, int
                                                unsigned long long qw) {
     const int ts = start / kResTile, te = end / kResTile;
     if (ts == te) {
-        atomicAdd(&g.res_sum[ts], (unsigned long long)n_in * qw);
+        add_res_sum(g, ts, (unsigned long long)n_in * qw);
         return;
     }
     const bool all_in = n_in == end - start + 1;
@@ -150,7 +150,7 @@ __device__ __forceinline__ void add_persistent(const GridDesc& g, int start, int
             cnt = 0;
             for (int i = lo; i < hi; ++i) cnt += (g.S_key[i] & kOutBit) ? 0 : 1;
         }
-        if (cnt) atomicAdd(&g.res_sum[rt], (unsigned long long)cnt * qw);
+        if (cnt) add_res_sum(g, rt, (unsigned long long)cnt * qw);
     }
 }
 
@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                 qb += quantize(o.rho_b, g.q_shift);
             }
             if (mask & kPartReweight) {
-                g.w_cell[k] = wp;
+                if (n_in > 0) g.w_cell[k] = wp;  // read only through the keys of in-grid particles
                 const unsigned long long qw = n_in > 0 ? quantize(wp, g.q_shift) : 0ull;
                 if (qw) {
                     jq += (unsigned long long)n_in * qw;
@@ -602,10 +602,21 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             }
             __syncwarp();  // the stage is refilled by the next r
         }
-        unsigned long long tile_qb, tile_jq;
-        block_excl_scan_u64<kCellThreads>(qb, sm.red, &tile_qb);
-        block_excl_scan_u64<kCellThreads>(jq, sm.red2, &tile_jq);
+        // the tile's exact sums: warp sums, then thread 0 adds the warps' (sm.red is next
+        // written at the end of the next tile, after that tile's barriers)
+        qb = warp_sum_u64(qb);
+        jq = warp_sum_u64(jq);
+        if (lane == 0) {
+            sm.red[warp] = qb;
+            sm.red2[warp] = jq;
+        }
+        __syncthreads();
         if (threadIdx.x == 0) {
+            unsigned long long tile_qb = 0ull, tile_jq = 0ull;
+            for (int w = 0; w < kCellWarps; ++w) {
+                tile_qb += sm.red[w];
+                tile_jq += sm.red2[w];
+            }
             if (mask & kPartMasses) {
                 g.cell_sum[lt] = tile_qb;
                 atomicAdd(&g.fs->qb_total, tile_qb);
@@ -628,7 +639,7 @@ constexpr int kRunTiles = 4;  // resample tiles a thread accumulates in register
 // q per slot over joint positions [a, b), added per resample tile: the first kRunTiles tiles
 // from rt0 in registers, any further ones straight to the global sums.
 __device__ __forceinline__ void add_joint_range(unsigned long long (&racc)[kRunTiles], long long rt0,
-                                                unsigned long long* res_sum, long long a, long long b,
+                                                const GridDesc& g, long long a, long long b,
                                                 unsigned long long q) {
     if (q == 0ull) return;
     for (long long rt = a / kResTile; rt * kResTile < b; ++rt) {
@@ -641,7 +652,7 @@ __device__ __forceinline__ void add_joint_range(unsigned long long (&racc)[kRunT
 #pragma unroll
             for (int i = 0; i < kRunTiles; ++i) racc[i] += (o == i) ? v : 0ull;
         } else {
-            atomicAdd(&res_sum[rt], v);
+            add_res_sum(g, rt, v);
         }
     }
 }
@@ -747,14 +758,14 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
             const int nA = min(max(nuA, 0), nnew);
             const unsigned long long qA = quantize(wA, g.q_shift), qU = quantize(wUA, g.q_shift);
             jq += (unsigned long long)nA * qA + (unsigned long long)(nnew - nA) * qU;
-            add_joint_range(racc, rt0, g.res_sum, N + b0, N + b0 + nA, qA);
-            add_joint_range(racc, rt0, g.res_sum, N + b0 + nA, N + b1, qU);
+            add_joint_range(racc, rt0, g, N + b0, N + b0 + nA, qA);
+            add_joint_range(racc, rt0, g, N + b0 + nA, N + b1, qU);
         }
 #pragma unroll
         for (int i = 0; i < kRunTiles; ++i) {
             if (!__any_sync(0xffffffffu, racc[i] != 0ull)) continue;  // warp-uniform
             const unsigned long long s = warp_sum_u64(racc[i]);
-            if (lane == 0 && s) atomicAdd(&g.res_sum[rt0 + i], s);
+            if (lane == 0 && s) add_res_sum(g, rt0 + i, s);
         }
         if (__any_sync(0xffffffffu, jq != 0ull)) {
             jq = warp_sum_u64(jq);

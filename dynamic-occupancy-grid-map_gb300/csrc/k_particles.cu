@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restric
         for (int gi = 0; gi < bt->n_grids; ++gi) {
             const GridDesc& g = bt->g[gi];
             for (int i = tid; i < g.tiles[kStResample]; i += stride) g.res_sum[i] = 0ull;
-            if (tid == 0) {
+                if (tid == 0) {
                 g.fs->status = 0u;
                 g.fs->qb_total = 0ull;
                 g.fs->joint_total = 0ull;

@@ -52,7 +52,7 @@ struct ResSmem {
     int claim;
 };
 
-__global__ void __launch_bounds__(kThreads, 6) k_resample(Batch* __restrict__ bt) {
+__global__ void __launch_bounds__(kThreads, 5) k_resample(Batch* __restrict__ bt) {
     grid_dependency_begin();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     ResSmem& sm = *reinterpret_cast<ResSmem*>(smem_raw);
@@ -263,7 +263,7 @@ cudaError_t prepare_kernels() {
 
 cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg) {
     const int smem = (int)sizeof(ResSmem);
-    return launch_kernel(cfg, k_resample, launch_blocks(cfg, 6), kThreads, (size_t)smem, const_cast<Batch*>(d_batch));
+    return launch_kernel(cfg, k_resample, launch_blocks(cfg, 5), kThreads, (size_t)smem, const_cast<Batch*>(d_batch));
 }
 
 // ---------------------------------------------------------------------------------------

@@ -149,7 +149,7 @@ def main():
                              capture_output=True, text=True, timeout=10).stdout.strip()
     except (OSError, subprocess.SubprocessError):
         gpu = "unknown"
-    rep["summary"]["provenance"] = {"command": "python tests/precision_study.py " + " ".join(sys.argv[1:]),
+    rep["summary"]["provenance"] = {"command": "python tests/precision_study.py --frames %d" % args.frames,
                                     "gpu": gpu, "wall_s": round(time.time() - t0, 1)}
     print(json.dumps(rep["summary"], indent=1))
     if args.out:
