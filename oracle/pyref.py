@@ -70,6 +70,52 @@ def load() -> C.CDLL:
     return lib
 
 
+MEAS_CUBIN = os.path.join(CUBIN_DIR, "measurement_grid.cubin")
+
+
+def meas_missing() -> str | None:
+    """Why the reference's measurement-grid kernels cannot run here, or None."""
+    if not os.path.exists(MEAS_CUBIN):
+        return "%s missing: build it with oracle/ref/build_ref.py where the reference sources are" % MEAS_CUBIN
+    return missing()
+
+
+def _meas_lib() -> C.CDLL:
+    lib = load()
+    if not getattr(lib, "_meas_ready", False):
+        vp = C.c_void_p
+        lib.dogm_ref_meas_load.argtypes = [C.c_char_p]
+        lib.dogm_ref_polar_ism.argtypes = [vp, C.c_int, C.c_int, C.c_float, C.c_float, vp, vp]
+        lib.dogm_ref_cart_to_meas.argtypes = [vp, C.c_int, vp]
+        if lib.dogm_ref_meas_load(MEAS_CUBIN.encode()) != 0:
+            raise RuntimeError("reference measurement kernels: " + lib.dogm_ref_last_error().decode())
+        lib._meas_ready = True
+    return lib
+
+
+def polar_ism(ranges, bins: int, resolution: float, stddev_range: float, prior=None) -> np.ndarray:
+    """The reference's createPolarGridTextureKernel (or, with prior, fusePolarGridTextureKernel)
+    on a surface: (bins, beams, 2) float32 {occ, free}."""
+    lib = _meas_lib()
+    r = np.ascontiguousarray(ranges, np.float32)
+    beams = r.shape[0]
+    out = np.zeros((bins, beams, 2), np.float32)
+    pr = None if prior is None else np.ascontiguousarray(prior, np.float32).reshape(bins, beams, 2)
+    _check(lib.dogm_ref_polar_ism(_p(r), beams, bins, resolution, stddev_range, _p(pr), _p(out)), "dogm_ref_polar_ism")
+    return out
+
+
+def cart_to_meas(rgba) -> np.ndarray:
+    """The reference's cartesianGridToMeasurementGridKernel on an RGBA float image (gs, gs, 4),
+    row y = framebuffer row: (gs * gs, 4) float32 MeasurementCells."""
+    lib = _meas_lib()
+    img = np.ascontiguousarray(rgba, np.float32)
+    gs = img.shape[0]
+    out = np.zeros((gs * gs, 4), np.float32)
+    _check(lib.dogm_ref_cart_to_meas(_p(img), gs, _p(out)), "dogm_ref_cart_to_meas")
+    return out
+
+
 def _check(rc: int, what: str) -> None:
     if rc != 0:
         raise RuntimeError("%s: %s" % (what, load().dogm_ref_last_error().decode()))

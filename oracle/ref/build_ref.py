@@ -68,6 +68,28 @@ def _one(name: str) -> str:
     return dst
 
 
+MEAS_SRC = os.path.join("demo", "simulator", "mapping", "kernel", "measurement_grid.cu")
+
+
+def build_meas() -> str:
+    """Builds oracle/_ref/measurement_grid.cubin: the demo's measurement-grid kernels (inverse
+    sensor model into a polar surface, its fusion, framebuffer -> MeasurementCell), plain CUDA
+    compiled from dogm/demo/simulator/mapping/kernel/measurement_grid.cu with the demo's own
+    flags (no fast math, multiply-add contraction as nvcc defaults)."""
+    src = os.path.join(REFERENCE, MEAS_SRC)
+    dst = os.path.join(OUT, "measurement_grid.cubin")
+    inc = os.path.join(REFERENCE, "demo", "simulator", "include")
+    deps = [src, __file__, os.path.join(inc, "mapping", "kernel", "measurement_grid.h")]
+    if os.path.exists(dst) and all(os.path.getmtime(d) <= os.path.getmtime(dst) for d in deps):
+        return dst
+    tmp = dst + ".tmp"
+    r = subprocess.run([_nvcc()] + FLAGS + ["-I" + inc, src, "-o", tmp], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference measurement-grid kernels did not compile:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, dst)
+    return dst
+
+
 EVAL_SOURCES = ["dbscan.cpp", "metrics.cpp", "precision_evaluator.cpp"]
 EVAL_LIB = os.path.join(OUT, "libref_eval.so")
 
@@ -99,7 +121,8 @@ def build(verbose: bool = False) -> list[str]:
     os.makedirs(OUT, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(KERNEL_FILES)) as ex:
         ev = ex.submit(build_eval)
-        outs = list(ex.map(_one, KERNEL_FILES)) + [ev.result()]
+        ms = ex.submit(build_meas)
+        outs = list(ex.map(_one, KERNEL_FILES)) + [ev.result(), ms.result()]
     if verbose:
         print("built %d reference cubins in %s" % (len(outs), OUT))
     return outs

@@ -532,4 +532,98 @@ int dogm_ref_get_birth(dogm_ref* d, float* state, int* idx, float* weight, unsig
 int dogm_ref_grid_size(const dogm_ref* d) { return d->gs; }
 int dogm_ref_rng_threads(const dogm_ref* d) { return (int)(d->pgrid.x * d->block.x); }
 
+// ---- the demo's measurement-grid kernels (dogm/demo/simulator/mapping/kernel/
+// measurement_grid.cu), compiled from their source into oracle/_ref/measurement_grid.cubin ----
+static CUfunction g_meas_fn[3] = {};  // createPolarGridTexture, fusePolarGridTexture, cartesianGridToMeasurementGrid
+
+int dogm_ref_meas_load(const char* cubin_path) {
+    if (g_meas_fn[0]) return 0;
+    RCU(cudaFree(0));
+    RDRV(cuInit(0));
+    CUmodule mod;
+    RDRV(cuModuleLoad(&mod, cubin_path));
+    unsigned int n = 0;
+    RDRV(cuModuleGetFunctionCount(&n, mod));
+    std::vector<CUfunction> fns(n);
+    RDRV(cuModuleEnumerateFunctions(fns.data(), n, mod));
+    const char* want[3] = {"createPolarGridTextureKernel", "fusePolarGridTextureKernel",
+                           "cartesianGridToMeasurementGridKernel"};
+    for (CUfunction f : fns) {
+        const char* name = nullptr;
+        if (cuFuncGetName(&name, f) != CUDA_SUCCESS || !name) continue;
+        for (int k = 0; k < 3; ++k)
+            if (std::strstr(name, want[k])) g_meas_fn[k] = f;
+    }
+    for (int k = 0; k < 3; ++k)
+        if (!g_meas_fn[k]) return fail(std::string("kernel ") + want[k] + " not found in " + cubin_path);
+    return 0;
+}
+
+// The polar grid of one scan as the demo builds it (laser_to_meas_grid.cu:40-48): a float2
+// cudaArray of width = beams, height = range bins, bound as a surface; createPolarGridTexture
+// writes it, or, with prior (bins x beams float2) uploaded first, fusePolarGridTexture
+// combines the scan into it.  out: bins x beams float2.
+int dogm_ref_polar_ism(const float* ranges, int beams, int bins, float resolution, float stddev_range,
+                       const float* prior, float* out) {
+    if (!g_meas_fn[0]) return fail("dogm_ref_meas_load first");
+    if (beams <= 0 || bins <= 0) return fail("bad polar grid size");
+    cudaChannelFormatDesc desc = cudaCreateChannelDesc(32, 32, 0, 0, cudaChannelFormatKindFloat);
+    cudaArray_t arr = nullptr;
+    RCU(cudaMallocArray(&arr, &desc, (size_t)beams, (size_t)bins, cudaArraySurfaceLoadStore));
+    const size_t pitch = sizeof(float) * 2 * (size_t)beams;
+    if (prior) RCU(cudaMemcpy2DToArray(arr, 0, 0, prior, pitch, pitch, (size_t)bins, cudaMemcpyHostToDevice));
+    cudaResourceDesc res;
+    std::memset(&res, 0, sizeof(res));
+    res.resType = cudaResourceTypeArray;
+    res.res.array.array = arr;
+    cudaSurfaceObject_t surf = 0;
+    RCU(cudaCreateSurfaceObject(&surf, &res));
+    float* d_ranges = nullptr;
+    RCU(cudaMalloc(&d_ranges, sizeof(float) * (size_t)beams));
+    RCU(cudaMemcpy(d_ranges, ranges, sizeof(float) * (size_t)beams, cudaMemcpyHostToDevice));
+    unsigned long long s = (unsigned long long)surf;
+    int w = beams, h = bins;
+    void* p[] = {&s, &d_ranges, &w, &h, &resolution, &stddev_range};
+    // 32 x 32 blocks over (beam, bin), as laser_to_meas_grid.cu:45-47
+    RDRV(cuLaunchKernel(g_meas_fn[prior ? 1 : 0], (unsigned)(beams + 31) / 32, (unsigned)(bins + 31) / 32, 1, 32, 32, 1,
+                        0, nullptr, p, nullptr));
+    RCU(cudaDeviceSynchronize());
+    RCU(cudaMemcpy2DFromArray(out, pitch, arr, 0, 0, pitch, (size_t)bins, cudaMemcpyDeviceToHost));
+    cudaDestroySurfaceObject(surf);
+    cudaFreeArray(arr);
+    cudaFree(d_ranges);
+    return 0;
+}
+
+// cartesianGridToMeasurementGridKernel (measurement_grid.cu:115-132) on an RGBA float image
+// (gs x gs, row y = framebuffer row, y up) bound as a surface; out: gs x gs MeasurementCells.
+int dogm_ref_cart_to_meas(const float* rgba, int gs, float* out) {
+    if (!g_meas_fn[2]) return fail("dogm_ref_meas_load first");
+    if (gs <= 0) return fail("bad grid size");
+    cudaChannelFormatDesc desc = cudaCreateChannelDesc(32, 32, 32, 32, cudaChannelFormatKindFloat);
+    cudaArray_t arr = nullptr;
+    RCU(cudaMallocArray(&arr, &desc, (size_t)gs, (size_t)gs, cudaArraySurfaceLoadStore));
+    const size_t pitch = sizeof(float) * 4 * (size_t)gs;
+    RCU(cudaMemcpy2DToArray(arr, 0, 0, rgba, pitch, pitch, (size_t)gs, cudaMemcpyHostToDevice));
+    cudaResourceDesc res;
+    std::memset(&res, 0, sizeof(res));
+    res.resType = cudaResourceTypeArray;
+    res.res.array.array = arr;
+    cudaSurfaceObject_t surf = 0;
+    RCU(cudaCreateSurfaceObject(&surf, &res));
+    RMeas* d_out = nullptr;
+    RCU(cudaMalloc(&d_out, sizeof(RMeas) * (size_t)gs * gs));
+    RCU(cudaMemset(d_out, 0, sizeof(RMeas) * (size_t)gs * gs));
+    unsigned long long s = (unsigned long long)surf;
+    void* p[] = {&d_out, &s, &gs};
+    RDRV(cuLaunchKernel(g_meas_fn[2], (unsigned)(gs + 31) / 32, (unsigned)(gs + 31) / 32, 1, 32, 32, 1, 0, nullptr, p,
+                        nullptr));
+    RCU(cudaDeviceSynchronize());
+    RCU(cudaMemcpy(out, d_out, sizeof(RMeas) * (size_t)gs * gs, cudaMemcpyDeviceToHost));
+    cudaDestroySurfaceObject(surf);
+    cudaFreeArray(arr);
+    cudaFree(d_out);
+    return 0;
+}
+
 }  // extern "C"

@@ -6,7 +6,9 @@
     range bin whose occupancy sits exactly at a branch threshold may take the other branch:
     at most 1e-3 of the entries);
   * the warp, fed the GPU's own polar grid: bit-exact.
-The sensor geometry is checked on a scan with one return straight ahead."""
+The sensor geometry is checked on a scan with one return straight ahead.  Against the reference's
+own measurement-grid kernels (compiled from their source, run on cudaArray surfaces): the
+inverse sensor model bit-exact, its fusion within 2 ulp, the framebuffer conversion bit-exact."""
 import math
 
 import numpy as np
@@ -101,4 +103,74 @@ def test_generated_grid_feeds_the_update(dogm):
     cells = h.get_grid_cells()
     assert np.isfinite(cells["occ_mass"]).all() and cells["occ_mass"].max() > 0.3
     h.close()
+    g.close()
+
+
+# ---- against the reference's own measurement-grid kernels ------------------------------------
+# createPolarGridTextureKernel, fusePolarGridTextureKernel and cartesianGridToMeasurementGridKernel
+# (dogm/demo/simulator/mapping/kernel/measurement_grid.cu:72-132), compiled from their source into
+# oracle/_ref/measurement_grid.cubin and run on cudaArray surfaces as the demo runs them
+# (laser_to_meas_grid.cu:40-61).  Only the OpenGL rasterisation between them stays unpinned.
+ISM_ULP_BOUND = 0        # same operations in the same order, the same expf: bit-exact
+FUSE_ULP_BOUND = 2       # the reference build contracts its a*b + c*d sums into multiply-adds
+                         # (observed: at most 2 ulp, on ~10 % of the entries)
+
+
+@pytest.fixture(scope="module")
+def pyref_meas():
+    import pyref
+    why = pyref.meas_missing()
+    if why:
+        pytest.skip(why)
+    return pyref
+
+
+def _ulps(a, b):
+    """Distance in units in the last place between float32 arrays (both finite)."""
+    ia = np.asarray(a, np.float32).view(np.int32).astype(np.int64)
+    ib = np.asarray(b, np.float32).view(np.int32).astype(np.int64)
+    ia = np.where(ia < 0, -(ia & 0x7fffffff), ia)
+    ib = np.where(ib < 0, -(ib & 0x7fffffff), ib)
+    return np.abs(ia - ib)
+
+
+@pytest.mark.parametrize("cfg", [DEMO, dict(max_range=60.0, resolution=0.1, fov=90.0, stddev_range=0.3,
+                                            grid_length=51.2, grid_resolution=0.1, beams=733)])
+def test_ism_against_reference_kernel(dogm, pyref_meas, cfg):
+    g = dogm.MeasurementGridGenerator(**cfg)
+    bins = int(np.float32(cfg["max_range"]) / np.float32(cfg["resolution"]))
+    for k in range(3):
+        ranges = _scan(cfg["beams"], seed=20 + k, max_range=cfg["max_range"])
+        g.generate(ranges)
+        ours = g.polar()
+        ref = pyref_meas.polar_ism(ranges, bins, cfg["resolution"], cfg["stddev_range"])
+        d = _ulps(ours, ref)
+        print("ISM vs reference kernel, %d beams x %d bins: max %d ulp, %d entries differ"
+              % (cfg["beams"], bins, d.max(), (d > 0).sum()))
+        assert d.max() <= ISM_ULP_BOUND
+        # the fusion of a second scan into the polar grid (fusePolarGridTextureKernel)
+        r2 = _scan(cfg["beams"], seed=40 + k, max_range=cfg["max_range"])
+        g.generate(r2, fuse=True)
+        fused = g.polar()
+        ref_fused = pyref_meas.polar_ism(r2, bins, cfg["resolution"], cfg["stddev_range"], prior=ours)
+        d = _ulps(fused, ref_fused)
+        print("fused ISM vs reference kernel: max %d ulp, %.2e of the entries differ" % (d.max(), np.mean(d > 0)))
+        assert d.max() <= FUSE_ULP_BOUND
+    g.close()
+
+
+def test_framebuffer_conversion_against_reference_kernel(dogm, pyref_meas):
+    """The reference turns its framebuffer into MeasurementCells with rows flipped, occupied mass
+    from the red channel, free from the green, likelihood = p_A = 1 (measurement_grid.cu:115-132):
+    our grid, written back as that framebuffer, comes out of the reference kernel unchanged."""
+    cfg = dict(max_range=60.0, resolution=0.1, fov=90.0, stddev_range=0.3, grid_length=51.2, grid_resolution=0.1,
+               beams=733)
+    g = dogm.MeasurementGridGenerator(**cfg)
+    gs = g.grid_size
+    out = g.generate(_scan(cfg["beams"], seed=5, max_range=cfg["max_range"])).view(np.float32).reshape(gs, gs, 4)
+    fb = np.zeros((gs, gs, 4), np.float32)   # fb[y] = our row gs - 1 - y
+    fb[:, :, 0] = out[::-1, :, 1]
+    fb[:, :, 1] = out[::-1, :, 0]
+    ref = pyref_meas.cart_to_meas(fb)
+    assert np.array_equal(ref.view(np.uint32), out.reshape(-1, 4).view(np.uint32))
     g.close()
