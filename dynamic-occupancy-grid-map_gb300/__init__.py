@@ -93,12 +93,12 @@ class ServerStats(C.Structure):
 
 
 class Tune(C.Structure):
-    """dogm_tune: blocks per SM per stage (0 = default), radix low-digit width (0 = default)."""
-    _fields_ = [("blocks_per_sm", C.c_int * 8), ("radix_low_bits", C.c_int), ("ms_tuned", C.c_float),
+    """dogm_tune: blocks per SM per stage (0 = default), resampling tile 2^bits (0 = default 10)."""
+    _fields_ = [("blocks_per_sm", C.c_int * 8), ("resample_tile_bits", C.c_int), ("ms_tuned", C.c_float),
                 ("ms_default", C.c_float)]
 
     def as_dict(self) -> dict:
-        return {"blocks_per_sm": list(self.blocks_per_sm), "radix_low_bits": self.radix_low_bits,
+        return {"blocks_per_sm": list(self.blocks_per_sm), "resample_tile_bits": self.resample_tile_bits,
                 "ms_tuned": round(self.ms_tuned, 4), "ms_default": round(self.ms_default, 4)}
 
 
@@ -376,7 +376,7 @@ class DOGM:
         return out[:min(n.value, max_out)]
 
     def autotune(self, meas, reps: int = 10, cache_path: str | None = None, device: bool = False) -> Tune:
-        """Times launch widths and the radix split on a scratch handle fed `meas` (host array
+        """Times the resampling tile and launch widths on a scratch handle fed `meas` (host array
         or int device pointer) and applies the fastest to this handle."""
         t = Tune()
         p = C.c_void_p(meas) if isinstance(meas, int) else _ptr(np.ascontiguousarray(meas))

@@ -22,8 +22,9 @@ constexpr int kSegIpt = 4;           // sorted particles per thread in a chunk o
 constexpr int kSegTile = kThreads * kSegIpt;
 constexpr int kCellIpt = 4;          // cells per thread in the cell passes
 constexpr int kCellTile = kThreads * kCellIpt;
-constexpr int kResIpt = 4;           // joint particles per thread in resampling
-constexpr int kResTile = kThreads * kResIpt;
+// resampling tile: 2^res_bits joint particles (256 threads, 2, 4 or 8 each); a launch-shape
+// choice of the autotuner, the same for every grid of a launch
+constexpr int kResBitsMin = 9, kResBitsDefault = 10, kResBitsMax = 11;
 
 static_assert(kPredictTile == kSortTile, "predict writes the bucket counts of the scatter tiles");
 
@@ -31,7 +32,7 @@ constexpr int kMaxKeyBits = 22;      // grid_size <= 2048 -> cells < 2^22
 constexpr int kCellTileBits = 10;
 constexpr int kMaxCellTiles = (1 << kMaxKeyBits) >> kCellTileBits;  // buckets of the particle sort
 static_assert(kCellTile == (1 << kCellTileBits), "cell tiles are indexed by cell >> kCellTileBits");
-static_assert(kResTile % 32 == 0, "32 aligned sorted positions lie in one resample tile");
+static_assert((1 << kResBitsMin) % 32 == 0, "32 aligned sorted positions lie in one resample tile");
 constexpr int kMaxParticles = (1 << 24) - 1;  // keys, counts and slot indices stay below 2^24
 
 // Particle key word: bits 0..29 cell index, bit 30 "out of grid" (weight 0), bit 31 associated.
@@ -81,7 +82,7 @@ struct GridDesc {
     int q_shift;            // fixed point: weight w -> round(w * 2^q_shift)
     int ctiles;             // cell tiles = buckets of the particle sort
     int bucket_stride;      // words per row of the per-tile bucket counts (ctiles rounded up to 4)
-    int pad0;
+    int res_bits;           // resampling tile = 2^res_bits joint particles (set per launch)
     unsigned long long gs_div;  // floor(2^42 / gs) + 1: k / gs == (k * gs_div) >> 42 for k < 2^22
     // filter parameters
     float p_S, sigma_pos, sigma_vel, p_B, sigma_birth, init_max_vel;
@@ -193,7 +194,7 @@ cudaError_t launch_sort_scatter(const Batch* d_batch, int max_ctiles, const Laun
 // staged: a stage call, running the parts of GridDesc::stage_mask
 cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg, bool staged = false);
 cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);
-cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_resample(const Batch* d_batch, int res_bits, const LaunchCfg& cfg);
 cudaError_t launch_shift_stage(const GridDesc& g, int x_move, int y_move, const LaunchCfg& cfg);
 // Allocation-free shift stage: the copy of the previous cell records goes to a fixed device
 // array of kShiftScratchBytes (16 MiB = 262,144 cells, e.g. a 512 x 512 grid).

@@ -137,14 +137,15 @@ __device__ __forceinline__ int stage_slot(int rec, int chunk) { return rec * 4 +
 // 0) lie only in border cells; only for those is a split across tiles counted from the keys.
 __device__ __forceinline__ void add_persistent(const GridDesc& g, int start, int end, int n_in,
                                                unsigned long long qw) {
-    const int ts = start / kResTile, te = end / kResTile;
+    const int rb = g.res_bits;
+    const int ts = start >> rb, te = end >> rb;
     if (ts == te) {
         add_res_sum(g, ts, (unsigned long long)n_in * qw);
         return;
     }
     const bool all_in = n_in == end - start + 1;
     for (int rt = ts; rt <= te; ++rt) {
-        const int lo = max(start, rt * kResTile), hi = min(end + 1, (rt + 1) * kResTile);
+        const int lo = max(start, rt << rb), hi = min(end + 1, (rt + 1) << rb);
         int cnt = hi - lo;
         if (!all_in) {
             cnt = 0;
@@ -642,9 +643,10 @@ __device__ __forceinline__ void add_joint_range(unsigned long long (&racc)[kRunT
                                                 const GridDesc& g, long long a, long long b,
                                                 unsigned long long q) {
     if (q == 0ull) return;
-    for (long long rt = a / kResTile; rt * kResTile < b; ++rt) {
-        const long long lo = max(a, rt * (long long)kResTile);
-        const long long hi = min(b, (rt + 1) * (long long)kResTile);
+    const int rb = g.res_bits;
+    for (long long rt = a >> rb; (rt << rb) < b; ++rt) {
+        const long long lo = max(a, rt << rb);
+        const long long hi = min(b, (rt + 1) << rb);
         if (hi <= lo) continue;
         const unsigned long long v = (unsigned long long)(hi - lo) * q;
         const long long o = rt - rt0;
@@ -738,7 +740,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
         __syncthreads();
         const int lo_tile = s_bnd[0], hi_tile = s_bnd[kCellTile];
         const long long N = g.N;
-        const long long rt0 = (N + lo_tile) / kResTile;
+        const long long rt0 = (N + lo_tile) >> g.res_bits;
         unsigned long long racc[kRunTiles] = {0ull, 0ull, 0ull, 0ull};
         unsigned long long jq = 0ull;
         // w_A / w_UA of each listed cell (init_new_particles.cu:145-153) and its joint weights

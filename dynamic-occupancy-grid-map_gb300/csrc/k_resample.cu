@@ -30,10 +30,14 @@ __device__ __forceinline__ int comb_count_est(unsigned long long a, unsigned lon
 }
 
 // Shared words of a tile indexed with one pad word per 32, so that both the blocked
-// (thread t: items 8t..8t+7) and the warp-striped (item r*256 + t) accesses are free of
-// bank conflicts.
+// (thread t: items IPT t .. IPT t + IPT - 1) and the warp-striped (item r*256 + t) accesses are
+// free of bank conflicts.
 __device__ __forceinline__ int pad_idx(int j) { return j + (j >> 5); }
-constexpr int kResPadded = kResTile + 1 + ((kResTile + 1) >> 5) + 1;
+template <int IPT>
+struct ResShape {
+    static constexpr int kTile = kThreads * IPT;
+    static constexpr int kPadded = kTile + 1 + ((kTile + 1) >> 5) + 1;
+};
 
 struct HeavyRef {
     int item, first, end;  // a joint item with more copies than one thread writes
@@ -42,20 +46,25 @@ constexpr int kOwnCopies = 8;
 constexpr int kWarpCopies = 256;  // output slots a warp writes together (8 stores of 32)
 constexpr int kMaxHeavy = 256;
 
+template <int IPT>
 struct ResSmem {
-    float4 st[kResTile];         // states of the tile's joint items
-    uint32_t kw[kResTile];       // their key words
-    uint32_t lw[kResPadded];     // weight (float bits), then first output slot of each item (+ end)
+    float4 st[ResShape<IPT>::kTile];         // states of the tile's joint items
+    uint32_t kw[ResShape<IPT>::kTile];       // their key words
+    uint32_t lw[ResShape<IPT>::kPadded];     // weight (float bits), then first output slot of each item (+ end)
     HeavyRef heavy[kMaxHeavy];
     unsigned long long red[2 * (kThreads / 32)];
     int nheavy;
     int claim;
 };
 
-__global__ void __launch_bounds__(kThreads, 5) k_resample(Batch* __restrict__ bt) {
+// IPT joint particles per thread: tiles of 512, 1024 or 2048 (GridDesc::res_bits 9, 10, 11)
+template <int IPT>
+__global__ void __launch_bounds__(kThreads, IPT <= 4 ? 5 : 4) k_resample(Batch* __restrict__ bt) {
     grid_dependency_begin();
+    constexpr int kResIpt = IPT;
+    constexpr int kResTile = ResShape<IPT>::kTile;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    ResSmem& sm = *reinterpret_cast<ResSmem*>(smem_raw);
+    ResSmem<IPT>& sm = *reinterpret_cast<ResSmem<IPT>*>(smem_raw);
     const int total = batch_total(bt, kStResample);
     // tiles are taken dynamically from the end: the newborn tiles (last in the joint order,
     // with the heaviest copy counts) start first and the light tiles fill in around them
@@ -258,12 +267,22 @@ __global__ void __launch_bounds__(kThreads, 5) k_resample(Batch* __restrict__ bt
 }
 
 cudaError_t prepare_kernels() {
-    return cudaFuncSetAttribute(k_resample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ResSmem));
+    cudaError_t e = cudaFuncSetAttribute(k_resample<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ResSmem<2>));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_resample<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ResSmem<4>));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_resample<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ResSmem<8>));
+    return e;
 }
 
-cudaError_t launch_resample(const Batch* d_batch, const LaunchCfg& cfg) {
-    const int smem = (int)sizeof(ResSmem);
-    return launch_kernel(cfg, k_resample, launch_blocks(cfg, 5), kThreads, (size_t)smem, const_cast<Batch*>(d_batch));
+cudaError_t launch_resample(const Batch* d_batch, int res_bits, const LaunchCfg& cfg) {
+    Batch* b = const_cast<Batch*>(d_batch);
+    switch (res_bits) {
+        case 9: return launch_kernel(cfg, k_resample<2>, launch_blocks(cfg, 5), kThreads, sizeof(ResSmem<2>), b);
+        case 10: return launch_kernel(cfg, k_resample<4>, launch_blocks(cfg, 5), kThreads, sizeof(ResSmem<4>), b);
+        case 11: return launch_kernel(cfg, k_resample<8>, launch_blocks(cfg, 4), kThreads, sizeof(ResSmem<8>), b);
+    }
+    return cudaErrorInvalidValue;
 }
 
 // ---------------------------------------------------------------------------------------

@@ -68,6 +68,8 @@ struct Ctx {
     // bucket-count class of the batch being built: the bucket scatter's shared memory is sized
     // for 2048 buckets, or 4096 when a grid of the batch has more than 2048 cell tiles
     int scatter_ctiles = 2048;
+    // resampling tile of this context's launches: 2^res_bits joint particles
+    int res_bits = kResBitsDefault;
 
     // Captured graphs hold the launch widths: drop them when the widths change.
     void drop_graphs() {
@@ -188,7 +190,7 @@ dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
     s.pred_tiles = div_up(s.N, kPredictTile);
     s.sort_tiles = div_up(s.N, kSortTile);
     s.cell_tiles = div_up(s.C, kCellTile);
-    s.res_tiles = div_up((long long)s.N + s.B, kResTile);
+    s.res_tiles = div_up((long long)s.N + s.B, 1 << kResBitsMin);  // the finest resampling tiling
     s.scan = div_up(s.cell_tiles, 32) + 1;  // bucket groups of the column scan + the cell-tile start scan
     return DOGM_OK;
 }
@@ -200,7 +202,8 @@ void set_tiles(GridDesc& g, const Sizes& s) {
     g.tiles[kStSort] = s.sort_tiles;
     g.tiles[kStCell] = s.cell_tiles;
     g.tiles[kStBirth] = s.cell_tiles;
-    g.tiles[kStResample] = s.res_tiles;
+    g.tiles[kStResample] = div_up((long long)s.N + s.B, 1 << kResBitsDefault);
+    g.res_bits = kResBitsDefault;
     g.tiles[kStInitScan] = s.cell_tiles;
     g.tiles[kStInitExpand] = s.cell_tiles;
     g.sort_tiles = s.sort_tiles;
@@ -266,6 +269,9 @@ void build_batch(Ctx& c, dogm_handle* const* hs, int n, const std::vector<int>& 
     for (int i = 0; i < n; ++i) {
         b.g[i] = hs[i]->desc;
         b.g[i].status_out = &c.d_batch->status;
+        // the context's resampling tile (the per-tile sums are scratch of one frame)
+        b.g[i].res_bits = c.res_bits;
+        b.g[i].tiles[kStResample] = div_up((long long)b.g[i].N + b.g[i].B, 1 << c.res_bits);
         for (int s = 0; s < kNumStages; ++s) {
             int tiles = b.g[i].tiles[s];
             if ((s == kStInitScan || s == kStInitExpand) && !init_mask[i]) tiles = 0;
@@ -311,7 +317,7 @@ cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
     STAGE(2, launch_sort_scatter(c.d_batch, c.scatter_ctiles, cfg));
     STAGE(3, launch_cells(c.d_batch, cfg));
     STAGE(4, launch_newborn(c.d_batch, cfg));
-    STAGE(5, launch_resample(c.d_batch, cfg));
+    STAGE(5, launch_resample(c.d_batch, c.res_bits, cfg));
 #undef STAGE
     if (prof && (e = cudaEventRecord(c.ev[kStages], c.stream)) != cudaSuccess) return e;
     return cudaSuccess;
@@ -327,9 +333,9 @@ int graph_bucket(int n) {
     return std::min(b, kMaxBatch);
 }
 
-// A graph is keyed by its batch-size bucket, mirror and bucket-scatter class.
-int graph_key(int nb, int mirror, int scatter_ctiles) {
-    return (scatter_ctiles > 2048 ? 1 << 20 : 0) + nb * 2 + mirror;
+// A graph is keyed by its batch-size bucket, mirror, bucket-scatter class and resampling tile.
+int graph_key(int nb, int mirror, int scatter_ctiles, int res_bits) {
+    return (res_bits << 21) + (scatter_ctiles > 2048 ? 1 << 20 : 0) + nb * 2 + mirror;
 }
 
 // A device-to-host copy queued after a frame's kernels and before its completion event.
@@ -353,7 +359,7 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
         *launches = kLaunchesPerFrame + (any_init || any_clear ? 1 : 0) + (any_init ? kLaunchesInit : 0);
     } else {
         const int nb = graph_bucket(n);
-        const int key = graph_key(nb, c.cur, c.scatter_ctiles);
+        const int key = graph_key(nb, c.cur, c.scatter_ctiles, c.res_bits);
         auto it = c.graphs.find(key);
         if (it == c.graphs.end()) {
             cudaGraph_t graph;
@@ -897,7 +903,8 @@ dogm_status dogm_statistical_moments(dogm_handle* h) {
 dogm_status dogm_resampling(dogm_handle* h) {
     if (!h) return fail(DOGM_ERR_INVALID_ARGUMENT, "handle is NULL");
     Ctx& c = h->ctx;
-    dogm_status st = run_stage(h, h->stage_dt, 0u, 1, [&](const LaunchCfg& cfg) { return launch_resample(c.d_batch, cfg); });
+    dogm_status st = run_stage(h, h->stage_dt, 0u, 1,
+                               [&](const LaunchCfg& cfg) { return launch_resample(c.d_batch, c.res_bits, cfg); });
     if (st != DOGM_OK) return st;
     // the resampled particles are the current ones (the reference's particle_array =
     // particle_array_next, dogm.cu:128), and the frame ends as an update's does
@@ -1300,6 +1307,7 @@ dogm_status dogm_get_tune(dogm_handle* h, dogm_tune* out) {
     if (!h || !out) return fail(DOGM_ERR_INVALID_ARGUMENT, "NULL argument");
     std::memset(out, 0, sizeof(*out));
     for (int i = 0; i < kStages; ++i) out->blocks_per_sm[i] = h->ctx.mult[i];
+    out->resample_tile_bits = h->ctx.res_bits == kResBitsDefault ? 0 : h->ctx.res_bits;
     return DOGM_OK;
 }
 
@@ -1308,12 +1316,13 @@ dogm_status dogm_set_tune(dogm_handle* h, const dogm_tune* t) {
     for (int i = 0; i < 8; ++i)
         if (t->blocks_per_sm[i] < 0 || t->blocks_per_sm[i] > 32 || (i >= kStages && t->blocks_per_sm[i] != 0))
             return fail(DOGM_ERR_INVALID_ARGUMENT, "blocks_per_sm must be in [0, 32] for the 6 stages and 0 after them");
-    if (t->radix_low_bits != 0)
-        return fail(DOGM_ERR_INVALID_ARGUMENT, "radix_low_bits must be 0: the particle sort is one bucket pass");
+    if (t->resample_tile_bits != 0 && (t->resample_tile_bits < kResBitsMin || t->resample_tile_bits > kResBitsMax))
+        return fail(DOGM_ERR_INVALID_ARGUMENT, "resample_tile_bits must be 0 or in [9, 11] (tiles of 512 .. 2048)");
     DeviceGuard dg(h->device);
     dogm_status st = dogm_synchronize(h);  // no frame of the old shape in flight
     if (st != DOGM_OK) return st;
     for (int i = 0; i < kStages; ++i) h->ctx.mult[i] = t->blocks_per_sm[i];
+    h->ctx.res_bits = t->resample_tile_bits ? t->resample_tile_bits : kResBitsDefault;
     h->ctx.drop_graphs();
     return DOGM_OK;
 }
@@ -1336,7 +1345,7 @@ dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int
                 if (sep == std::string::npos || ln.compare(0, sep, key) != 0) continue;
                 int* m = t.blocks_per_sm;
                 found = std::sscanf(ln.c_str() + sep + 3, "%d %d %d %d %d %d %d %d %d %f %f", &m[0], &m[1], &m[2],
-                                    &m[3], &m[4], &m[5], &m[6], &m[7], &t.radix_low_bits, &t.ms_tuned,
+                                    &m[3], &m[4], &m[5], &m[6], &m[7], &t.resample_tile_bits, &t.ms_tuned,
                                     &t.ms_default) == 11;
             }
             std::fclose(f);
@@ -1364,7 +1373,25 @@ dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int
     float ms_def = 0.f;
     if ((st = time_updates(s, reps, &ms_def)) != DOGM_OK) return st;
 
-    // each stage's width, timed by the per-stage events (plain launches)
+    // 1: the resampling tile (512, 1024 or 2048 joint particles; a template instance each),
+    // whole-update time
+    int best_bits = kResBitsDefault;
+    float best_ms = ms_def;
+    for (int bits = kResBitsMin; bits <= kResBitsMax; ++bits) {
+        if (bits == kResBitsDefault) continue;
+        s->ctx.res_bits = bits;
+        s->ctx.drop_graphs();
+        float ms = 0.f;
+        if ((st = time_updates(s, reps, &ms)) != DOGM_OK) return st;
+        if (ms < 0.99f * best_ms) {
+            best_ms = ms;
+            best_bits = bits;
+        }
+    }
+    s->ctx.res_bits = best_bits;
+    s->ctx.drop_graphs();
+
+    // 2: each stage's width, timed by the per-stage events (plain launches)
     static const int kCand[] = {1, 2, 3, 4, 6, 8};
     int best_mult[kStages] = {};
     s->ctx.profile = true;
@@ -1399,6 +1426,7 @@ dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int
     dogm_tune t{};
     if (ms_tuned < 0.995f * ms_def) {
         for (int i = 0; i < kStages; ++i) t.blocks_per_sm[i] = best_mult[i];
+        t.resample_tile_bits = best_bits == kResBitsDefault ? 0 : best_bits;
         t.ms_tuned = ms_tuned;
     } else {
         t.ms_tuned = ms_def;  // nothing beat the defaults
@@ -1409,7 +1437,7 @@ dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int
         if (FILE* f = std::fopen(cache_path, "a")) {
             const int* m = t.blocks_per_sm;
             std::fprintf(f, "%s : %d %d %d %d %d %d %d %d %d %.5f %.5f\n", key.c_str(), m[0], m[1], m[2], m[3], m[4],
-                         m[5], m[6], m[7], t.radix_low_bits, t.ms_tuned, t.ms_default);
+                         m[5], m[6], m[7], t.resample_tile_bits, t.ms_tuned, t.ms_default);
             std::fclose(f);
         }
     }
@@ -1544,7 +1572,7 @@ dogm_status slot_prewarm(BatchSlot* s, int max_n) {
     for (int m = 0; m < 2; ++m) {
         for (int nb = 1; nb <= graph_bucket(std::max(1, max_n)); nb <<= 1) {
             c.scatter_ctiles = 2048;  // streams of the serving loop have at most 2048 cell tiles
-            const int key = graph_key(nb, m, c.scatter_ctiles);
+            const int key = graph_key(nb, m, c.scatter_ctiles, c.res_bits);
             if (c.graphs.count(key)) continue;
             c.cur = m;
             cudaGraph_t graph;

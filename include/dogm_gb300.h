@@ -548,31 +548,33 @@ const char* dogm_stage_name(int i);
 
 /* ---- autotuning -------------------------------------------------------------------------
  * No counterpart in the reference (its launch shape is fixed: SMs x maxThreadsPerSM / 256
- * blocks of 256 threads for every kernel, dogm/src/dogm.cu:45-47).  The runtime-tunable shape
- * of an update is the width of each stage's persistent launch (blocks per SM) and the digit
- * split of the two-pass cell-key radix sort; tile shapes are fixed at compile time. */
+ * blocks of 256 threads for every kernel, dogm/src/dogm.cu:45-47).  The tunable shape of an
+ * update is the width of each stage's persistent launch (blocks per SM) and the resampling tile
+ * (one of three compiled tile shapes). */
 typedef struct dogm_tune {
-    int blocks_per_sm[8]; /* per stage, in dogm_stage_name order; 0 = the built-in default */
-    int radix_low_bits;   /* low digit width of the cell-key sort; 0 = default (half, rounded up) */
-    float ms_tuned;       /* dogm_autotune: ms per update with these settings             */
-    float ms_default;     /* dogm_autotune: ms per update with the defaults               */
+    int blocks_per_sm[8];   /* per stage, in dogm_stage_name order (6 stages, the last two entries
+                               0); 0 = the built-in default                                       */
+    int resample_tile_bits; /* joint particles per resampling tile = 2^bits: 9, 10 or 11 (three
+                               compiled tile shapes); 0 = the default 10                        */
+    float ms_tuned;         /* dogm_autotune: ms per update with these settings               */
+    float ms_default;       /* dogm_autotune: ms per update with the defaults                 */
 } dogm_tune;
 
 /* The handle's current settings (zeros: defaults). */
 dogm_status dogm_get_tune(dogm_handle* h, dogm_tune* out);
 
-/* Applies settings to the handle's own updates (dogm_update); the radix split also applies
- * when the handle is in a batch.  Results do not change: every setting computes the same bits.
- * blocks_per_sm in [0, 32]; radix_low_bits 0 or in [key_bits - 11, min(11, key_bits - 1)]. */
+/* Applies settings to the handle's own updates (dogm_update); a batch uses its own launch
+ * context's defaults.  Results do not change: every setting computes the same bits.
+ * blocks_per_sm in [0, 32]; resample_tile_bits 0 or in [9, 11]. */
 dogm_status dogm_set_tune(dogm_handle* h, const dogm_tune* t);
 
 /* Times candidate settings on a scratch handle with the same parameters, fed `meas`
- * (grid_size^2 cells, a device pointer if device != 0): each radix split, then each stage's
- * width in {1, 2, 3, 4, 6, 8} blocks per SM with per-stage CUDA events, `reps` updates per
- * candidate.  The fastest per stage is kept only if the whole update is faster than with the
- * defaults; the result is applied to h and returned in *out.  With cache_path (may be NULL),
- * a line keyed by device name, grid size and particle counts is read instead of tuning, or
- * appended after tuning. */
+ * (grid_size^2 cells, a device pointer if device != 0): each resampling tile shape (whole
+ * updates), then each stage's width in {1, 2, 3, 4, 6, 8} blocks per SM with per-stage CUDA
+ * events, `reps` updates per candidate.  The choice is kept only if the whole update is faster
+ * than with the defaults; the result is applied to h and returned in *out.  With cache_path (may
+ * be NULL), a line keyed by device name, grid size and particle counts is read instead of
+ * tuning, or appended after tuning. */
 dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int device, int reps,
                           const char* cache_path, dogm_tune* out);
 
