@@ -53,6 +53,7 @@ struct ResSmem {
     uint32_t lw[ResShape<IPT>::kPadded];     // weight (float bits), then first output slot of each item (+ end)
     HeavyRef heavy[kMaxHeavy];
     unsigned long long red[2 * (kThreads / 32)];
+    unsigned long long r64;  // the frame's comb draw (one Philox block, drawn by thread 0)
     int nheavy;
     int claim;
 };
@@ -79,7 +80,15 @@ __global__ void __launch_bounds__(kThreads, IPT <= 4 ? 5 : 4) k_resample(Batch* 
         const int N = g.N, C = g.C, gs = g.gs, S = g.q_shift;
         const int M = N + g.fs->n_birth;
         const unsigned long long T = g.fs->joint_total;
-        if (threadIdx.x == 0) sm.nheavy = 0;
+        if (threadIdx.x == 0) {
+            sm.nheavy = 0;
+            if (g.rp_resample) {
+                sm.r64 = *g.rp_resample;
+            } else {
+                const U4 r = draw_block(g, 0u, g.frame, kDrawResample);
+                sm.r64 = ((unsigned long long)r.x << 32) | r.y;
+            }
+        }
 
         // ---- 1: the tile's joint items, warp-striped into shared memory -------------------
         // persistent items: asynchronous copies, then one batch of cell-weight gathers
@@ -152,14 +161,7 @@ __global__ void __launch_bounds__(kThreads, IPT <= 4 ? 5 : 4) k_resample(Batch* 
         __syncthreads();
 
         // ---- 2: exact scan (blocked) -> first output slot of every item -----------------
-        unsigned long long r64;
-        if (g.rp_resample) {
-            r64 = *g.rp_resample;
-        } else {
-            const U4 r = draw_block(g, 0u, g.frame, kDrawResample);
-            r64 = ((unsigned long long)r.x << 32) | r.y;
-        }
-        const unsigned long long U = __umul64hi(r64, T);  // floor(u * T), u = r64 / 2^64
+        const unsigned long long U = __umul64hi(sm.r64, T);  // floor(u * T), u = r64 / 2^64
         const float inv_T = T ? __frcp_rn(__ull2float_rn(T)) : 0.0f;
         const int j0 = threadIdx.x * kResIpt;
         unsigned long long q[kResIpt];
