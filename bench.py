@@ -297,6 +297,30 @@ def run_gb300(args, rank: int, world: int):
     launches = g.last_launch_count() * K * repeats
     total_ms = reduce_max(total_ms, world)
 
+    # the update at the residency a single persistent kernel per frame would have: every stage
+    # limited to what the largest one (the cell pass: 64 registers, 87 KB shared memory) allows,
+    # two 512-thread blocks = 1024 threads per SM (predict 2 x 512, bucket scan 1 x 1024,
+    # newborn and resampling 4 x 256); same frames, 0.3 s of updates
+    saved = g.get_tune()
+    single = dogm.Tune()
+    for i, m in enumerate((2, 1, 2, 2, 4, 4)):
+        single.blocks_per_sm[i] = m
+    g.set_tune(single)
+    for r in range(3):
+        timed_block(1 + repeats + r)
+    g.synchronize()
+    sr = max(1, repeats * 3 // 10)
+    a, b_ = ev.new(), ev.new()
+    ev.record(a)
+    for r in range(sr):
+        timed_block(4 + repeats + r)
+    ev.record(b_)
+    single_ms = reduce_max(ev.elapsed(a, b_), world) / (sr * K)
+    g.set_tune(saved)
+    for r in range(3):
+        timed_block(4 + repeats + sr + r)
+    g.synchronize()
+
     # synchronous updates, each waited for on the host like the reference's updateGrid
     # (dogm.cu:130): host wall clock per update, measurement grids in HBM
     sync_ms = []
@@ -382,6 +406,9 @@ def run_gb300(args, rank: int, world: int):
                    "autotune": tune.as_dict() if tune is not None else "off"},
         "hbm_gbs_whole_update": round(alg / (ms * 1e-3) / 1e9, 1),
         "updates_per_s": round(1e3 / ms, 1),
+        "single_kernel_residency": {"ms_per_update": round(single_ms, 4), "blocks_per_sm": [2, 1, 2, 2, 4, 4],
+                                    "note": "every stage at the residency of one persistent kernel per frame "
+                                            "(the cell pass's 2 x 512 threads per SM)"},
         "sync_update_ms": {"median": round(statistics.median(sync_ms), 4), "mean": round(statistics.fmean(sync_ms), 4),
                            "updates": len(sync_ms),
                            "method": "host wall clock around one update and its synchronisation (as the reference's "
