@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
 constexpr int kPredictThreads = 512;
 static_assert(kPredictTile % kPredictThreads == 0, "whole particles per thread");
 
-__global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restrict__ bt, int mode) {
+__global__ void __launch_bounds__(kPredictThreads, 3) k_predict(Batch* __restrict__ bt, int mode) {
     grid_dependency_begin();
     __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (bucket of the sort)
     const int total = batch_total(bt, kStPredict);
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(kPredictThreads, 4) k_predict(Batch* __restric
         const bool shift = (mode == 0) && g.shifted;
         const float fsx = (float)g.shift_x, fsy = (float)g.shift_y;
         const int base = lt * kPredictTile;
-#pragma unroll 4
+#pragma unroll
         for (int k = 0; k < kPredictTile / kPredictThreads; ++k) {
             const int i = base + k * kPredictThreads + threadIdx.x;
             bool valid = i < g.N;
@@ -300,7 +300,7 @@ cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCf
 }
 
 cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg) {
-    k_predict<<<launch_blocks(cfg, 4), kPredictThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), stage_mode);
+    k_predict<<<launch_blocks(cfg, 3), kPredictThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), stage_mode);
     return cudaGetLastError();
 }
 
