@@ -112,8 +112,8 @@ struct GridDesc {
     // scratch
     uint32_t* hsort;        // sort_tiles x bucket_stride: per-tile bucket counts, then offsets
     uint32_t* ctile_cnt;    // per cell tile: particles whose cell lies in it (counted by predict)
-    uint32_t* ctile_start;  // per cell tile + 1: first sorted position of the tile (exclusive scan)
-    uint32_t* ctile_order;  // cell tiles in claim order: tiles with many particles first
+    uint4* ctile_job;       // cell tiles in claim order (many particles first): {tile, first
+                            // sorted position, end, 0}
     unsigned long long* cell_sum;  // per cell tile: quantised newborn mass (first half) and
                                    // first-frame occupied mass (second half)
     unsigned long long* res_sum;   // per resample tile: quantised joint weight (exact atomics)

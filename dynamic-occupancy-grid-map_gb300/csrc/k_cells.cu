@@ -67,7 +67,7 @@ __device__ __forceinline__ Run run_shfl_up(const Run& a, int o) {
 
 // ---------------------------------------------------------------------------------------
 // Fused per-cell update over one tile of kCellTile cells and the particles that lie in it,
-// positions [ctile_start[t], ctile_start[t + 1]) of the bucketed (T) and sorted (S) arrays.
+// positions [start, end) of the bucketed (T) and sorted (S) arrays (the tile's ctile_job).
 //   S  stable counting sort of the bucket by cell, T -> S: per-cell counts, their exclusive
 //      scan, then, chunk by chunk in bucket order, each particle's rank among the earlier
 //      particles of its cell (warp ranks by match_any, per-warp counts, offsets across warps).
@@ -120,10 +120,13 @@ struct CellSmem {
     Run wagg[kCellThreads / 32];  // each warp's run, then (wpre) the runs before each warp
     Run wpre[kCellThreads / 32];
     unsigned long long red[kCellThreads / 32], red2[kCellThreads / 32];
-    int tiles[2];  // the block's current tile and the one claimed for the next iteration
+    uint4 job[2];  // the block's current tile and the one claimed for the next iteration:
+    int jt[2];     // work index (>= total: none left), grid, and ctile_job entry
+    int jgrid[2];
 };
 static_assert(offsetof(CellSmem, meas) % 16 == 0, "16-byte cp.async destination");
 static_assert(offsetof(CellSmem, u2) % 16 == 0, "16-byte staged records");
+static_assert(offsetof(CellSmem, job) % 16 == 0, "16-byte cp.async destination");
 static_assert(sizeof(dogm_grid_cell) == 64, "a record is four float4");
 
 // Record chunk j of lane l is staged at float4 slot 4 l + (j ^ ((l >> 1) & 3)): for each j the
@@ -371,19 +374,28 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             for (int i = tid; i < g.tiles[kStCell]; i += stride) g.ctile_cnt[i] = 0u;
         }
     }
-    // tiles are claimed one ahead: thread 0 takes the next tile while the block works on this
-    // one, so a claim costs no barrier of its own (the body's barriers publish it)
-    if (threadIdx.x == 0) sm.tiles[0] = (int)atomicAdd(&bt->counters[kStCell], 1u);
+    // tiles are claimed one ahead: thread 0 takes the next work index at the start of a tile
+    // and, once the in-bucket sort is done, copies its ctile_job entry to shared memory
+    // (cp.async); the body's barriers publish both, so a tile starts without a load chain
+    if (threadIdx.x == 0) {
+        const int t0 = (int)atomicAdd(&bt->counters[kStCell], 1u);
+        sm.jt[0] = t0;
+        if (t0 < total) {
+            const int gi = grid_of_tile(bt, kStCell, t0);
+            sm.jgrid[0] = gi;
+            sm.job[0] = bt->g[gi].ctile_job[t0 - bt->prefix[gi][kStCell]];
+        }
+    }
     __syncthreads();
     for (int it = 0;; it ^= 1) {
-        const int t = sm.tiles[it];
-        if (t >= total) break;
-        if (threadIdx.x == 0) sm.tiles[it ^ 1] = (int)atomicAdd(&bt->counters[kStCell], 1u);
-        const int gi = grid_of_tile(bt, kStCell, t);
-        const GridDesc& g = bt->g[gi];
-        const int lt = (int)g.ctile_order[t - bt->prefix[gi][kStCell]];  // full tiles first
+        if (sm.jt[it] >= total) break;
+        int next = 0;
+        if (threadIdx.x == 0) next = (int)atomicAdd(&bt->counters[kStCell], 1u);
+        const GridDesc& g = bt->g[sm.jgrid[it]];
+        const uint4 job = sm.job[it];
+        const int lt = (int)job.x;  // full tiles first
         const int base = lt * kCellTile;
-        const int p0 = (int)g.ctile_start[lt], p1 = (int)g.ctile_start[lt + 1];
+        const int p0 = (int)job.y, p1 = (int)job.z;
         // prefetch the measurement and the (shifted) previous free mass of this thread's cells
         const bool meas16 = (reinterpret_cast<uintptr_t>(g.meas_src) & 15u) == 0u;
         for (int r = 0; r < kCellTile / kCellThreads; ++r) {
@@ -412,6 +424,14 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
         const int np = p1 - p0;
         if (np > 0) sort_bucket(sm, g, base, p0, p1);  // block-uniform; ends with a barrier
         else __syncthreads();
+        if (threadIdx.x == 0) {  // the next tile's job (slot it ^ 1 was last read before the barrier)
+            sm.jt[it ^ 1] = next;
+            if (next < total) {
+                const int gn = grid_of_tile(bt, kStCell, next);
+                sm.jgrid[it ^ 1] = gn;
+                cp_async16(&sm.job[it ^ 1], bt->g[gn].ctile_job + (next - bt->prefix[gn][kStCell]));
+            }
+        }
 
         // ---- A: segmented reduction of the tile's particles ------------------------------
         // thread t walks its own consecutive share [i_beg, i_end) of the tile's particles, so
@@ -611,6 +631,7 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             sm.red[warp] = qb;
             sm.red2[warp] = jq;
         }
+        if (threadIdx.x == 0) cp_async_wait_all();  // the next tile's job has landed
         __syncthreads();
         if (threadIdx.x == 0) {
             unsigned long long tile_qb = 0ull, tile_jq = 0ull;

@@ -26,10 +26,10 @@ constexpr int kScanKeep = 16;  // tiles per warp kept in registers (N up to 2M p
 constexpr int kCtilePer = kMaxCellTiles / (kScanWarps * 32);
 static_assert(kCtilePer * kScanWarps * 32 == kMaxCellTiles, "one block scans every cell-tile count");
 
-// Exclusive scan of the per-cell-tile particle counts that predict took: ctile_start[i] is
-// the first sorted position of cell tile i, ctile_start[n] = N.  Also the claim order of the
-// cell pass: tiles by decreasing bit length of their particle count (the fullest, slowest
-// tiles start first; the last tiles claimed are the quickest), in any order within a class.
+// Exclusive scan of the per-cell-tile particle counts that predict took, written as the cell
+// pass's work list: ctile_job[j] = {tile, first sorted position, end, 0} of the j-th tile to
+// claim, tiles by decreasing bit length of their particle count (the fullest, slowest tiles
+// start first; the last tiles claimed are the quickest), in any order within a class.
 // Run by one block as the last work item of the bucket scan (after predict, before the
 // scatter and the cell pass).  scratch: >= 64 words.
 __device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) {
@@ -56,14 +56,8 @@ __device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) 
     uint32_t e = x - s;
     for (int w = 0; w < warp; ++w) e += red[w];
 #pragma unroll
-    for (int j = 0; j < kCtilePer; ++j) {
-        if (i0 + j < n) {
-            g.ctile_start[i0 + j] = e;
-            atomicAdd(&cls_count[15 - min(15, 32 - __clz((int)v[j]))], 1u);
-        }
-        e += v[j];
-    }
-    if (i0 < n && n <= i0 + kCtilePer) g.ctile_start[n] = e;
+    for (int j = 0; j < kCtilePer; ++j)
+        if (i0 + j < n) atomicAdd(&cls_count[15 - min(15, 32 - __clz((int)v[j]))], 1u);
     __syncthreads();
     if (warp == 0) {
         const uint32_t c = lane < 16 ? cls_count[lane] : 0u;
@@ -77,8 +71,13 @@ __device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) 
     }
     __syncthreads();
 #pragma unroll
-    for (int j = 0; j < kCtilePer; ++j)
-        if (i0 + j < n) g.ctile_order[atomicAdd(&cls_next[15 - min(15, 32 - __clz((int)v[j]))], 1u)] = (uint32_t)(i0 + j);
+    for (int j = 0; j < kCtilePer; ++j) {
+        if (i0 + j < n) {
+            const uint32_t pos = atomicAdd(&cls_next[15 - min(15, 32 - __clz((int)v[j]))], 1u);
+            g.ctile_job[pos] = make_uint4((uint32_t)(i0 + j), e, e + v[j], 0u);
+        }
+        e += v[j];
+    }
     __syncthreads();
 }
 

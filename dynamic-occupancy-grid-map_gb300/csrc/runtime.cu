@@ -538,8 +538,7 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     g.free_old = fa; g.free_new = fb;
     ALLOC(g.rho_b, s.C); ALLOC(g.w_cell, s.C);
     ALLOC(g.hsort, (size_t)s.sort_tiles * g.bucket_stride);
-    ALLOC(g.ctile_cnt, s.cell_tiles); ALLOC(g.ctile_start, (size_t)s.cell_tiles + 1);
-    ALLOC(g.ctile_order, s.cell_tiles);
+    ALLOC(g.ctile_cnt, s.cell_tiles); ALLOC(g.ctile_job, s.cell_tiles);
     ALLOC(g.cell_sum, 2 * (size_t)s.cell_tiles);
     ALLOC(g.res_sum, s.res_tiles);
     ALLOC(g.fs, 1);
