@@ -142,6 +142,7 @@ struct Batch {
     int n_grids;
     unsigned int status;                     // OR of every grid's error bits this frame
     unsigned int counters[kNumStages];       // dynamic tile counters
+    unsigned int* status_host;               // this frame's status word in mapped host memory
     int prefix[kMaxBatch + 1][kNumStages];   // prefix[i][s]: tiles of stage s in grids < i
     GridDesc g[kMaxBatch];
 };

@@ -52,7 +52,8 @@ struct Ctx {
     bool own_stream = false;
     Batch* d_batch = nullptr;
     Batch* h_batch[2] = {nullptr, nullptr};      // pinned
-    unsigned int* h_status = nullptr;            // pinned, one word per mirror
+    unsigned int* h_status = nullptr;            // pinned and mapped, one word per mirror
+    unsigned int* d_h_status = nullptr;          // its device address
     cudaEvent_t done[2] = {nullptr, nullptr};    // the frame that read mirror i has finished
     bool pending[2] = {false, false};
     int cur = 0;                                 // mirror of the frame being built
@@ -104,8 +105,9 @@ dogm_status ctx_init(Ctx& c, int device) {
         std::memset(c.h_batch[i], 0, sizeof(Batch));
         DOGM_CUDA(cudaEventCreateWithFlags(&c.done[i], cudaEventDisableTiming));
     }
-    DOGM_CUDA(cudaMallocHost(&c.h_status, 2 * sizeof(unsigned int)));
+    DOGM_CUDA(cudaHostAlloc((void**)&c.h_status, 2 * sizeof(unsigned int), cudaHostAllocMapped | cudaHostAllocPortable));
     c.h_status[0] = c.h_status[1] = 0;
+    DOGM_CUDA(cudaHostGetDevicePointer((void**)&c.d_h_status, c.h_status, 0));
     for (auto& e : c.ev) DOGM_CUDA(cudaEventCreate(&e));
     return DOGM_OK;
 }
@@ -261,6 +263,7 @@ void build_batch(Ctx& c, dogm_handle* const* hs, int n, const std::vector<int>& 
     Batch& b = *c.h_batch[c.cur];
     b.n_grids = n;
     b.status = 0u;
+    b.status_host = c.d_h_status + c.cur;
     c.scatter_ctiles = 2048;
     for (int i = 0; i < n; ++i)
         if (hs[i]->desc.ctiles > c.scatter_ctiles) c.scatter_ctiles = kMaxCellTiles;
@@ -280,16 +283,16 @@ void build_batch(Ctx& c, dogm_handle* const* hs, int n, const std::vector<int>& 
     }
 }
 
-size_t batch_head_bytes(int n) { return offsetof(Batch, prefix) + sizeof(int) * kNumStages * (size_t)(n + 1); }
-size_t batch_desc_bytes(int n) { return sizeof(GridDesc) * (size_t)n; }
+// The header (with the unused prefix rows past n, about 2 KB) and n descriptors in one copy:
+// a second copy cost about 2 us of every graph-launched frame.
+size_t batch_upload_bytes(int n) { return offsetof(Batch, g) + sizeof(GridDesc) * (size_t)n; }
 
 cudaError_t upload_batch(Ctx& c, int n) {
-    Batch* h = c.h_batch[c.cur];
-    cudaError_t e = cudaMemcpyAsync(c.d_batch, h, batch_head_bytes(n), cudaMemcpyHostToDevice, c.stream);
-    if (e != cudaSuccess) return e;
-    return cudaMemcpyAsync(&c.d_batch->g[0], &h->g[0], batch_desc_bytes(n), cudaMemcpyHostToDevice, c.stream);
+    return cudaMemcpyAsync(c.d_batch, c.h_batch[c.cur], batch_upload_bytes(n), cudaMemcpyHostToDevice, c.stream);
 }
 
+// Status of a frame launched without a graph (stage calls end with other kernels than the
+// resampling, which writes the word itself; the same value either way).
 cudaError_t download_status(Ctx& c) {
     return cudaMemcpyAsync(c.h_status + c.cur, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
                            c.stream);
@@ -363,10 +366,11 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
         auto it = c.graphs.find(key);
         if (it == c.graphs.end()) {
             cudaGraph_t graph;
+            // the descriptor upload and the six kernels; the resampling kernel stores the
+            // frame's status word into mapped host memory, so no copy follows the kernels
             DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
             e = upload_batch(c, nb);
             if (e == cudaSuccess) e = frame_kernels(c, false, false);
-            if (e == cudaSuccess) e = download_status(c);
             cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
             if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
             if (e2 != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
@@ -1578,7 +1582,6 @@ dogm_status slot_prewarm(BatchSlot* s, int max_n) {
             DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
             cudaError_t e = upload_batch(c, nb);
             if (e == cudaSuccess) e = frame_kernels(c, false, false);
-            if (e == cudaSuccess) e = download_status(c);
             cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
             c.cur = cur;
             if (e != cudaSuccess || e2 != cudaSuccess)
