@@ -93,6 +93,7 @@ static_assert(kCellTile % kCellThreads == 0, "whole cells per thread");
 constexpr int kCellWarps = kCellThreads / 32;
 constexpr int kBucketIpt = 8;  // bucket particles per thread in a chunk of the counting sort
 constexpr int kBucketChunk = kCellThreads * kBucketIpt;
+static_assert(kCellTile == 2 * kCellThreads && kBucketChunk < 65536, "one pair of 16-bit cell counts per thread");
 
 struct CellSmem {
     dogm_measurement_cell meas[kCellTile];  // prefetched (cp.async) while S and A run
@@ -294,15 +295,19 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
         __syncthreads();
         rank_chunk(R);
         __syncthreads();
-        for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) {
+        {
+            // two cells per 32-bit word: the halves never carry (a chunk holds <= 4096)
+            uint32_t* wh = reinterpret_cast<uint32_t*>(&sm.u2.whist[0][0]);
+            const int cp = threadIdx.x;  // cells 2 cp, 2 cp + 1
             uint32_t acc = 0u;
 #pragma unroll
             for (int w = 0; w < kCellWarps; ++w) {
-                const uint32_t n = sm.u2.whist[w][c];
-                sm.u2.whist[w][c] = (uint16_t)acc;
+                const uint32_t n = wh[w * (kCellTile / 2) + cp];
+                wh[w * (kCellTile / 2) + cp] = acc;
                 acc += n;
             }
-            sm.u1.srt.cnt[c] = acc;
+            sm.u1.srt.cnt[2 * cp] = acc & 0xffffu;
+            sm.u1.srt.cnt[2 * cp + 1] = acc >> 16;
         }
         __syncthreads();
         scan_counts();
@@ -337,17 +342,19 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
         __syncthreads();
         rank_chunk(R);
         __syncthreads();
-        for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) {
+        {
+            // two cells per 32-bit word, as above
+            uint32_t* wh = reinterpret_cast<uint32_t*>(&sm.u2.whist[0][0]);
+            const int cp = threadIdx.x;
             uint32_t acc = 0u;
-            if (sm.u1.srt.cnt[c]) {  // cells without particles keep zero offsets
 #pragma unroll
-                for (int w = 0; w < kCellWarps; ++w) {
-                    const uint32_t n = sm.u2.whist[w][c];
-                    sm.u2.whist[w][c] = (uint16_t)acc;
-                    acc += n;
-                }
+            for (int w = 0; w < kCellWarps; ++w) {
+                const uint32_t n = wh[w * (kCellTile / 2) + cp];
+                wh[w * (kCellTile / 2) + cp] = acc;
+                acc += n;
             }
-            sm.u1.srt.off[cur ^ 1][c] = sm.u1.srt.off[cur][c] + acc;
+            sm.u1.srt.off[cur ^ 1][2 * cp] = sm.u1.srt.off[cur][2 * cp] + (acc & 0xffffu);
+            sm.u1.srt.off[cur ^ 1][2 * cp + 1] = sm.u1.srt.off[cur][2 * cp + 1] + (acc >> 16);
         }
         __syncthreads();
         scatter_chunk(c0, R, cur);
