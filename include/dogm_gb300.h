@@ -571,10 +571,11 @@ dogm_status dogm_set_tune(dogm_handle* h, const dogm_tune* t);
 /* Times candidate settings on a scratch handle with the same parameters, fed `meas`
  * (grid_size^2 cells, a device pointer if device != 0): each resampling tile shape (whole
  * updates), then each stage's width in {1, 2, 3, 4, 6, 8} blocks per SM with per-stage CUDA
- * events, `reps` updates per candidate.  The choice is kept only if the whole update is faster
- * than with the defaults; the result is applied to h and returned in *out.  With cache_path (may
- * be NULL), a line keyed by device name, grid size and particle counts is read instead of
- * tuning, or appended after tuning. */
+ * events, `reps` updates per candidate and timing.  Candidates are timed in three interleaved
+ * rounds (the scratch state evolves while it is timed) and compared on their sums; a setting
+ * other than the built-in one, and the tuned shape as a whole, must win by 2 %.  The result is
+ * applied to h and returned in *out.  With cache_path (may be NULL), a line keyed by device
+ * name, grid size and particle counts is read instead of tuning, or appended after tuning. */
 dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int device, int reps,
                           const char* cache_path, dogm_tune* out);
 
