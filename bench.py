@@ -429,8 +429,9 @@ def run_gb300(args, rank: int, world: int):
         d.free()
     line["meas_grid"] = run_meas_grid(dogm)
     if not args.no_serving:
-        line["batched"] = run_batched(dogm, scene)
+        # the latency-sensitive serving leg first: later in a process its tails grew
         line["serving"] = run_serving(dogm, scene, seconds=args.serve_seconds)
+        line["batched"] = run_batched(dogm, scene)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(frames, cfg, args.cpu_frames)
     return line
