@@ -196,12 +196,14 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
         const uint32_t c = kw == 0xffffffffu ? 0xffffffffu : (kw & kCellMask) - (uint32_t)base;
         return c < (uint32_t)kCellTile ? c : 0xffffffffu;
     };
+    // the bucketed particles are last read in this pass: evict-first loads (__ldcs) keep L2
+    // for the sorted copy, which resampling reads again
     auto load_chunk = [&](int c0, int R) {
         const int wbase = c0 + warp * 32 * R;
 #pragma unroll
         for (int k = 0; k < kBucketIpt; ++k) {
             const int i = wbase + k * 32 + lane;
-            key[k] = (k < R && i < p1) ? g.T_key[i] : 0xffffffffu;
+            key[k] = (k < R && i < p1) ? __ldcs(g.T_key + i) : 0xffffffffu;
         }
     };
     auto zero_whist = [&]() {
@@ -268,7 +270,7 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
                 out[j] = -1;
                 if (k < R && c != 0xffffffffu)
                     out[j] = p0 + (int)(sm.u1.srt.off[cur][c] + sm.u2.whist[warp][c] + rank[k]);
-                st[j] = g.T_state[(k < R && i < p1) ? i : p1 - 1];
+                st[j] = __ldcs(g.T_state + ((k < R && i < p1) ? i : p1 - 1));
             }
 #pragma unroll
             for (int j = 0; j < kHalf; ++j) {
@@ -607,8 +609,11 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                 stage[stage_slot(lane, 3)] = s3;
             }
             if (mask & kPartMasses) {
-                if (g.copy_meas) g.meas_own[k] = m;
-                g.free_new[k] = o.free_up;
+                // read by nothing later in the frame: stored with the evict-first hint, so they
+                // do not push the sorted particles and cell weights (read by resampling) out of L2
+                if (g.copy_meas)
+                    __stcs(reinterpret_cast<float4*>(g.meas_own + k), make_float4(m.free_mass, m.occ_mass, m.likelihood, m.p_A));
+                __stcs(g.free_new + k, o.free_up);
                 g.rho_b[k] = make_float2(o.rho_b, m.p_A);
                 qb += quantize(o.rho_b, g.q_shift);
             }
@@ -621,12 +626,13 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                 }
             }
             }  // k < g.C
-            // the warp's records, 512 contiguous bytes per store instruction
+            // the warp's records, 512 contiguous bytes per store instruction (evict-first: only
+            // the newborn pass and the readback touch them again)
             __syncwarp();
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int rec = q * 8 + (lane >> 2), chunk = lane & 3;
-                if (rec < n_rec) dst[rec * 4 + chunk] = stage[stage_slot(rec, chunk)];
+                if (rec < n_rec) __stcs(dst + rec * 4 + chunk, stage[stage_slot(rec, chunk)]);
             }
             __syncwarp();  // the stage is refilled by the next r
         }
@@ -710,7 +716,7 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
             const int k = base + threadIdx.x * kCellIpt + j;
-            bp[j] = (k < g.C) ? g.rho_b[k] : make_float2(0.0f, 0.0f);  // {rho_b, p_A}
+            bp[j] = (k < g.C) ? __ldcs(g.rho_b + k) : make_float2(0.0f, 0.0f);  // {rho_b, p_A}
         }
         // the earlier tiles' sums load while the cells' values are in flight
         const unsigned long long part = block_prefix_part(g.cell_sum, lt);

@@ -208,6 +208,8 @@ __global__ void __launch_bounds__(kThreads, IPT <= 4 ? 5 : 4) k_resample(Batch* 
         // per store, each lane finding the owner of its slot (the last lane whose first slot
         // is <= it; items without copies share their first slot with the next item).  A warp
         // with a long range writes per item, and items with many copies go to the block.
+        // the resampled set is read again only by the next frame's predict, after hundreds of MB
+        // of other traffic: evict-first stores (__stcs)
         float4* __restrict__ P_state = g.P_state;
         uint32_t* __restrict__ P_key = g.P_key;
         int* __restrict__ dbg_src = g.dbg_src;
@@ -228,8 +230,8 @@ __global__ void __launch_bounds__(kThreads, IPT <= 4 ? 5 : 4) k_resample(Batch* 
                         if (f <= slot) owner += step;
                     }
                     if (slot < we) {
-                        P_state[slot] = sm.st[j0 + owner];
-                        P_key[slot] = sm.kw[j0 + owner];
+                        __stcs(P_state + slot, sm.st[j0 + owner]);
+                        __stcs(P_key + slot, sm.kw[j0 + owner]);
                         if (dbg_src) dbg_src[slot] = base + j0 + owner;
                     }
                 }
@@ -244,8 +246,8 @@ __global__ void __launch_bounds__(kThreads, IPT <= 4 ? 5 : 4) k_resample(Batch* 
                     const float4 st = sm.st[j];
                     const uint32_t kw = sm.kw[j];
                     for (int s = first; s < end; ++s) {
-                        P_state[s] = st;
-                        P_key[s] = kw;
+                        __stcs(P_state + s, st);
+                        __stcs(P_key + s, kw);
                         if (dbg_src) dbg_src[s] = base + j;
                     }
                 }
@@ -258,8 +260,8 @@ __global__ void __launch_bounds__(kThreads, IPT <= 4 ? 5 : 4) k_resample(Batch* 
             const float4 st = sm.st[e.item];
             const uint32_t kw = sm.kw[e.item];
             for (int s = e.first + threadIdx.x; s < e.end; s += kThreads) {
-                P_state[s] = st;
-                P_key[s] = kw;
+                __stcs(P_state + s, st);
+                __stcs(P_key + s, kw);
                 if (dbg_src) dbg_src[s] = base + e.item;
             }
         }

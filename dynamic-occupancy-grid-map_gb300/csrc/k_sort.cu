@@ -217,10 +217,12 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_sort_scatter(Batch* __re
         const int base = lt * kSortTile + warp * (32 * kScatterIpt);
         uint32_t key[kScatterIpt];
         uint16_t rank[kScatterIpt];
+        // the predicted particles are read here for the last time in the frame: evict-first
+        // loads (__ldcs) leave L2 to the bucketed copy the cell pass reads next
 #pragma unroll
         for (int k = 0; k < kScatterIpt; ++k) {
             const int pos = base + k * 32 + lane;
-            key[k] = pos < g.N ? g.P_key[pos] : 0xffffffffu;
+            key[k] = pos < g.N ? __ldcs(g.P_key + pos) : 0xffffffffu;
         }
         // stable rank within the warp: rounds in input order, peers by match_any (a key whose
         // bucket lies outside the grid -- only injected state can hold one -- is not placed)
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_sort_scatter(Batch* __re
                 const uint32_t d = (key[k] & kCellMask) >> kCellTileBits;
                 out[j] = 0xffffffffu;
                 if (pos < g.N && d < (uint32_t)nb) out[j] = gbase[d] + my_hist[d] + rank[k];
-                st[j] = p_state[pos < g.N ? pos : g.N - 1];
+                st[j] = __ldcs(p_state + (pos < g.N ? pos : g.N - 1));
             }
 #pragma unroll
             for (int j = 0; j < kHalf; ++j) {
