@@ -50,7 +50,11 @@ struct Ctx {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    Batch* d_batch = nullptr;
+    Batch* d_batch = nullptr;                    // the device batch of mirror `cur`
+    Batch* d_batch_m[2] = {nullptr, nullptr};    // one device batch per mirror
+    // graph frames upload their descriptors on this stream, ahead of the frame before them
+    cudaStream_t up_stream = nullptr;
+    cudaEvent_t up_done[2] = {nullptr, nullptr};
     Batch* h_batch[2] = {nullptr, nullptr};      // pinned
     unsigned int* h_status = nullptr;            // pinned and mapped, one word per mirror
     unsigned int* d_h_status = nullptr;          // its device address
@@ -80,11 +84,13 @@ struct Ctx {
 
     ~Ctx() {
         for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
-        if (d_batch) cudaFree(d_batch);
         for (int i = 0; i < 2; ++i) {
+            if (d_batch_m[i]) cudaFree(d_batch_m[i]);
             if (h_batch[i]) cudaFreeHost(h_batch[i]);
             if (done[i]) cudaEventDestroy(done[i]);
+            if (up_done[i]) cudaEventDestroy(up_done[i]);
         }
+        if (up_stream) cudaStreamDestroy(up_stream);
         for (auto& e : ev)
             if (e) cudaEventDestroy(e);
         if (h_status) cudaFreeHost(h_status);
@@ -98,18 +104,27 @@ dogm_status ctx_init(Ctx& c, int device) {
     DOGM_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
     DOGM_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
     c.own_stream = true;
-    DOGM_CUDA(cudaMalloc(&c.d_batch, sizeof(Batch)));
-    DOGM_CUDA(cudaMemset(c.d_batch, 0, sizeof(Batch)));
+    DOGM_CUDA(cudaStreamCreateWithFlags(&c.up_stream, cudaStreamNonBlocking));
     for (int i = 0; i < 2; ++i) {
+        DOGM_CUDA(cudaMalloc(&c.d_batch_m[i], sizeof(Batch)));
+        DOGM_CUDA(cudaMemset(c.d_batch_m[i], 0, sizeof(Batch)));
         DOGM_CUDA(cudaMallocHost(&c.h_batch[i], sizeof(Batch)));
         std::memset(c.h_batch[i], 0, sizeof(Batch));
         DOGM_CUDA(cudaEventCreateWithFlags(&c.done[i], cudaEventDisableTiming));
+        DOGM_CUDA(cudaEventCreateWithFlags(&c.up_done[i], cudaEventDisableTiming));
     }
+    c.d_batch = c.d_batch_m[0];
     DOGM_CUDA(cudaHostAlloc((void**)&c.h_status, 2 * sizeof(unsigned int), cudaHostAllocMapped | cudaHostAllocPortable));
     c.h_status[0] = c.h_status[1] = 0;
     DOGM_CUDA(cudaHostGetDevicePointer((void**)&c.d_h_status, c.h_status, 0));
     for (auto& e : c.ev) DOGM_CUDA(cudaEventCreate(&e));
     return DOGM_OK;
+}
+
+// Makes mirror m the current one (its pinned host batch and its device batch).
+void set_mirror(Ctx& c, int m) {
+    c.cur = m;
+    c.d_batch = c.d_batch_m[m];
 }
 
 // The mirror for the next frame: waits until the frame that last read it has finished.
@@ -362,15 +377,21 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
         *launches = kLaunchesPerFrame + (any_init || any_clear ? 1 : 0) + (any_init ? kLaunchesInit : 0);
     } else {
         const int nb = graph_bucket(n);
+        // the descriptors go up on the upload stream into this mirror's device batch (the frame
+        // that last read it has finished: acquire_mirror), so the copy runs while the frame
+        // before this one is still on the device instead of between the two
+        DOGM_CUDA(cudaMemcpyAsync(c.d_batch, c.h_batch[c.cur], batch_upload_bytes(nb), cudaMemcpyHostToDevice,
+                                  c.up_stream));
+        DOGM_CUDA(cudaEventRecord(c.up_done[c.cur], c.up_stream));
+        DOGM_CUDA(cudaStreamWaitEvent(c.stream, c.up_done[c.cur], 0));
         const int key = graph_key(nb, c.cur, c.scatter_ctiles, c.res_bits);
         auto it = c.graphs.find(key);
         if (it == c.graphs.end()) {
             cudaGraph_t graph;
-            // the descriptor upload and the six kernels; the resampling kernel stores the
-            // frame's status word into mapped host memory, so no copy follows the kernels
+            // the six kernels; the resampling kernel stores the frame's status word into
+            // mapped host memory, so no copy follows them
             DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-            e = upload_batch(c, nb);
-            if (e == cudaSuccess) e = frame_kernels(c, false, false);
+            e = frame_kernels(c, false, false);
             cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
             if (e != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
             if (e2 != cudaSuccess) return fail(DOGM_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
@@ -389,7 +410,7 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
             DOGM_CUDA(cudaMemcpyAsync(hc.dst, hc.src, hc.bytes, cudaMemcpyDeviceToHost, c.stream));
     DOGM_CUDA(cudaEventRecord(c.done[c.cur], c.stream));
     c.pending[c.cur] = true;
-    c.cur ^= 1;
+    set_mirror(c, c.cur ^ 1);
     return DOGM_OK;
 }
 
@@ -489,7 +510,7 @@ size_t dogm_state_bytes(const dogm_params* p) {
     b += C * (sizeof(dogm_grid_cell) + sizeof(dogm_measurement_cell) + 2 * 4 + 8 + 4);
     b += (size_t)s.sort_tiles * (size_t)((s.cell_tiles + 3) & ~3) * 4;  // per-tile bucket counts
     b += (size_t)s.cell_tiles * (16 + 12) + 4 + (size_t)s.res_tiles * 8;
-    b += sizeof(Batch);
+    b += 2 * sizeof(Batch);  // the launch context's device batch of each mirror
     return b;
 }
 
@@ -1579,8 +1600,8 @@ dogm_status slot_launch(BatchSlot* s, const SlotFrame* fr, int n) {
 }
 
 // Captures and instantiates the steady-state graph of every batch-size bucket up to max_n for
-// both mirrors, without launching it: a graph records the launches on the slot's device batch
-// and the copies from its pinned mirrors, none of which depends on the handles of a frame.
+// both mirrors, without launching it: a graph records the kernel launches on the mirror's
+// device batch, which depend on none of the handles of a frame.
 dogm_status slot_prewarm(BatchSlot* s, int max_n) {
     if (!s) return fail(DOGM_ERR_INVALID_ARGUMENT, "slot is NULL");
     Ctx& c = s->ctx;
@@ -1591,13 +1612,12 @@ dogm_status slot_prewarm(BatchSlot* s, int max_n) {
             c.scatter_ctiles = 2048;  // streams of the serving loop have at most 2048 cell tiles
             const int key = graph_key(nb, m, c.scatter_ctiles, c.res_bits);
             if (c.graphs.count(key)) continue;
-            c.cur = m;
+            set_mirror(c, m);
             cudaGraph_t graph;
             DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-            cudaError_t e = upload_batch(c, nb);
-            if (e == cudaSuccess) e = frame_kernels(c, false, false);
+            cudaError_t e = frame_kernels(c, false, false);
             cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
-            c.cur = cur;
+            set_mirror(c, cur);
             if (e != cudaSuccess || e2 != cudaSuccess)
                 return fail(DOGM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e != cudaSuccess ? e : e2));
             cudaGraphExec_t exec;
@@ -1607,7 +1627,7 @@ dogm_status slot_prewarm(BatchSlot* s, int max_n) {
             c.graphs.emplace(key, exec);
         }
     }
-    c.cur = cur;
+    set_mirror(c, cur);
     return DOGM_OK;
 }
 
