@@ -472,10 +472,10 @@ def _stream_pool(dogm, scene, n: int, seed: int, pinned: bool):
 
 def run_batched(dogm, scene, n_streams: int = 64, rounds: int = 30, warm: int = 3) -> dict:
     """Batched uneven grids: n_streams independent grids updated per frame by one launch per
-    stage (dogm_update_batch, CUDA graph) against two per-stream baselines: one dogm_update per
-    grid on its own CUDA stream as a CUDA graph launch with no host wait between grids (the
-    strongest per-stream form), and per-stream plain launches (every kernel launched one by one,
-    each update waited for, as the reference's updateGrid).  Measurement grids resident in HBM;
+    stage (dogm_update_batch, CUDA graph) against per-stream baselines: one dogm_update per grid
+    on its own CUDA stream with no host wait between grids, as a CUDA graph launch and as chained
+    launches (the default launch mode), and per-stream plain launches (every kernel launched one
+    by one, each update waited for, as the reference's updateGrid).  Measurement grids resident in HBM;
     host wall clock over `rounds` frames of all grids (synchronised at both ends)."""
     params, cells, bufs, _ = _stream_pool(dogm, scene, n_streams, seed=2, pinned=False)
     grids = [dogm.DOGM(p, seed=1000 + i, stream_id=i, sync_each_update=False) for i, p in enumerate(params)]
@@ -486,7 +486,7 @@ def run_batched(dogm, scene, n_streams: int = 64, rounds: int = 30, warm: int = 
         dogm.update_batch(grids, [bufs[i][r % 2].ptr for i in range(n_streams)], zeros, zeros, zeros, dts,
                           device=True)
 
-    def per_stream_graph(r):
+    def per_stream_graph(r):  # also the chained form: the same calls in another launch mode
         for i, g in enumerate(grids):
             g.update_grid(bufs[i][r % 2].ptr, 0.0, 0.0, 0.0, 0.1, device=True)
 
@@ -501,9 +501,9 @@ def run_batched(dogm, scene, n_streams: int = 64, rounds: int = 30, warm: int = 
 
     out = {}
     for name, step in (("batched", batched), ("per_stream_graph", per_stream_graph),
-                       ("per_stream_plain", per_stream_plain)):
+                       ("per_stream_chained", per_stream_graph), ("per_stream_plain", per_stream_plain)):
         for g in grids:
-            g.set_launch_mode(plain=(name == "per_stream_plain"))
+            g.set_launch_mode(plain=(name == "per_stream_plain"), graph=(name == "per_stream_graph"))
         for r in range(warm):
             step(r)
         sync()
@@ -526,6 +526,8 @@ def run_batched(dogm, scene, n_streams: int = 64, rounds: int = 30, warm: int = 
     gbs = alg * out["batched"] / n_streams / 1e9
     return {"frames_per_s": round(out["batched"], 1),
             "per_stream_graph_frames_per_s": round(out["per_stream_graph"], 1),
+            "per_stream_chained_frames_per_s": round(out["per_stream_chained"], 1),
+            "speedup_vs_per_stream_chained": round(out["batched"] / out["per_stream_chained"], 2),
             "per_stream_plain_frames_per_s": round(out["per_stream_plain"], 1),
             "speedup_vs_per_stream_graph": round(out["batched"] / out["per_stream_graph"], 2),
             "speedup_vs_per_stream_plain": round(out["batched"] / out["per_stream_plain"], 2),

@@ -103,6 +103,7 @@ class Tune(C.Structure):
 
 
 SERVE_BATCHED, SERVE_PER_STREAM, SERVE_PER_STREAM_PLAIN = 0, 1, 2
+LAUNCH_CHAINED, LAUNCH_PLAIN, LAUNCH_GRAPH = 0, 1, 2
 STREAM_WAITING, STREAM_ACTIVE, STREAM_CLOSED = 0, 1, 2
 
 
@@ -343,9 +344,11 @@ class DOGM:
     def get_iteration(self) -> int:
         return load().dogm_get_iteration(self.h)
 
-    def set_launch_mode(self, plain: bool) -> None:
-        """Plain kernel launches per update (as the reference) instead of a CUDA graph."""
-        check(load().dogm_set_launch_mode(self.h, 1 if plain else 0), "dogm_set_launch_mode")
+    def set_launch_mode(self, plain: bool = False, graph: bool = False) -> None:
+        """Plain kernel launches per update (as the reference), one CUDA graph per update, or
+        (neither: the default) chained launches with nothing between two updates."""
+        check(load().dogm_set_launch_mode(self.h, LAUNCH_PLAIN if plain else (LAUNCH_GRAPH if graph else LAUNCH_CHAINED)),
+              "dogm_set_launch_mode")
 
     def last_launch_count(self) -> int:
         return load().dogm_last_launch_count(self.h)

@@ -147,6 +147,16 @@ struct Batch {
     GridDesc g[kMaxBatch];
 };
 
+// One grid's frame passed to predict as a kernel parameter instead of through an upload of the
+// device batch: predict reads it from its parameters and writes the device batch for the later
+// kernels (valid = 0: the kernel reads the device batch as uploaded).
+struct FrameParam {
+    GridDesc g;
+    int tiles[kNumStages];
+    unsigned int* status_host;
+    int valid;
+};
+
 // ---- kernel launchers (defined in the .cu files) ---------------------------------------
 struct LaunchCfg {
     int num_sms;
@@ -187,7 +197,7 @@ cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg);
 // stage_mode 0: the update's predict (ego shift, motion, bucket counts, per-frame sums zeroed);
 // 1: the particlePrediction stage call (motion only); 2: the particleAssignment stage call
 // (bucket counts of the resident keys and per-frame sums zeroed, no motion)
-cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg);
+cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg, const FrameParam* fp = nullptr);
 // bucket offsets (column scan of the per-tile bucket counts) and the stable bucket scatter;
 // max_ctiles: the largest bucket count of the batch's grids (sizes the scatter's shared memory)
 cudaError_t launch_sort_scan(const Batch* d_batch, const LaunchCfg& cfg);

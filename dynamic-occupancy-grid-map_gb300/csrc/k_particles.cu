@@ -43,18 +43,17 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
 constexpr int kPredictThreads = 512;
 static_assert(kPredictTile % kPredictThreads == 0, "whole particles per thread");
 
-__global__ void __launch_bounds__(kPredictThreads, 3) k_predict(Batch* __restrict__ bt, int mode) {
-    grid_dependency_begin();
-    __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (bucket of the sort)
-    const int total = batch_total(bt, kStPredict);
+template <class View>
+__device__ __forceinline__ void predict_body(const View& v, int mode, uint32_t* h2) {
+    const int total = v.total(kStPredict);
     const bool counts = mode != 1;
     if (counts) {
         // this frame's exact sums start at zero: the cell and newborn passes add into them
         // after this kernel, and the last reader (the previous frame's resampling) is done
         const int stride = gridDim.x * blockDim.x;
         const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-        for (int gi = 0; gi < bt->n_grids; ++gi) {
-            const GridDesc& g = bt->g[gi];
+        for (int gi = 0; gi < v.n(); ++gi) {
+            const GridDesc& g = v.g(gi);
             for (int i = tid; i < g.tiles[kStResample]; i += stride) g.res_sum[i] = 0ull;
                 if (tid == 0) {
                 g.fs->status = 0u;
@@ -65,9 +64,9 @@ __global__ void __launch_bounds__(kPredictThreads, 3) k_predict(Batch* __restric
     }
     const int lane = threadIdx.x & 31;
     for (int t = blockIdx.x; t < total; t += gridDim.x) {
-        const int gi = grid_of_tile(bt, kStPredict, t);
-        const GridDesc& g = bt->g[gi];
-        const int lt = t - bt->prefix[gi][kStPredict];
+        const int gi = v.grid(kStPredict, t);
+        const GridDesc& g = v.g(gi);
+        const int lt = t - v.first(gi, kStPredict);
         if (counts) {
             for (int i = threadIdx.x; i < g.ctiles; i += kPredictThreads) h2[i] = 0u;
             __syncthreads();
@@ -134,6 +133,57 @@ __global__ void __launch_bounds__(kPredictThreads, 3) k_predict(Batch* __restric
             }
             __syncthreads();
         }
+    }
+}
+
+
+// The frame's descriptors as the device batch holds them, or as one grid's kernel parameter.
+struct BatchView {
+    const Batch* b;
+    __device__ int n() const { return b->n_grids; }
+    __device__ int total(int s) const { return batch_total(b, s); }
+    __device__ int grid(int s, int t) const { return grid_of_tile(b, s, t); }
+    __device__ int first(int gi, int s) const { return b->prefix[gi][s]; }
+    __device__ const GridDesc& g(int gi) const { return b->g[gi]; }
+};
+struct ParamView {
+    const FrameParam* p;
+    __device__ int n() const { return 1; }
+    __device__ int total(int s) const { return p->tiles[s]; }
+    __device__ int grid(int, int) const { return 0; }
+    __device__ int first(int, int) const { return 0; }
+    __device__ const GridDesc& g(int) const { return p->g; }
+};
+
+// Writes a one-grid frame from predict's parameter into the device batch, for the kernels after
+// predict (they wait for predict to finish before reading it).  Block 0, after the wait for the
+// previous kernel, so no earlier kernel still reads the batch.
+__device__ void publish_frame(Batch* bt, const FrameParam& fp) {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&fp.g);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&bt->g[0]);
+    static_assert(sizeof(GridDesc) % 4 == 0, "descriptor copied in words");
+    for (int i = threadIdx.x; i < (int)(sizeof(GridDesc) / 4); i += blockDim.x) dst[i] = src[i];
+    if (threadIdx.x < kNumStages) {
+        bt->counters[threadIdx.x] = 0u;
+        bt->prefix[0][threadIdx.x] = 0;
+        bt->prefix[1][threadIdx.x] = fp.tiles[threadIdx.x];
+    }
+    if (threadIdx.x == 0) {
+        bt->n_grids = 1;
+        bt->status = 0u;
+        bt->status_host = fp.status_host;
+    }
+}
+
+__global__ void __launch_bounds__(kPredictThreads, 3) k_predict(Batch* __restrict__ bt, int mode,
+                                                             const __grid_constant__ FrameParam fp) {
+    grid_dependency_begin();
+    __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (bucket of the sort)
+    if (fp.valid) {
+        if (blockIdx.x == 0) publish_frame(bt, fp);
+        predict_body(ParamView{&fp}, mode, h2);
+    } else {
+        predict_body(BatchView{bt}, mode, h2);
     }
 }
 
@@ -299,9 +349,10 @@ cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCf
     return cudaGetLastError();
 }
 
-cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg) {
-    k_predict<<<launch_blocks(cfg, 3), kPredictThreads, 0, cfg.stream>>>(const_cast<Batch*>(d_batch), stage_mode);
-    return cudaGetLastError();
+cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg, const FrameParam* fp) {
+    FrameParam none{};
+    return launch_kernel(cfg, k_predict, launch_blocks(cfg, 3), kPredictThreads, 0, const_cast<Batch*>(d_batch),
+                         stage_mode, fp ? *fp : none);
 }
 
 cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg) {

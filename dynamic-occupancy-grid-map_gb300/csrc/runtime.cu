@@ -68,13 +68,20 @@ struct Ctx {
     // programmatic dependent launch between the frame's kernels (environment DOGM_PDL=0 turns
     // it off, for comparison)
     bool pdl = true;
-    // steady-state frames as CUDA graph launches (dogm_set_launch_mode; plain launches otherwise)
-    bool use_graphs = true;
+    // how steady-state frames are launched (dogm_set_launch_mode): chained (one grid of a
+    // handle's own context; otherwise a graph), a CUDA graph, or plain launches
+    int launch_mode = DOGM_LAUNCH_CHAINED;
     // bucket-count class of the batch being built: the bucket scatter's shared memory is sized
     // for 2048 buckets, or 4096 when a grid of the batch has more than 2048 cell tiles
     int scatter_ctiles = 2048;
     // resampling tile of this context's launches: 2^res_bits joint particles
     int res_bits = kResBitsDefault;
+    // a handle's own context: a steady-state frame of its one grid runs chained (no graph, no
+    // upload, no event between frames; predict takes the descriptor as a parameter and follows
+    // the previous frame's resampling programmatically).  Launch slots and the batch context
+    // keep graphs, since their callers wait on the frames' events.
+    bool chain = false;
+    bool last_chained = false;  // the last frame queued ran chained
 
     // Captured graphs hold the launch widths: drop them when the widths change.
     void drop_graphs() {
@@ -315,7 +322,9 @@ cudaError_t download_status(Ctx& c) {
 
 // The steady-state frame: 6 kernels; with profiling, a CUDA event before each stage and at the
 // end.
-cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
+// fp: a chained frame's descriptor (predict then follows the previous frame's resampling
+// programmatically too).
+cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin, const FrameParam* fp = nullptr) {
     LaunchCfg cfg{c.num_sms, c.stream};
     const bool prof = c.profile && !with_init;
     cudaError_t e;
@@ -323,14 +332,14 @@ cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin) {
     do {                                                                            \
         if (prof && (e = cudaEventRecord(c.ev[i], c.stream)) != cudaSuccess) return e; \
         cfg.mult = c.mult[i];                                                       \
-        cfg.pdl = c.pdl && !prof && i > 0; /* predict follows the batch upload */   \
+        cfg.pdl = c.pdl && !prof && (i > 0 || fp); /* else predict follows the upload */ \
         if ((e = (call)) != cudaSuccess) return e;                                  \
     } while (0)
     // the per-frame counters are reset by predict and the cell pass of the previous frame; a
     // full reset runs only on a grid's first frame or after a failed frame
     if ((with_begin || with_init) && (e = launch_frame_begin(c.d_batch, 0, cfg)) != cudaSuccess) return e;
     if (with_init && (e = launch_init_particles(c.d_batch, cfg)) != cudaSuccess) return e;
-    STAGE(0, launch_predict(c.d_batch, 0, cfg));
+    STAGE(0, launch_predict(c.d_batch, 0, cfg, fp));
     STAGE(1, launch_sort_scan(c.d_batch, cfg));
     STAGE(2, launch_sort_scatter(c.d_batch, c.scatter_ctiles, cfg));
     STAGE(3, launch_cells(c.d_batch, cfg));
@@ -367,8 +376,25 @@ struct HostCopy {
 dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launches,
                       const std::vector<HostCopy>* after = nullptr) {
     cudaError_t e;
-    const bool plain = any_init || any_clear || c.profile || !c.use_graphs;
-    if (plain) {
+    const bool plain = any_init || any_clear || c.profile || c.launch_mode == DOGM_LAUNCH_PLAIN;
+    const bool chained = !plain && n == 1 && c.chain && c.pdl && c.launch_mode == DOGM_LAUNCH_CHAINED;
+    if (!chained && c.last_chained) {
+        // chained frames record no completion event: let them finish before a frame that
+        // relies on the mirrors' events and uploads into the device batches
+        DOGM_CUDA(cudaStreamSynchronize(c.stream));
+        c.last_chained = false;
+    }
+    if (chained) {
+        const Batch& hb = *c.h_batch[c.cur];
+        FrameParam fp{};
+        fp.g = hb.g[0];
+        for (int s = 0; s < kNumStages; ++s) fp.tiles[s] = hb.prefix[1][s];
+        fp.status_host = hb.status_host;
+        fp.valid = 1;
+        DOGM_CUDA(frame_kernels(c, false, false, &fp));
+        *launches = kLaunchesPerFrame;
+        c.last_chained = true;
+    } else if (plain) {
         // first frame of some grid (init runs between begin and predict), a frame after a
         // failed one (full counter reset first) or per-stage timing
         DOGM_CUDA(upload_batch(c, n));
@@ -408,8 +434,10 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
     if (after)
         for (const HostCopy& hc : *after)
             DOGM_CUDA(cudaMemcpyAsync(hc.dst, hc.src, hc.bytes, cudaMemcpyDeviceToHost, c.stream));
-    DOGM_CUDA(cudaEventRecord(c.done[c.cur], c.stream));
-    c.pending[c.cur] = true;
+    if (!chained) {  // a chained frame's parameters were copied at launch: its mirror is free
+        DOGM_CUDA(cudaEventRecord(c.done[c.cur], c.stream));
+        c.pending[c.cur] = true;
+    }
     set_mirror(c, c.cur ^ 1);
     return DOGM_OK;
 }
@@ -528,6 +556,7 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     h->gs = s.gs; h->N = s.N; h->B = s.B; h->C = s.C;
     auto cleanup = [&](dogm_status s2) { dogm_destroy(h); return s2; };
     if ((st = ctx_init(h->ctx, h->device)) != DOGM_OK) return cleanup(st);
+    h->ctx.chain = true;
     if (prepare_kernels() != cudaSuccess || prepare_cells() != cudaSuccess || prepare_sort() != cudaSuccess)
         return cleanup(fail(DOGM_ERR_CUDA, "kernel attribute setup failed"));
 
@@ -824,9 +853,9 @@ int dogm_get_new_born_particle_count(const dogm_handle* h) { return h ? h->B : 0
 int dogm_last_launch_count(const dogm_handle* h) { return h ? h->last_launches : 0; }
 
 dogm_status dogm_set_launch_mode(dogm_handle* h, int mode) {
-    if (!h || (mode != DOGM_LAUNCH_GRAPH && mode != DOGM_LAUNCH_PLAIN))
+    if (!h || (mode != DOGM_LAUNCH_CHAINED && mode != DOGM_LAUNCH_GRAPH && mode != DOGM_LAUNCH_PLAIN))
         return fail(DOGM_ERR_INVALID_ARGUMENT, "bad handle or launch mode");
-    h->ctx.use_graphs = mode == DOGM_LAUNCH_GRAPH;
+    h->ctx.launch_mode = mode;
     return DOGM_OK;
 }
 

@@ -294,7 +294,7 @@ size_t dogm_state_bytes(const dogm_params* params);
 typedef enum dogm_serve_mode {
     DOGM_SERVE_BATCHED = 0,    /* continuous batching over launch slots                      */
     DOGM_SERVE_PER_STREAM = 1, /* one dogm_update per frame on the stream's own CUDA stream,
-                                  a CUDA graph launch, frames of several streams in flight    */
+                                  chained launches, frames of several streams in flight      */
     DOGM_SERVE_PER_STREAM_PLAIN = 2 /* one dogm_update per frame with plain kernel launches,
                                   each waited for before the next frame starts (the
                                   reference's synchronous updateGrid, dogm/src/dogm.cu:115-131) */
@@ -583,10 +583,19 @@ dogm_status dogm_autotune(dogm_handle* h, const dogm_measurement_cell* meas, int
 int dogm_last_launch_count(const dogm_handle* h);
 
 /* How a handle's steady-state updates are launched (no counterpart in the reference, whose
- * updateGrid issues every kernel itself): DOGM_LAUNCH_GRAPH (default) replays one captured CUDA
- * graph per update; DOGM_LAUNCH_PLAIN issues the kernels one by one, as the reference does.  The
- * results are the same bits either way. */
-typedef enum dogm_launch_mode { DOGM_LAUNCH_GRAPH = 0, DOGM_LAUNCH_PLAIN = 1 } dogm_launch_mode;
+ * updateGrid issues every kernel itself).  DOGM_LAUNCH_CHAINED (the default): the six kernels
+ * are launched one after another, each programmatically dependent on the one before it (the
+ * first on the previous update's last), with the update's descriptor passed to the first
+ * kernel as a parameter, so nothing else runs on the stream between two updates.
+ * DOGM_LAUNCH_GRAPH: one captured CUDA graph per update, its descriptor uploaded on a second
+ * stream (the form a batch's update and the serving loop's launch slots always take).
+ * DOGM_LAUNCH_PLAIN: the kernels one by one, the descriptor copied up before them and the
+ * status back after, as the reference does.  The results are the same bits in every mode. */
+typedef enum dogm_launch_mode {
+    DOGM_LAUNCH_CHAINED = 0,
+    DOGM_LAUNCH_PLAIN = 1,
+    DOGM_LAUNCH_GRAPH = 2
+} dogm_launch_mode;
 dogm_status dogm_set_launch_mode(dogm_handle* h, int mode);
 const char* dogm_last_error(void);
 const char* dogm_status_string(dogm_status s);
