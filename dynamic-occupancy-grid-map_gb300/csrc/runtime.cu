@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 
+#include <unistd.h>
+
 #include "dogm_internal.h"
 
 using namespace dogm_gb300;
@@ -194,6 +196,21 @@ dogm_status dalloc(dogm_handle* h, T** p, size_t count) {
     *p = static_cast<T*>(q);
     return DOGM_OK;
 }
+
+// A handle's frame buffers are carved from one allocation: a first pass over the buffer list
+// sums their sizes, a second assigns the pointers.  One mapping per grid keeps its buffers
+// together whatever earlier handles of the process allocated and freed.
+constexpr size_t kCarveAlign = 256;
+struct Carver {
+    unsigned char* base = nullptr;  // null: sizing pass
+    size_t off = 0;
+    template <class T>
+    void take(T** p, size_t count) {
+        off = (off + kCarveAlign - 1) & ~(kCarveAlign - 1);
+        if (base) *p = reinterpret_cast<T*>(base + off);
+        off += std::max<size_t>(count, 1) * sizeof(T);
+    }
+};
 
 struct Sizes {
     int gs, N, B, C, key_bits, sort_tiles, cell_tiles, res_tiles, pred_tiles, scan;
@@ -577,26 +594,35 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
     g.seed_hi = (uint32_t)(h->opt.seed >> 32);
     set_tiles(g, s);
 
-#define ALLOC(ptr, n) if ((st = dalloc(h, &(ptr), (n))) != DOGM_OK) return cleanup(st)
-    ALLOC(g.P_state, s.N); ALLOC(g.P_key, s.N);
-    ALLOC(g.T_state, s.N); ALLOC(g.T_key, s.N);
-    ALLOC(g.S_state, s.N); ALLOC(g.S_key, s.N);
-    ALLOC(g.B_state, s.B); ALLOC(g.B_key, s.B); ALLOC(g.B_w, s.B);
-    ALLOC(g.cells, s.C);
     dogm_measurement_cell* meas_own = nullptr;
-    ALLOC(meas_own, s.C);
+    float* fa = nullptr; float* fb = nullptr;
+    auto carve = [&](Carver& cv) {
+        cv.take(&g.P_state, s.N); cv.take(&g.P_key, s.N);
+        cv.take(&g.T_state, s.N); cv.take(&g.T_key, s.N);
+        cv.take(&g.S_state, s.N); cv.take(&g.S_key, s.N);
+        cv.take(&g.B_state, s.B); cv.take(&g.B_key, s.B); cv.take(&g.B_w, s.B);
+        cv.take(&g.cells, s.C);
+        cv.take(&meas_own, s.C);
+        cv.take(&fa, s.C); cv.take(&fb, s.C);
+        cv.take(&g.rho_b, s.C); cv.take(&g.w_cell, s.C);
+        cv.take(&g.hsort, (size_t)s.sort_tiles * g.bucket_stride);
+        cv.take(&g.ctile_cnt, s.cell_tiles); cv.take(&g.ctile_job, s.cell_tiles);
+        cv.take(&g.cell_sum, 2 * (size_t)s.cell_tiles);
+        cv.take(&g.res_sum, s.res_tiles);
+        cv.take(&g.fs, 1);
+    };
+    {
+        Carver sizing;
+        carve(sizing);
+        unsigned char* arena = nullptr;  // zeroed, freed with the handle's allocations
+        if ((st = dalloc(h, &arena, sizing.off)) != DOGM_OK) return cleanup(st);
+        Carver cv;
+        cv.base = arena;
+        carve(cv);
+    }
     g.meas_own = meas_own;
     g.meas_src = meas_own;
-    float* fa = nullptr; float* fb = nullptr;
-    ALLOC(fa, s.C); ALLOC(fb, s.C);
     g.free_old = fa; g.free_new = fb;
-    ALLOC(g.rho_b, s.C); ALLOC(g.w_cell, s.C);
-    ALLOC(g.hsort, (size_t)s.sort_tiles * g.bucket_stride);
-    ALLOC(g.ctile_cnt, s.cell_tiles); ALLOC(g.ctile_job, s.cell_tiles);
-    ALLOC(g.cell_sum, 2 * (size_t)s.cell_tiles);
-    ALLOC(g.res_sum, s.res_tiles);
-    ALLOC(g.fs, 1);
-#undef ALLOC
     // measurement cells start as in initGridCellsKernel (init.cu:65-80): no evidence,
     // likelihood 1, p_A 1; cells start with zero masses and empty ranges.
     {
@@ -650,6 +676,23 @@ static dogm_status wait_readback(dogm_handle* h, cudaStream_t stream) {
     return DOGM_OK;
 }
 
+// Host pages that a copy engine reads: on the Grace host of a GB300, host-to-device copies from
+// pinned pages that the CPU has not accessed for some seconds slow down the longer the pages stay
+// untouched (from 160 to 16 GB/s over 40 s, pages copied every 3 s), while pages that the CPU read
+// or wrote just before copy at full speed.  The calling thread therefore reads one byte of every
+// page of a host measurement grid before its copy is queued: a few microseconds per grid.
+static void touch_host_pages(const void* p, size_t bytes) {
+    static const size_t page = [] {
+        const long s = sysconf(_SC_PAGESIZE);
+        return s >= 4096 ? (size_t)s : (size_t)4096;
+    }();
+    const volatile unsigned char* b = static_cast<const volatile unsigned char*>(p);
+    unsigned int acc = 0;
+    for (size_t o = 0; o < bytes; o += page) acc += b[o];
+    if (bytes) acc += b[bytes - 1];
+    (void)acc;
+}
+
 static dogm_status prepare_measurement(dogm_handle* h, const dogm_measurement_cell* meas, int device,
                                        cudaStream_t stream, const dogm_measurement_cell** src, int* copy) {
     *src = h->desc.meas_own;
@@ -660,6 +703,7 @@ static dogm_status prepare_measurement(dogm_handle* h, const dogm_measurement_ce
         *copy = 1;
         return DOGM_OK;
     }
+    touch_host_pages(meas, sizeof(dogm_measurement_cell) * (size_t)h->C);
     DOGM_CUDA(cudaMemcpyAsync(h->desc.meas_own, meas, sizeof(dogm_measurement_cell) * (size_t)h->C,
                               cudaMemcpyHostToDevice, stream));
     return DOGM_OK;

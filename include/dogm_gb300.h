@@ -289,7 +289,8 @@ size_t dogm_state_bytes(const dogm_params* params);
  * others run join the next launch and launches overlap on the device.  Each frame's result is
  * bit-identical to updating its stream alone with dogm_update (same handle, same frames).
  * DOGM_SERVE_PER_STREAM instead updates every frame on its own with dogm_update on the
- * stream's own CUDA stream (the plain-launch comparison).  All calls are thread-safe. */
+ * stream's own CUDA stream, and DOGM_SERVE_PER_STREAM_PLAIN also waits for each frame before
+ * the next (the two per-stream comparisons).  All calls are thread-safe. */
 
 typedef enum dogm_serve_mode {
     DOGM_SERVE_BATCHED = 0,    /* continuous batching over launch slots                      */
