@@ -95,28 +95,33 @@ constexpr int kBucketIpt = 8;  // bucket particles per thread in a chunk of the 
 constexpr int kBucketChunk = kCellThreads * kBucketIpt;
 static_assert(kCellTile == 2 * kCellThreads && kBucketChunk < 65536, "one pair of 16-bit cell counts per thread");
 
+// Records a warp stages at a time in B (half of its 32 cells): the staging area then fits in the
+// space the sort's counts use, and two blocks of the pass leave the SM the larger L1 split.
+constexpr int kStageRecs = 16;
+
 struct CellSmem {
     dogm_measurement_cell meas[kCellTile];  // prefetched (cp.async) while S and A run
     float free_prev[kCellTile];             // previous free mass, ego shift applied
-    int start[kCellTile];   // sorted position of the first particle (-1: none)
-    int end[kCellTile];     // sorted position of the last particle
-    int n_in[kCellTile];    // in-grid particles
     union {
-        struct {            // A and B: per-cell sums
+        // S: per-warp particle counts per cell in the current chunk, then offsets across warps
+        uint16_t whist[kCellWarps][kCellTile];
+        struct {            // A and B: each occupied cell's range, in-grid count and sums
+            int start[kCellTile];   // sorted position of the first particle
+            int end[kCellTile];     // sorted position of the last particle
+            int n_in[kCellTile];    // in-grid particles
             float vx[kCellTile], vy[kCellTile], vxx[kCellTile], vyy[kCellTile], vxy[kCellTile];
-        } sum;
+        } cell;
+    } u1;
+    union {
         struct {            // S: particles per cell, then running offsets (two chunks in turn)
             uint32_t cnt[kCellTile];
             uint32_t off[2][kCellTile];
         } srt;
-    } u1;
-    union {
-        // B, per warp: its 32 cell records (2 KB), staged so that the warp stores them as 512
-        // contiguous bytes per instruction instead of four 16-byte pieces at 64-byte stride
-        float4 stage[kCellWarps][32 * 4];
-        // S: per-warp particle counts per cell in the current chunk, then offsets across warps
-        uint16_t whist[kCellWarps][kCellTile];
+        // B, per warp: kStageRecs of its cell records, staged so that the warp stores them as
+        // 512 contiguous bytes per instruction instead of four 16-byte pieces at 64-byte stride
+        float4 stage[kCellWarps][kStageRecs * 4];
     } u2;
+    uint8_t occ[kCellTile];  // cell holds particles (from the sort's counts; read by its B thread)
     int scan[kCellWarps];
     Run wagg[kCellThreads / 32];  // each warp's run, then (wpre) the runs before each warp
     Run wpre[kCellThreads / 32];
@@ -127,11 +132,12 @@ struct CellSmem {
 };
 static_assert(offsetof(CellSmem, meas) % 16 == 0, "16-byte cp.async destination");
 static_assert(offsetof(CellSmem, u2) % 16 == 0, "16-byte staged records");
+static_assert(sizeof(CellSmem) <= 80 * 1024, "two blocks per SM within the 164 KB shared-memory split");
 static_assert(offsetof(CellSmem, job) % 16 == 0, "16-byte cp.async destination");
 static_assert(sizeof(dogm_grid_cell) == 64, "a record is four float4");
 
-// Record chunk j of lane l is staged at float4 slot 4 l + (j ^ ((l >> 1) & 3)): for each j the
-// eight lanes of a 128-byte shared-memory wavefront hit eight distinct 16-byte bank groups, and
+// Record chunk j of record l is staged at float4 slot 4 l + (j ^ ((l >> 1) & 3)): for each j the
+// eight records of a 128-byte shared-memory wavefront hit eight distinct 16-byte bank groups, and
 // reading record r's chunk c back from slot 4 r + (c ^ ((r >> 1) & 3)) gives lanes 4 q .. 4 q + 3
 // one whole record, again without conflicts.
 __device__ __forceinline__ int stage_slot(int rec, int chunk) { return rec * 4 + (chunk ^ ((rec >> 1) & 3)); }
@@ -164,13 +170,13 @@ __device__ __forceinline__ void put_cell(CellSmem& sm, const GridDesc& g, uint32
         flag_status(g, kStatusBounds);
         return;
     }
-    sm.end[cl] = last;
-    sm.n_in[cl] = (int)(r.fn & ~kRunHead);
-    sm.u1.sum.vx[cl] = r.vx;
-    sm.u1.sum.vy[cl] = r.vy;
-    sm.u1.sum.vxx[cl] = r.vxx;
-    sm.u1.sum.vyy[cl] = r.vyy;
-    sm.u1.sum.vxy[cl] = r.vxy;
+    sm.u1.cell.end[cl] = last;
+    sm.u1.cell.n_in[cl] = (int)(r.fn & ~kRunHead);
+    sm.u1.cell.vx[cl] = r.vx;
+    sm.u1.cell.vy[cl] = r.vy;
+    sm.u1.cell.vxx[cl] = r.vxx;
+    sm.u1.cell.vyy[cl] = r.vyy;
+    sm.u1.cell.vxy[cl] = r.vxy;
 }
 
 // S: the stable counting sort of one bucket (bucketed positions [p0, p1) of T, whose cells lie
@@ -207,8 +213,8 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
         }
     };
     auto zero_whist = [&]() {
-        uint4* wz = reinterpret_cast<uint4*>(&sm.u2.whist[0][0]);
-        for (int i = threadIdx.x; i < (int)(sizeof(sm.u2.whist) / sizeof(uint4)); i += kCellThreads)
+        uint4* wz = reinterpret_cast<uint4*>(&sm.u1.whist[0][0]);
+        for (int i = threadIdx.x; i < (int)(sizeof(sm.u1.whist) / sizeof(uint4)); i += kCellThreads)
             wz[i] = make_uint4(0u, 0u, 0u, 0u);
     };
     // warp ranks of the loaded chunk: rank[k] = earlier same-cell particles of the warp
@@ -219,10 +225,10 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
             const uint32_t d = cell_of(key[k]);
             const uint32_t peers = __match_any_sync(0xffffffffu, d);
             uint16_t before = 0;
-            if (d != 0xffffffffu) before = sm.u2.whist[warp][d];
+            if (d != 0xffffffffu) before = sm.u1.whist[warp][d];
             rank[k] = (uint16_t)(before + __popc(peers & lt_mask));
             __syncwarp();
-            if (d != 0xffffffffu && lane == __ffs(peers) - 1) sm.u2.whist[warp][d] = (uint16_t)(before + __popc(peers));
+            if (d != 0xffffffffu && lane == __ffs(peers) - 1) sm.u1.whist[warp][d] = (uint16_t)(before + __popc(peers));
             __syncwarp();
         }
     };
@@ -233,7 +239,7 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
         uint32_t v[kPer], s = 0u;
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
-            v[j] = sm.u1.srt.cnt[c0 + j];
+            v[j] = sm.u2.srt.cnt[c0 + j];
             s += v[j];
         }
         uint32_t x = s;
@@ -248,7 +254,7 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
         for (int w = 0; w < warp; ++w) e += (uint32_t)sm.scan[w];
 #pragma unroll
         for (int j = 0; j < kPer; ++j) {
-            sm.u1.srt.off[0][c0 + j] = e;
+            sm.u2.srt.off[0][c0 + j] = e;
             e += v[j];
         }
     };
@@ -269,7 +275,7 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
                 const uint32_t c = cell_of(key[k]);
                 out[j] = -1;
                 if (k < R && c != 0xffffffffu)
-                    out[j] = p0 + (int)(sm.u1.srt.off[cur][c] + sm.u2.whist[warp][c] + rank[k]);
+                    out[j] = p0 + (int)(sm.u2.srt.off[cur][c] + sm.u1.whist[warp][c] + rank[k]);
                 st[j] = __ldcs(g.T_state + ((k < R && i < p1) ? i : p1 - 1));
             }
 #pragma unroll
@@ -299,7 +305,7 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
         __syncthreads();
         {
             // two cells per 32-bit word: the halves never carry (a chunk holds <= 4096)
-            uint32_t* wh = reinterpret_cast<uint32_t*>(&sm.u2.whist[0][0]);
+            uint32_t* wh = reinterpret_cast<uint32_t*>(&sm.u1.whist[0][0]);
             const int cp = threadIdx.x;  // cells 2 cp, 2 cp + 1
             uint32_t acc = 0u;
 #pragma unroll
@@ -308,8 +314,8 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
                 wh[w * (kCellTile / 2) + cp] = acc;
                 acc += n;
             }
-            sm.u1.srt.cnt[2 * cp] = acc & 0xffffu;
-            sm.u1.srt.cnt[2 * cp + 1] = acc >> 16;
+            sm.u2.srt.cnt[2 * cp] = acc & 0xffffu;
+            sm.u2.srt.cnt[2 * cp + 1] = acc >> 16;
         }
         __syncthreads();
         scan_counts();
@@ -320,7 +326,7 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
     }
 
     // several chunks: particles per cell over the whole bucket first
-    for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) sm.u1.srt.cnt[c] = 0u;
+    for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) sm.u2.srt.cnt[c] = 0u;
     __syncthreads();
     for (int c0 = p0; c0 < p1; c0 += kBucketChunk) {
         const int R = chunk_rounds(min(kBucketChunk, p1 - c0));
@@ -330,7 +336,7 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
             if (k >= R) break;  // block-uniform
             const uint32_t d = cell_of(key[k]);
             const uint32_t peers = __match_any_sync(0xffffffffu, d);
-            if (d != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&sm.u1.srt.cnt[d], (uint32_t)__popc(peers));
+            if (d != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&sm.u2.srt.cnt[d], (uint32_t)__popc(peers));
         }
     }
     __syncthreads();
@@ -346,7 +352,7 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
         __syncthreads();
         {
             // two cells per 32-bit word, as above
-            uint32_t* wh = reinterpret_cast<uint32_t*>(&sm.u2.whist[0][0]);
+            uint32_t* wh = reinterpret_cast<uint32_t*>(&sm.u1.whist[0][0]);
             const int cp = threadIdx.x;
             uint32_t acc = 0u;
 #pragma unroll
@@ -355,8 +361,8 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
                 wh[w * (kCellTile / 2) + cp] = acc;
                 acc += n;
             }
-            sm.u1.srt.off[cur ^ 1][2 * cp] = sm.u1.srt.off[cur][2 * cp] + (acc & 0xffffu);
-            sm.u1.srt.off[cur ^ 1][2 * cp + 1] = sm.u1.srt.off[cur][2 * cp + 1] + (acc >> 16);
+            sm.u2.srt.off[cur ^ 1][2 * cp] = sm.u2.srt.off[cur][2 * cp] + (acc & 0xffffu);
+            sm.u2.srt.off[cur ^ 1][2 * cp + 1] = sm.u2.srt.off[cur][2 * cp + 1] + (acc >> 16);
         }
         __syncthreads();
         scatter_chunk(c0, R, cur);
@@ -427,12 +433,17 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             if (src >= 0) cp_async4(&sm.free_prev[cl], g.free_old + src);
             else sm.free_prev[cl] = 0.0f;
         }
-        for (int c = threadIdx.x; c < kCellTile; c += kCellThreads) sm.start[c] = -1;
 
         // ---- S: stable counting sort of the tile's bucket into S -------------------------
         const int np = p1 - p0;
         if (np > 0) sort_bucket(sm, g, base, p0, p1);  // block-uniform; ends with a barrier
         else __syncthreads();
+        // which of this thread's B cells hold particles (the counts are overwritten in B; A's
+        // barriers order these reads before any staging)
+        for (int r = 0; r < kCellTile / kCellThreads; ++r) {
+            const int cl = r * kCellThreads + threadIdx.x;
+            sm.occ[cl] = (np > 0 && sm.u2.srt.cnt[cl] != 0u) ? 1 : 0;
+        }
         if (threadIdx.x == 0) {  // the next tile's job (slot it ^ 1 was last read before the barrier)
             sm.jt[it ^ 1] = next;
             if (next < total) {
@@ -480,7 +491,7 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                         if (c != prev) {  // segment head
                             cur = run_empty(kRunHead);
                             const uint32_t cl = c - (uint32_t)base;
-                            if (cl < (uint32_t)kCellTile) sm.start[cl] = i;
+                            if (cl < (uint32_t)kCellTile) sm.u1.cell.start[cl] = i;
                         }
                         run_add(cur, kw[r], v[r]);
                         last_tail = c != next;
@@ -545,96 +556,111 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             float4* stage = sm.u2.stage[warp];
             const int n_rec = min(32, g.C - warp_first);
             float4* dst = reinterpret_cast<float4*>(g.cells + warp_first);
-            if (!all) {  // block-uniform: the warp's records as they are
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int rec = q * 8 + (lane >> 2), chunk = lane & 3;
-                    if (rec < n_rec) stage[stage_slot(rec, chunk)] = dst[rec * 4 + chunk];
-                }
-                __syncwarp();
-            }
+            // the lane's new record, every field (a stage call keeps only its parts' fields)
+            float4 n0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), n1 = n0, n2 = n0, n3 = n0;
             if (k < g.C) {
-            const bool occupied = sm.start[cl] >= 0;  // end, count and sums are set only then
-            const int start = occupied ? sm.start[cl] : -1, end = occupied ? sm.end[cl] : -1;
-            const int n_in = occupied ? sm.n_in[cl] : 0;
-            const float free_prev = sm.free_prev[cl];
-            const dogm_measurement_cell m = sm.meas[cl];
-            const CellOut o = cell_masses(n_in, c_pred, free_prev, g.alpha, g.p_B, m.free_mass, m.occ_mass);
-            float muA = 0.0f, muUA = 0.0f, wp = 0.0f;
-            float mx = 0.0f, my = 0.0f, vx = 0.0f, vy = 0.0f, cxy = 0.0f;
-            if (occupied) {
-                const float wu = __fmul_rn(m.likelihood, o.w_norm);
-                const float swu = __fmul_rn((float)n_in, wu);
-                muA = swu > 0.0f ? __fdiv_rn(o.rho_p, swu) : 0.0f;
-                muUA = o.m_occ_pred > 0.0f ? __fdiv_rn(o.rho_p, o.m_occ_pred) : 0.0f;
-                wp = __fadd_rn(__fmul_rn(__fmul_rn(m.p_A, muA), wu),
-                               __fmul_rn(__fmul_rn(__fsub_rn(1.0f, m.p_A), muUA), o.w_norm));
-                if (o.rho_p > 0.0f && (mask & kPartMoments)) {
-                    const float inv = __fdiv_rn(1.0f, o.rho_p);
-                    mx = __fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vx[cl]));
-                    my = __fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vy[cl]));
-                    vx = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vxx[cl])), __fmul_rn(mx, mx));
-                    vy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vyy[cl])), __fmul_rn(my, my));
-                    cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.sum.vxy[cl])), __fmul_rn(mx, my));
+                const bool occupied = sm.occ[cl] != 0;  // range, count and sums are set only then
+                const int start = occupied ? sm.u1.cell.start[cl] : -1, end = occupied ? sm.u1.cell.end[cl] : -1;
+                const int n_in = occupied ? sm.u1.cell.n_in[cl] : 0;
+                const float free_prev = sm.free_prev[cl];
+                const dogm_measurement_cell m = sm.meas[cl];
+                const CellOut o = cell_masses(n_in, c_pred, free_prev, g.alpha, g.p_B, m.free_mass, m.occ_mass);
+                float muA = 0.0f, muUA = 0.0f, wp = 0.0f;
+                float mx = 0.0f, my = 0.0f, vx = 0.0f, vy = 0.0f, cxy = 0.0f;
+                if (occupied) {
+                    const float wu = __fmul_rn(m.likelihood, o.w_norm);
+                    const float swu = __fmul_rn((float)n_in, wu);
+                    muA = swu > 0.0f ? __fdiv_rn(o.rho_p, swu) : 0.0f;
+                    muUA = o.m_occ_pred > 0.0f ? __fdiv_rn(o.rho_p, o.m_occ_pred) : 0.0f;
+                    wp = __fadd_rn(__fmul_rn(__fmul_rn(m.p_A, muA), wu),
+                                   __fmul_rn(__fmul_rn(__fsub_rn(1.0f, m.p_A), muUA), o.w_norm));
+                    if (o.rho_p > 0.0f && (mask & kPartMoments)) {
+                        const float inv = __fdiv_rn(1.0f, o.rho_p);
+                        mx = __fmul_rn(inv, __fmul_rn(wp, sm.u1.cell.vx[cl]));
+                        my = __fmul_rn(inv, __fmul_rn(wp, sm.u1.cell.vy[cl]));
+                        vx = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.cell.vxx[cl])), __fmul_rn(mx, mx));
+                        vy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.cell.vyy[cl])), __fmul_rn(my, my));
+                        cxy = __fsub_rn(__fmul_rn(inv, __fmul_rn(wp, sm.u1.cell.vxy[cl])), __fmul_rn(mx, my));
+                    }
                 }
-            }
-            if (all) {
-                stage[stage_slot(lane, 0)] = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
-                stage[stage_slot(lane, 1)] = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
-                stage[stage_slot(lane, 2)] = make_float4(muUA, 0.0f, 0.0f, mx);
-                stage[stage_slot(lane, 3)] = make_float4(my, vx, vy, cxy);
-            } else {
-                float4 s0 = stage[stage_slot(lane, 0)], s1 = stage[stage_slot(lane, 1)];
-                float4 s2 = stage[stage_slot(lane, 2)], s3 = stage[stage_slot(lane, 3)];
-                if (mask & kPartRanges) {
-                    s0.x = __int_as_float(start);
-                    s0.y = __int_as_float(end);
-                }
+                n0 = make_float4(__int_as_float(start), __int_as_float(end), o.rho_b, o.rho_p);
+                n1 = make_float4(o.free_up, o.occ_up, o.m_occ_pred, muA);
+                n2 = make_float4(muUA, 0.0f, 0.0f, mx);  // w_A / w_UA: the newborn pass sets them
+                n3 = make_float4(my, vx, vy, cxy);
                 if (mask & kPartMasses) {
-                    s0.z = o.rho_b; s0.w = o.rho_p;
-                    s1.x = o.free_up; s1.y = o.occ_up; s1.z = o.m_occ_pred;
-                    s2.y = 0.0f; s2.z = 0.0f;  // w_A / w_UA: the newborn stage sets them
+                    // read by nothing later in the frame: stored with the evict-first hint, so they
+                    // do not push the sorted particles and cell weights (read by resampling) out of L2
+                    if (g.copy_meas)
+                        __stcs(reinterpret_cast<float4*>(g.meas_own + k), make_float4(m.free_mass, m.occ_mass, m.likelihood, m.p_A));
+                    __stcs(g.free_new + k, o.free_up);
+                    g.rho_b[k] = make_float2(o.rho_b, m.p_A);
+                    qb += quantize(o.rho_b, g.q_shift);
                 }
                 if (mask & kPartReweight) {
-                    s1.w = muA;
-                    s2.x = muUA;
-                }
-                if (mask & kPartMoments) {
-                    s2.w = mx;
-                    s3 = make_float4(my, vx, vy, cxy);
-                }
-                stage[stage_slot(lane, 0)] = s0;
-                stage[stage_slot(lane, 1)] = s1;
-                stage[stage_slot(lane, 2)] = s2;
-                stage[stage_slot(lane, 3)] = s3;
-            }
-            if (mask & kPartMasses) {
-                // read by nothing later in the frame: stored with the evict-first hint, so they
-                // do not push the sorted particles and cell weights (read by resampling) out of L2
-                if (g.copy_meas)
-                    __stcs(reinterpret_cast<float4*>(g.meas_own + k), make_float4(m.free_mass, m.occ_mass, m.likelihood, m.p_A));
-                __stcs(g.free_new + k, o.free_up);
-                g.rho_b[k] = make_float2(o.rho_b, m.p_A);
-                qb += quantize(o.rho_b, g.q_shift);
-            }
-            if (mask & kPartReweight) {
-                if (n_in > 0) g.w_cell[k] = wp;  // read only through the keys of in-grid particles
-                const unsigned long long qw = n_in > 0 ? quantize(wp, g.q_shift) : 0ull;
-                if (qw) {
-                    jq += (unsigned long long)n_in * qw;
-                    add_persistent(g, start, end, n_in, qw);
+                    if (n_in > 0) g.w_cell[k] = wp;  // read only through the keys of in-grid particles
+                    const unsigned long long qw = n_in > 0 ? quantize(wp, g.q_shift) : 0ull;
+                    if (qw) {
+                        jq += (unsigned long long)n_in * qw;
+                        add_persistent(g, start, end, n_in, qw);
+                    }
                 }
             }
-            }  // k < g.C
-            // the warp's records, 512 contiguous bytes per store instruction (evict-first: only
-            // the newborn pass and the readback touch them again)
-            __syncwarp();
+            // the warp's records, kStageRecs at a time: 512 contiguous bytes per store instruction
+            // (evict-first: only the newborn pass and the readback touch them again)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int rec = q * 8 + (lane >> 2), chunk = lane & 3;
-                if (rec < n_rec) __stcs(dst + rec * 4 + chunk, stage[stage_slot(rec, chunk)]);
+            for (int h = 0; h < 32 / kStageRecs; ++h) {
+                const int rec0 = h * kStageRecs;
+                if (rec0 >= n_rec) break;  // warp-uniform
+                const int nr = min(kStageRecs, n_rec - rec0);
+                if (!all) {  // block-uniform: the records as they are
+#pragma unroll
+                    for (int q = 0; q < kStageRecs / 8; ++q) {
+                        const int rec = q * 8 + (lane >> 2), chunk = lane & 3;
+                        if (rec < nr) stage[stage_slot(rec, chunk)] = dst[(rec0 + rec) * 4 + chunk];
+                    }
+                    __syncwarp();
+                }
+                const int rl = lane - rec0;  // this lane's record in the half
+                if (rl >= 0 && rl < nr) {
+                    if (all) {
+                        stage[stage_slot(rl, 0)] = n0;
+                        stage[stage_slot(rl, 1)] = n1;
+                        stage[stage_slot(rl, 2)] = n2;
+                        stage[stage_slot(rl, 3)] = n3;
+                    } else {
+                        float4 s0 = stage[stage_slot(rl, 0)], s1 = stage[stage_slot(rl, 1)];
+                        float4 s2 = stage[stage_slot(rl, 2)], s3 = stage[stage_slot(rl, 3)];
+                        if (mask & kPartRanges) {
+                            s0.x = n0.x;
+                            s0.y = n0.y;
+                        }
+                        if (mask & kPartMasses) {
+                            s0.z = n0.z; s0.w = n0.w;
+                            s1.x = n1.x; s1.y = n1.y; s1.z = n1.z;
+                            s2.y = n2.y; s2.z = n2.z;
+                        }
+                        if (mask & kPartReweight) {
+                            s1.w = n1.w;
+                            s2.x = n2.x;
+                        }
+                        if (mask & kPartMoments) {
+                            s2.w = n2.w;
+                            s3 = n3;
+                        }
+                        stage[stage_slot(rl, 0)] = s0;
+                        stage[stage_slot(rl, 1)] = s1;
+                        stage[stage_slot(rl, 2)] = s2;
+                        stage[stage_slot(rl, 3)] = s3;
+                    }
+                }
+                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < kStageRecs / 8; ++q) {
+                    const int rec = q * 8 + (lane >> 2), chunk = lane & 3;
+                    if (rec < nr) __stcs(dst + (rec0 + rec) * 4 + chunk, stage[stage_slot(rec, chunk)]);
+                }
+                __syncwarp();  // the stage is refilled by the next half
             }
-            __syncwarp();  // the stage is refilled by the next r
         }
         // the tile's exact sums: warp sums, then thread 0 adds the warps' (sm.red is next
         // written at the end of the next tile, after that tile's barriers)
