@@ -62,9 +62,13 @@ struct ResSmem {
 template <int IPT>
 __global__ void __launch_bounds__(kThreads, IPT <= 4 ? 5 : 4) k_resample(Batch* __restrict__ bt) {
     grid_dependency_begin();
-    // the frame's status bits are final here (only the sort and cell passes set them): one
-    // store to the mapped host word replaces a device-to-host copy after the frame
-    if (blockIdx.x == 0 && threadIdx.x == 0 && bt->status_host) *bt->status_host = bt->status;
+    // the frame's status bits are final here (only the sort and cell passes set them): they are
+    // ORed into the mapped host word, where they stay until the host's next synchronisation reads
+    // and clears it (no device-to-host copy after the frame; a clean frame touches nothing)
+    if (blockIdx.x == 0 && threadIdx.x == 0 && bt->status_host) {
+        const unsigned int st = bt->status;
+        if (st) *(volatile unsigned int*)bt->status_host |= st;
+    }
     constexpr int kResIpt = IPT;
     constexpr int kResTile = ResShape<IPT>::kTile;
     extern __shared__ __align__(16) unsigned char smem_raw[];

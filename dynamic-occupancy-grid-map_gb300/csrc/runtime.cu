@@ -58,7 +58,7 @@ struct Ctx {
     cudaStream_t up_stream = nullptr;
     cudaEvent_t up_done[2] = {nullptr, nullptr};
     Batch* h_batch[2] = {nullptr, nullptr};      // pinned
-    unsigned int* h_status = nullptr;            // pinned and mapped, one word per mirror
+    unsigned int* h_status = nullptr;            // pinned and mapped: one word per mirror, one for copies
     unsigned int* d_h_status = nullptr;          // its device address
     cudaEvent_t done[2] = {nullptr, nullptr};    // the frame that read mirror i has finished
     bool pending[2] = {false, false};
@@ -123,8 +123,8 @@ dogm_status ctx_init(Ctx& c, int device) {
         DOGM_CUDA(cudaEventCreateWithFlags(&c.up_done[i], cudaEventDisableTiming));
     }
     c.d_batch = c.d_batch_m[0];
-    DOGM_CUDA(cudaHostAlloc((void**)&c.h_status, 2 * sizeof(unsigned int), cudaHostAllocMapped | cudaHostAllocPortable));
-    c.h_status[0] = c.h_status[1] = 0;
+    DOGM_CUDA(cudaHostAlloc((void**)&c.h_status, 3 * sizeof(unsigned int), cudaHostAllocMapped | cudaHostAllocPortable));
+    c.h_status[0] = c.h_status[1] = c.h_status[2] = 0;
     DOGM_CUDA(cudaHostGetDevicePointer((void**)&c.d_h_status, c.h_status, 0));
     for (auto& e : c.ev) DOGM_CUDA(cudaEventCreate(&e));
     return DOGM_OK;
@@ -330,10 +330,10 @@ cudaError_t upload_batch(Ctx& c, int n) {
     return cudaMemcpyAsync(c.d_batch, c.h_batch[c.cur], batch_upload_bytes(n), cudaMemcpyHostToDevice, c.stream);
 }
 
-// Status of a frame launched without a graph (stage calls end with other kernels than the
-// resampling, which writes the word itself; the same value either way).
+// Status of a frame launched without a graph, copied into the third word (stage calls end with
+// other kernels than the resampling, which ORs the bits into its mirror's word itself).
 cudaError_t download_status(Ctx& c) {
-    return cudaMemcpyAsync(c.h_status + c.cur, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+    return cudaMemcpyAsync(c.h_status + 2, &c.d_batch->status, sizeof(unsigned int), cudaMemcpyDeviceToHost,
                            c.stream);
 }
 
@@ -431,8 +431,8 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
         auto it = c.graphs.find(key);
         if (it == c.graphs.end()) {
             cudaGraph_t graph;
-            // the six kernels; the resampling kernel stores the frame's status word into
-            // mapped host memory, so no copy follows them
+            // the six kernels; the resampling kernel ORs the frame's status bits into mapped
+            // host memory, so no copy follows them
             DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
             e = frame_kernels(c, false, false);
             cudaError_t e2 = cudaStreamEndCapture(c.stream, &graph);
@@ -463,8 +463,10 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
 dogm_status finish_frame(Ctx& c, dogm_handle* const* hs, int n) {
     DOGM_CUDA(cudaStreamSynchronize(c.stream));
     c.pending[0] = c.pending[1] = false;
-    const unsigned int st = c.h_status[0] | c.h_status[1];
-    c.h_status[0] = c.h_status[1] = 0;
+    // the resampling kernel ORs a frame's bits into its mirror's word, so the bits of every frame
+    // since the last synchronisation are here, not only the last two frames'
+    const unsigned int st = c.h_status[0] | c.h_status[1] | c.h_status[2];
+    c.h_status[0] = c.h_status[1] = c.h_status[2] = 0;
     if (st & kStatusTimeout) {
         for (int i = 0; i < n; ++i) hs[i]->need_clear = true;
         return fail(DOGM_ERR_DEVICE_TIMEOUT, "a bounded device-side wait gave up");
