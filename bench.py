@@ -36,9 +36,14 @@ sys.path.insert(0, REPO)
 PKG = "dynamic-occupancy-grid-map_gb300"
 
 METRIC = "ms/update and HBM GB/s at 2M particles/1.44M cells; batched frames/s, p50/p99"
+# the headline workload, and the reference's own published case (--workload small)
+WORKLOADS = {
+    "large": "large: 120 x 120 m at 0.1 m (1200^2 = 1.44e6 cells), 2e6 persistent + 2e5 newborn particles, ego 10 m/s",
+    "small": "small: 50 x 50 m at 0.2 m (250^2 = 62,500 cells), 3e5 persistent + 3e4 newborn particles, static ego "
+             "(the case the reference's README times)",
+}
 WORKLOAD = "large"
-WORKLOAD_DESC = ("large: 120 x 120 m at 0.1 m (1200^2 = 1.44e6 cells), 2e6 persistent + 2e5 newborn particles, "
-                 "ego 10 m/s")
+WORKLOAD_DESC = WORKLOADS[WORKLOAD]
 # Per-unit algorithmic bytes of the whole update (compulsory traffic of a single-read,
 # single-write pipeline): 152 B per particle, 29 B per newborn, 108 B per cell.
 ALG_PER_PARTICLE, ALG_PER_NEWBORN, ALG_PER_CELL = 152, 29, 108
@@ -663,7 +668,8 @@ def run_reference(args, rank: int, world: int):
         m, x, y, yaw = frames[pingpong(W + 1 + k, len(frames))]
         ref.update(m, x, y, yaw, 0.1)
     ms = (time.perf_counter() - t0) * 1e3 / K
-    sample = "%d full updates of the %s workload (1.44e6 cells, 2e6 + 2e5 particles)" % (K, WORKLOAD)
+    sample = "%d full updates of the %s workload (%d cells, %d + %d particles)" % (
+        K, WORKLOAD, int(p.size / p.resolution) ** 2, p.particle_count, p.new_born_particle_count)
     line = {"impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms/update", "n_gpus": world,
             "steps": K, "warmup": W, "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -751,10 +757,14 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="time the built-in launch shape")
     ap.add_argument("--min-seconds", type=float, default=1.0,
                     help="the timed region repeats the K steps until it lasts at least this long")
+    ap.add_argument("--workload", default="large", choices=sorted(WORKLOADS),
+                    help="the single-grid workload of value, e2e and the baselines (large: the headline)")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="seconds of Poisson arrivals per serving mode (the serving workload names 60)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    global WORKLOAD, WORKLOAD_DESC
+    WORKLOAD, WORKLOAD_DESC = args.workload, WORKLOADS[args.workload]
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     global _dist
