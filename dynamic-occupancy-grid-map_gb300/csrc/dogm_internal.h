@@ -32,6 +32,19 @@ constexpr int kMaxKeyBits = 22;      // grid_size <= 2048 -> cells < 2^22
 constexpr int kCellTileBits = 10;
 constexpr int kMaxCellTiles = (1 << kMaxKeyBits) >> kCellTileBits;  // buckets of the particle sort
 static_assert(kCellTile == (1 << kCellTileBits), "cell tiles are indexed by cell >> kCellTileBits");
+// Buckets of the particle sort: 2^bucket_bits cells.  A grid of at most kFineMaxTiles cell tiles
+// with more than kFineMinPerTile particles per tile on average sorts by finer buckets (down to
+// 2^kMinBucketBits cells, at most kFineMaxBuckets of them), so that the cell pass can split a
+// cell tile whose particles are many into jobs of whole buckets of about kJobTarget particles;
+// other grids sort by cell tile (on a sparser or larger grid the finer rows cost more than the
+// split gains).  The choice depends on the grid's parameters alone, so a grid gives the same bits
+// alone and in any batch.
+constexpr int kMinBucketBits = 6;
+constexpr int kFineMaxTiles = 128;
+constexpr int kFineMinPerTile = 2048;
+constexpr int kFineMaxBuckets = 1024;
+constexpr int kJobTarget = 4096;     // particles of a cell-pass job (one chunk of its counting sort)
+static_assert(kMinBucketBits >= 6, "a job's cell range covers whole warps of the per-cell part");
 static_assert((1 << kResBitsMin) % 32 == 0, "32 aligned sorted positions lie in one resample tile");
 constexpr int kMaxParticles = (1 << 24) - 1;  // keys, counts and slot indices stay below 2^24
 
@@ -80,8 +93,9 @@ struct GridDesc {
     // sizes
     int N, B, C, gs;
     int q_shift;            // fixed point: weight w -> round(w * 2^q_shift)
-    int ctiles;             // cell tiles = buckets of the particle sort
+    int ctiles;             // buckets of the particle sort (2^bucket_bits cells each)
     int bucket_stride;      // words per row of the per-tile bucket counts (ctiles rounded up to 4)
+    int bucket_bits;        // log2 of the cells per bucket (kCellTileBits, or finer for small grids)
     int res_bits;           // resampling tile = 2^res_bits joint particles (set per launch)
     unsigned long long gs_div;  // floor(2^42 / gs) + 1: k / gs == (k * gs_div) >> 42 for k < 2^22
     // filter parameters
@@ -111,11 +125,13 @@ struct GridDesc {
     float* w_cell;          // per cell weight of an in-grid persistent particle after reweighting
     // scratch
     uint32_t* hsort;        // sort_tiles x bucket_stride: per-tile bucket counts, then offsets
-    uint32_t* ctile_cnt;    // per cell tile: particles whose cell lies in it (counted by predict)
-    uint4* ctile_job;       // cell tiles in claim order (many particles first): {tile, first
-                            // sorted position, end, 0}
-    unsigned long long* cell_sum;  // per cell tile: quantised newborn mass (first half) and
-                                   // first-frame occupied mass (second half)
+    uint32_t* ctile_cnt;    // per bucket: particles whose cell lies in it (counted by predict)
+    uint4* ctile_job;       // jobs of the cell pass in claim order (many particles first): {cell
+                            // tile, first sorted position, end, first cell | end cell << 16 within
+                            // the tile}; unused entries at the end: {0xffffffff, 0, 0, 0}
+    unsigned long long* cell_sum;  // per bucket: quantised newborn mass of the job that starts at
+                                   // it (0 inside a job); then per cell tile (offset
+                                   // tiles[kStCell]): first-frame occupied mass
     unsigned long long* res_sum;   // per resample tile: quantised joint weight (exact atomics)
     FrameState* fs;
     unsigned int* status_out;  // the batch-level status word
@@ -197,14 +213,15 @@ cudaError_t launch_init_particles(const Batch* d_batch, const LaunchCfg& cfg);
 // stage_mode 0: the update's predict (ego shift, motion, bucket counts, per-frame sums zeroed);
 // 1: the particlePrediction stage call (motion only); 2: the particleAssignment stage call
 // (bucket counts of the resident keys and per-frame sums zeroed, no motion)
-cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg, const FrameParam* fp = nullptr);
+cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg, const FrameParam* fp = nullptr,
+                           bool fine = true);
 // bucket offsets (column scan of the per-tile bucket counts) and the stable bucket scatter;
 // max_ctiles: the largest bucket count of the batch's grids (sizes the scatter's shared memory)
 cudaError_t launch_sort_scan(const Batch* d_batch, const LaunchCfg& cfg);
-cudaError_t launch_sort_scatter(const Batch* d_batch, int max_ctiles, const LaunchCfg& cfg);
+cudaError_t launch_sort_scatter(const Batch* d_batch, int max_ctiles, const LaunchCfg& cfg, bool fine = true);
 // staged: a stage call, running the parts of GridDesc::stage_mask
-cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg, bool staged = false);
-cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg);
+cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg, bool staged = false, bool fine = true);
+cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg, bool fine = true);
 cudaError_t launch_resample(const Batch* d_batch, int res_bits, const LaunchCfg& cfg);
 cudaError_t launch_shift_stage(const GridDesc& g, int x_move, int y_move, const LaunchCfg& cfg);
 // Allocation-free shift stage: the copy of the previous cell records goes to a fixed device

@@ -371,8 +371,10 @@ __device__ __forceinline__ void sort_bucket(CellSmem& sm, const GridDesc& g, int
 }
 
 // STAGED: a stage call (GridDesc::stage_mask selects the parts); the update's instantiation runs
-// every part with no mask tests.
-template <bool STAGED>
+// every part with no mask tests.  FINE: some grid of the launch sorts by buckets finer than a
+// cell tile, so a job may be a run of buckets or an unused slot; without it every job is a whole
+// tile.
+template <bool STAGED, bool FINE>
 __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ bt) {
     grid_dependency_begin();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -386,12 +388,14 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
         const int tid = blockIdx.x * blockDim.x + threadIdx.x;
         for (int gi = 0; gi < bt->n_grids; ++gi) {
             const GridDesc& g = bt->g[gi];
-            for (int i = tid; i < g.tiles[kStCell]; i += stride) g.ctile_cnt[i] = 0u;
+            for (int i = tid; i < g.ctiles; i += stride) g.ctile_cnt[i] = 0u;
         }
     }
-    // tiles are claimed one ahead: thread 0 takes the next work index at the start of a tile
+    // jobs are claimed one ahead: thread 0 takes the next work index at the start of a job
     // and, once the in-bucket sort is done, copies its ctile_job entry to shared memory
-    // (cp.async); the body's barriers publish both, so a tile starts without a load chain
+    // (cp.async); the body's barriers publish both, so a job starts without a load chain.  A job
+    // is a cell tile, or for a finely sorted grid a run of its buckets: cells [c_lo, c_hi) of the
+    // tile and the sorted positions [p0, p1) of their particles.
     if (threadIdx.x == 0) {
         const int t0 = (int)atomicAdd(&bt->counters[kStCell], 1u);
         sm.jt[0] = t0;
@@ -408,7 +412,19 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
         if (threadIdx.x == 0) next = (int)atomicAdd(&bt->counters[kStCell], 1u);
         const GridDesc& g = bt->g[sm.jgrid[it]];
         const uint4 job = sm.job[it];
-        const int lt = (int)job.x;  // full tiles first
+        if (FINE && job.x == 0xffffffffu) {  // an unused slot after a grid's last job (block-uniform)
+            if (threadIdx.x == 0) {
+                sm.jt[it ^ 1] = next;
+                if (next < total) {
+                    const int gn = grid_of_tile(bt, kStCell, next);
+                    sm.jgrid[it ^ 1] = gn;
+                    sm.job[it ^ 1] = bt->g[gn].ctile_job[next - bt->prefix[gn][kStCell]];
+                }
+            }
+            __syncthreads();
+            continue;
+        }
+        const int lt = (int)job.x;  // full jobs first
         const int base = lt * kCellTile;
         const int p0 = (int)job.y, p1 = (int)job.z;
         // prefetch the measurement and the (shifted) previous free mass of this thread's cells
@@ -417,6 +433,7 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             const int cl = r * kCellThreads + threadIdx.x;
             const int k = base + cl;
             if (k >= g.C) break;
+            if (FINE && (cl < (int)(job.w & 0xffffu) || cl >= (int)(job.w >> 16))) continue;  // another job's cell
             if (meas16) {
                 cp_async16(&sm.meas[cl], g.meas_src + k);
             } else {
@@ -547,12 +564,15 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
         const float c_pred = g.weights_predicted ? g.fs->w_res                    // predicted weight of
                                                  : __fmul_rn(g.p_S, g.fs->w_res);  // an in-grid particle
         unsigned long long qb = 0ull, jq = 0ull;
+        // the job's cells (read again here, not held through S and A): whole warps of B
+        const int c_lo = FINE ? (int)(sm.job[it].w & 0xffffu) : 0, c_hi = FINE ? (int)(sm.job[it].w >> 16) : kCellTile;
         cp_async_wait_all();  // this thread's own prefetches (B reads only its own cells' slots)
         for (int r = 0; r < kCellTile / kCellThreads; ++r) {
             const int cl = r * kCellThreads + threadIdx.x;
             const int k = base + cl;
             const int warp_first = base + r * kCellThreads + warp * 32;  // the warp's 32 cells
             if (warp_first >= g.C) break;                                // warp-uniform
+            if (FINE && (warp_first - base < c_lo || warp_first - base >= c_hi)) continue;  // another job's
             float4* stage = sm.u2.stage[warp];
             const int n_rec = min(32, g.C - warp_first);
             float4* dst = reinterpret_cast<float4*>(g.cells + warp_first);
@@ -679,7 +699,16 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
                 tile_jq += sm.red2[w];
             }
             if (mask & kPartMasses) {
-                g.cell_sum[lt] = tile_qb;
+                // the job's sum at its first bucket, zeros at its others (the newborn pass sums
+                // the buckets before a tile)
+                if (FINE) {
+                    const int b0 = (lt << (kCellTileBits - g.bucket_bits)) + (c_lo >> g.bucket_bits);
+                    const int b1 = min(g.ctiles, (lt << (kCellTileBits - g.bucket_bits)) + (c_hi >> g.bucket_bits));
+                    g.cell_sum[b0] = tile_qb;
+                    for (int b = b0 + 1; b < b1; ++b) g.cell_sum[b] = 0ull;
+                } else {
+                    g.cell_sum[lt] = tile_qb;
+                }
                 atomicAdd(&g.fs->qb_total, tile_qb);
             }
             if (tile_jq) atomicAdd(&g.fs->joint_total, tile_jq);
@@ -719,6 +748,9 @@ __device__ __forceinline__ void add_joint_range(unsigned long long (&racc)[kRunT
     }
 }
 
+// FINE: some grid of the launch sorts by buckets finer than a cell tile (its tile sums are per
+// bucket); without it they are per tile.
+template <bool FINE>
 __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt) {
     grid_dependency_begin();
     __shared__ unsigned long long red[2 * (kThreads / 32)];
@@ -745,7 +777,8 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
             bp[j] = (k < g.C) ? __ldcs(g.rho_b + k) : make_float2(0.0f, 0.0f);  // {rho_b, p_A}
         }
         // the earlier tiles' sums load while the cells' values are in flight
-        const unsigned long long part = block_prefix_part(g.cell_sum, lt);
+        const unsigned long long part =
+            block_prefix_part(g.cell_sum, FINE ? lt << (kCellTileBits - g.bucket_bits) : lt);
         unsigned long long v = 0ull;
 #pragma unroll
         for (int j = 0; j < kCellIpt; ++j) {
@@ -850,19 +883,25 @@ __global__ void __launch_bounds__(kThreads, 6) k_newborn(Batch* __restrict__ bt)
 }
 
 cudaError_t prepare_cells() {
-    cudaError_t e = cudaFuncSetAttribute(k_cells<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CellSmem));
+    cudaError_t e = cudaFuncSetAttribute(k_cells<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CellSmem));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_cells<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CellSmem));
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_cells<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CellSmem));
+    return cudaFuncSetAttribute(k_cells<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CellSmem));
 }
 
-cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg, bool staged) {
+cudaError_t launch_cells(const Batch* d_batch, const LaunchCfg& cfg, bool staged, bool fine) {
     Batch* b = const_cast<Batch*>(d_batch);
-    if (staged) return launch_kernel(cfg, k_cells<true>, launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), b);
-    return launch_kernel(cfg, k_cells<false>, launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), b);
+    // (a stage call takes the instantiation that handles every job form)
+    if (staged) return launch_kernel(cfg, k_cells<true, true>, launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), b);
+    if (fine) return launch_kernel(cfg, k_cells<false, true>, launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), b);
+    return launch_kernel(cfg, k_cells<false, false>, launch_blocks(cfg, 2), kCellThreads, sizeof(CellSmem), b);
 }
 
-cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg) {
-    return launch_kernel(cfg, k_newborn, launch_blocks(cfg, 6), kThreads, 0, const_cast<Batch*>(d_batch));
+cudaError_t launch_newborn(const Batch* d_batch, const LaunchCfg& cfg, bool fine) {
+    Batch* b = const_cast<Batch*>(d_batch);
+    if (fine) return launch_kernel(cfg, k_newborn<true>, launch_blocks(cfg, 6), kThreads, 0, b);
+    return launch_kernel(cfg, k_newborn<false>, launch_blocks(cfg, 6), kThreads, 0, b);
 }
 
 }  // namespace dogm_gb300

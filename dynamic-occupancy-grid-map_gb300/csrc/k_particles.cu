@@ -12,8 +12,8 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     for (int gi = 0; gi < bt->n_grids; ++gi) {
         const GridDesc& g = bt->g[gi];
-        for (int i = tid; i < g.tiles[kStCell]; i += stride) g.ctile_cnt[i] = 0u;
-        for (int i = tid; i < 2 * g.tiles[kStCell]; i += stride) g.cell_sum[i] = 0ull;
+        for (int i = tid; i < g.ctiles; i += stride) g.ctile_cnt[i] = 0u;
+        for (int i = tid; i < g.ctiles + g.tiles[kStBirth]; i += stride) g.cell_sum[i] = 0ull;
         for (int i = tid; i < g.tiles[kStResample]; i += stride) g.res_sum[i] = 0ull;
         // (the per-tile bucket counts are written whole each frame)
         if (tid == 0) {
@@ -33,8 +33,8 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
 // evaluated as x' = (x + dt*vx) + n_x (the grouping of the reference's mat4 x vec4);
 // the weight is not stored per particle: every persistent particle carries the common
 // weight w_res, so the predicted weight is p_S * w_res, or 0 out of the grid (bit 30).
-// Each 4096-particle tile also counts its particles per bucket of the sort (cell tile): the
-// row of the tile is written whole, the grid's totals are added to ctile_cnt.
+// Each 4096-particle tile also counts its particles per bucket of the sort (2^bucket_bits
+// cells): the row of the tile is written whole, the grid's totals are added to ctile_cnt.
 // mode 0: full frame (shift + bucket counts); mode 1: particlePrediction stage call (no
 // counts); mode 2: particleAssignment stage call (bucket counts of the resident keys only).
 // ---------------------------------------------------------------------------------------
@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(kThreads) k_frame_begin(Batch* __restrict__ bt
 constexpr int kPredictThreads = 512;
 static_assert(kPredictTile % kPredictThreads == 0, "whole particles per thread");
 
-template <class View>
+template <bool FINE, class View>
 __device__ __forceinline__ void predict_body(const View& v, int mode, uint32_t* h2) {
     const int total = v.total(kStPredict);
     const bool counts = mode != 1;
@@ -117,7 +117,7 @@ __device__ __forceinline__ void predict_body(const View& v, int mode, uint32_t* 
                 g.P_key[i] = key | (out ? kOutBit : 0u) | (kw & kAssocBit);
             }
             if (counts) {
-                const uint32_t bucket = valid ? key >> kCellTileBits : 0xffffffffu;
+                const uint32_t bucket = valid ? key >> (FINE ? g.bucket_bits : kCellTileBits) : 0xffffffffu;
                 const uint32_t peers = __match_any_sync(0xffffffffu, bucket);
                 if (valid && lane == __ffs(peers) - 1) atomicAdd(&h2[bucket], (uint32_t)__popc(peers));
             }
@@ -175,15 +175,17 @@ __device__ void publish_frame(Batch* bt, const FrameParam& fp) {
     }
 }
 
+// FINE: some grid of the launch sorts by buckets finer than a cell tile.
+template <bool FINE>
 __global__ void __launch_bounds__(kPredictThreads, 3) k_predict(Batch* __restrict__ bt, int mode,
                                                              const __grid_constant__ FrameParam fp) {
     grid_dependency_begin();
     __shared__ uint32_t h2[kMaxCellTiles];  // particles per cell tile (bucket of the sort)
     if (fp.valid) {
         if (blockIdx.x == 0) publish_frame(bt, fp);
-        predict_body(ParamView{&fp}, mode, h2);
+        predict_body<FINE>(ParamView{&fp}, mode, h2);
     } else {
-        predict_body(BatchView{bt}, mode, h2);
+        predict_body<FINE>(BatchView{bt}, mode, h2);
     }
 }
 
@@ -349,9 +351,13 @@ cudaError_t launch_frame_begin(const Batch* d_batch, int n_grids, const LaunchCf
     return cudaGetLastError();
 }
 
-cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg, const FrameParam* fp) {
+cudaError_t launch_predict(const Batch* d_batch, int stage_mode, const LaunchCfg& cfg, const FrameParam* fp,
+                           bool fine) {
     FrameParam none{};
-    return launch_kernel(cfg, k_predict, launch_blocks(cfg, 3), kPredictThreads, 0, const_cast<Batch*>(d_batch),
+    if (fine)
+        return launch_kernel(cfg, k_predict<true>, launch_blocks(cfg, 3), kPredictThreads, 0,
+                             const_cast<Batch*>(d_batch), stage_mode, fp ? *fp : none);
+    return launch_kernel(cfg, k_predict<false>, launch_blocks(cfg, 3), kPredictThreads, 0, const_cast<Batch*>(d_batch),
                          stage_mode, fp ? *fp : none);
 }
 

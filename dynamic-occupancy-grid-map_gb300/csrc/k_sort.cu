@@ -26,14 +26,23 @@ constexpr int kScanKeep = 16;  // tiles per warp kept in registers (N up to 2M p
 constexpr int kCtilePer = kMaxCellTiles / (kScanWarps * 32);
 static_assert(kCtilePer * kScanWarps * 32 == kMaxCellTiles, "one block scans every cell-tile count");
 
-// Exclusive scan of the per-cell-tile particle counts that predict took, written as the cell
-// pass's work list: ctile_job[j] = {tile, first sorted position, end, 0} of the j-th tile to
-// claim, tiles by decreasing bit length of their particle count (the fullest, slowest tiles
-// start first; the last tiles claimed are the quickest), in any order within a class.
-// Run by one block as the last work item of the bucket scan (after predict, before the
-// scatter and the cell pass).  scratch: >= 64 words.
+// Exclusive scan of the per-bucket particle counts that predict took, written as the cell
+// pass's job list.  A job is a run of whole buckets of one cell tile: the tile itself when the
+// grid sorts by cell tile, else consecutive buckets of the tile merged while their particles stay
+// within kJobTarget (a bucket above it is a job of its own), so that a tile holding many
+// particles is shared by several blocks of the cell pass.  ctile_job[j] = {tile, first sorted
+// position, end, first cell | end cell << 16 (within the tile)} of the j-th job to claim, jobs
+// by decreasing bit length of their particle count (the fullest, slowest start first), in any
+// order within a class; entries after the last job are {0xffffffff, 0, 0, 0}.  Run by one block
+// as the last work item of the bucket scan (after predict, before the scatter and the cell
+// pass).  scratch: >= 64 words.
+__device__ __forceinline__ int job_class(uint32_t n) { return 15 - min(15, 32 - __clz((int)n)); }
+
 __device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) {
+    __shared__ uint32_t s_cnt[kFineMaxBuckets], s_pre[kFineMaxBuckets];  // buckets of a finely sorted grid
     const int n = g.ctiles;
+    const int bb = g.bucket_bits;
+    const bool fine = bb < kCellTileBits;  // then n <= kFineMaxBuckets
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int i0 = threadIdx.x * kCtilePer;
     uint32_t* cls_count = scratch;       // 16 classes
@@ -55,9 +64,41 @@ __device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) 
     __syncthreads();
     uint32_t e = x - s;
     for (int w = 0; w < warp; ++w) e += red[w];
+    const int bpt = 1 << (kCellTileBits - bb);  // buckets per cell tile
+    const int ntiles = (n + bpt - 1) / bpt;
+    // one job per tile; or, for a finely sorted grid, runs of buckets (counted, then placed)
+    auto walk = [&](int t, bool place) {
+        int b = t * bpt;
+        const int bend = min(n, b + bpt);
+        while (b < bend) {
+            const int j0 = b;
+            uint32_t sum = s_cnt[b++];
+            while (b < bend && sum + s_cnt[b] <= (uint32_t)kJobTarget) sum += s_cnt[b++];
+            if (!place) {
+                atomicAdd(&cls_count[job_class(sum)], 1u);
+            } else {
+                const uint32_t pos = atomicAdd(&cls_next[job_class(sum)], 1u);
+                const uint32_t c_lo = (uint32_t)(j0 - t * bpt) << bb, c_hi = (uint32_t)(b - t * bpt) << bb;
+                g.ctile_job[pos] = make_uint4((uint32_t)t, s_pre[j0], s_pre[j0] + sum, c_lo | (c_hi << 16));
+            }
+        }
+    };
+    if (fine) {
 #pragma unroll
-    for (int j = 0; j < kCtilePer; ++j)
-        if (i0 + j < n) atomicAdd(&cls_count[15 - min(15, 32 - __clz((int)v[j]))], 1u);
+        for (int j = 0; j < kCtilePer; ++j) {
+            if (i0 + j < n) {
+                s_cnt[i0 + j] = v[j];
+                s_pre[i0 + j] = e;
+            }
+            e += v[j];
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < ntiles; t += blockDim.x) walk(t, false);
+    } else {
+#pragma unroll
+        for (int j = 0; j < kCtilePer; ++j)
+            if (i0 + j < n) atomicAdd(&cls_count[job_class(v[j])], 1u);
+    }
     __syncthreads();
     if (warp == 0) {
         const uint32_t c = lane < 16 ? cls_count[lane] : 0u;
@@ -68,15 +109,22 @@ __device__ void ctile_scan(const GridDesc& g, uint32_t* red, uint32_t* scratch) 
             if (lane >= o) inc += y;
         }
         if (lane < 16) cls_next[lane] = inc - c;
+        if (lane == 15) scratch[48] = inc;  // jobs in all
     }
     __syncthreads();
+    if (fine) {
+        for (int t = threadIdx.x; t < ntiles; t += blockDim.x) walk(t, true);
+        for (int i = (int)scratch[48] + threadIdx.x; i < n; i += blockDim.x)
+            g.ctile_job[i] = make_uint4(0xffffffffu, 0u, 0u, 0u);
+    } else {
 #pragma unroll
-    for (int j = 0; j < kCtilePer; ++j) {
-        if (i0 + j < n) {
-            const uint32_t pos = atomicAdd(&cls_next[15 - min(15, 32 - __clz((int)v[j]))], 1u);
-            g.ctile_job[pos] = make_uint4((uint32_t)(i0 + j), e, e + v[j], 0u);
+        for (int j = 0; j < kCtilePer; ++j) {
+            if (i0 + j < n) {
+                const uint32_t pos = atomicAdd(&cls_next[job_class(v[j])], 1u);
+                g.ctile_job[pos] = make_uint4((uint32_t)(i0 + j), e, e + v[j], (uint32_t)kCellTile << 16);
+            }
+            e += v[j];
         }
-        e += v[j];
     }
     __syncthreads();
 }
@@ -193,6 +241,9 @@ __host__ __device__ __forceinline__ size_t scatter_smem(int W) {
     return (size_t)kScatterWarps * W * sizeof(uint16_t) + (size_t)W * sizeof(uint32_t);
 }
 
+// FINE: some grid of the launch sorts by buckets finer than a cell tile (bucket = cell >>
+// bucket_bits); without it the bucket is the cell tile.
+template <bool FINE>
 __global__ void __launch_bounds__(kScatterThreads, 2) k_sort_scatter(Batch* __restrict__ bt, int W) {
     grid_dependency_begin();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -228,7 +279,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_sort_scatter(Batch* __re
         // bucket lies outside the grid -- only injected state can hold one -- is not placed)
 #pragma unroll
         for (int k = 0; k < kScatterIpt; ++k) {
-            const uint32_t b = (key[k] & kCellMask) >> kCellTileBits;
+            const uint32_t b = (key[k] & kCellMask) >> (FINE ? g.bucket_bits : kCellTileBits);
             const bool valid = base + k * 32 + lane < g.N && b < (uint32_t)nb;
             const uint32_t d = valid ? b : 0xffffffffu;
             const uint32_t peers = __match_any_sync(0xffffffffu, d);
@@ -267,7 +318,7 @@ __global__ void __launch_bounds__(kScatterThreads, 2) k_sort_scatter(Batch* __re
             for (int j = 0; j < kHalf; ++j) {
                 const int k = h * kHalf + j;
                 const int pos = base + k * 32 + lane;
-                const uint32_t d = (key[k] & kCellMask) >> kCellTileBits;
+                const uint32_t d = (key[k] & kCellMask) >> (FINE ? g.bucket_bits : kCellTileBits);
                 out[j] = 0xffffffffu;
                 if (pos < g.N && d < (uint32_t)nb) out[j] = gbase[d] + my_hist[d] + rank[k];
                 st[j] = __ldcs(p_state + (pos < g.N ? pos : g.N - 1));
@@ -295,14 +346,17 @@ cudaError_t launch_sort_scan(const Batch* d_batch, const LaunchCfg& cfg) {
 }
 
 cudaError_t prepare_sort() {
-    return cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)scatter_smem(scatter_width(kMaxCellTiles)));
+    const int smem = (int)scatter_smem(scatter_width(kMaxCellTiles));
+    cudaError_t e = cudaFuncSetAttribute(k_sort_scatter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_sort_scatter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
-cudaError_t launch_sort_scatter(const Batch* d_batch, int max_ctiles, const LaunchCfg& cfg) {
+cudaError_t launch_sort_scatter(const Batch* d_batch, int max_ctiles, const LaunchCfg& cfg, bool fine) {
     const int W = scatter_width(max_ctiles);
-    return launch_kernel(cfg, k_sort_scatter, launch_blocks(cfg, 2), kScatterThreads, scatter_smem(W),
-                         const_cast<Batch*>(d_batch), W);
+    Batch* b = const_cast<Batch*>(d_batch);
+    if (fine) return launch_kernel(cfg, k_sort_scatter<true>, launch_blocks(cfg, 2), kScatterThreads, scatter_smem(W), b, W);
+    return launch_kernel(cfg, k_sort_scatter<false>, launch_blocks(cfg, 2), kScatterThreads, scatter_smem(W), b, W);
 }
 
 }  // namespace dogm_gb300

@@ -83,6 +83,9 @@ struct Ctx {
     // the previous frame's resampling programmatically).  Launch slots and the batch context
     // keep graphs, since their callers wait on the frames' events.
     bool chain = false;
+    // some grid of the current batch sorts by buckets finer than a cell tile (the cell pass then
+    // takes jobs of bucket runs)
+    bool fine = false;
     bool last_chained = false;  // the last frame queued ran chained
 
     // Captured graphs hold the launch widths: drop them when the widths change.
@@ -214,6 +217,7 @@ struct Carver {
 
 struct Sizes {
     int gs, N, B, C, key_bits, sort_tiles, cell_tiles, res_tiles, pred_tiles, scan;
+    int bucket_bits, buckets;  // buckets of the particle sort (= cell tiles unless the grid is small)
 };
 
 dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
@@ -231,8 +235,13 @@ dogm_status derive_sizes(const dogm_params& p, Sizes& s) {
     s.pred_tiles = div_up(s.N, kPredictTile);
     s.sort_tiles = div_up(s.N, kSortTile);
     s.cell_tiles = div_up(s.C, kCellTile);
+    s.bucket_bits = kCellTileBits;
+    if (s.cell_tiles <= kFineMaxTiles && (long long)s.N > (long long)kFineMinPerTile * s.cell_tiles)
+        while (s.bucket_bits > kMinBucketBits && div_up(s.C, 1 << (s.bucket_bits - 1)) <= kFineMaxBuckets)
+            --s.bucket_bits;
+    s.buckets = div_up(s.C, 1 << s.bucket_bits);
     s.res_tiles = div_up((long long)s.N + s.B, 1 << kResBitsMin);  // the finest resampling tiling
-    s.scan = div_up(s.cell_tiles, 32) + 1;  // bucket groups of the column scan + the cell-tile start scan
+    s.scan = div_up(s.buckets, 32) + 1;  // bucket groups of the column scan + the job list
     return DOGM_OK;
 }
 
@@ -241,7 +250,7 @@ void set_tiles(GridDesc& g, const Sizes& s) {
     g.tiles[kStPredict] = s.pred_tiles;
     g.tiles[kStScan] = s.scan;
     g.tiles[kStSort] = s.sort_tiles;
-    g.tiles[kStCell] = s.cell_tiles;
+    g.tiles[kStCell] = s.buckets;  // job slots of the cell pass (at most one job per bucket)
     g.tiles[kStBirth] = s.cell_tiles;
     g.tiles[kStResample] = div_up((long long)s.N + s.B, 1 << kResBitsDefault);
     g.res_bits = kResBitsDefault;
@@ -304,8 +313,11 @@ void build_batch(Ctx& c, dogm_handle* const* hs, int n, const std::vector<int>& 
     b.status = 0u;
     b.status_host = c.d_h_status + c.cur;
     c.scatter_ctiles = 2048;
-    for (int i = 0; i < n; ++i)
+    c.fine = false;
+    for (int i = 0; i < n; ++i) {
         if (hs[i]->desc.ctiles > c.scatter_ctiles) c.scatter_ctiles = kMaxCellTiles;
+        if (hs[i]->desc.bucket_bits < kCellTileBits) c.fine = true;
+    }
     for (int s = 0; s < kNumStages; ++s) b.counters[s] = 0u;
     for (int s = 0; s < kNumStages; ++s) b.prefix[0][s] = 0;
     for (int i = 0; i < n; ++i) {
@@ -356,11 +368,11 @@ cudaError_t frame_kernels(Ctx& c, bool with_init, bool with_begin, const FramePa
     // full reset runs only on a grid's first frame or after a failed frame
     if ((with_begin || with_init) && (e = launch_frame_begin(c.d_batch, 0, cfg)) != cudaSuccess) return e;
     if (with_init && (e = launch_init_particles(c.d_batch, cfg)) != cudaSuccess) return e;
-    STAGE(0, launch_predict(c.d_batch, 0, cfg, fp));
+    STAGE(0, launch_predict(c.d_batch, 0, cfg, fp, c.fine));
     STAGE(1, launch_sort_scan(c.d_batch, cfg));
-    STAGE(2, launch_sort_scatter(c.d_batch, c.scatter_ctiles, cfg));
-    STAGE(3, launch_cells(c.d_batch, cfg));
-    STAGE(4, launch_newborn(c.d_batch, cfg));
+    STAGE(2, launch_sort_scatter(c.d_batch, c.scatter_ctiles, cfg, c.fine));
+    STAGE(3, launch_cells(c.d_batch, cfg, false, c.fine));
+    STAGE(4, launch_newborn(c.d_batch, cfg, c.fine));
     STAGE(5, launch_resample(c.d_batch, c.res_bits, cfg));
 #undef STAGE
     if (prof && (e = cudaEventRecord(c.ev[kStages], c.stream)) != cudaSuccess) return e;
@@ -377,9 +389,10 @@ int graph_bucket(int n) {
     return std::min(b, kMaxBatch);
 }
 
-// A graph is keyed by its batch-size bucket, mirror, bucket-scatter class and resampling tile.
-int graph_key(int nb, int mirror, int scatter_ctiles, int res_bits) {
-    return (res_bits << 21) + (scatter_ctiles > 2048 ? 1 << 20 : 0) + nb * 2 + mirror;
+// A graph is keyed by its batch-size bucket, mirror, bucket-scatter class, resampling tile and
+// the cell pass's job form (whole tiles, or runs of finer buckets).
+int graph_key(int nb, int mirror, int scatter_ctiles, int res_bits, bool fine) {
+    return (res_bits << 21) + (scatter_ctiles > 2048 ? 1 << 20 : 0) + (fine ? 1 << 19 : 0) + nb * 2 + mirror;
 }
 
 // A device-to-host copy queued after a frame's kernels and before its completion event.
@@ -427,7 +440,7 @@ dogm_status run_frame(Ctx& c, int n, bool any_init, bool any_clear, int* launche
                                   c.up_stream));
         DOGM_CUDA(cudaEventRecord(c.up_done[c.cur], c.up_stream));
         DOGM_CUDA(cudaStreamWaitEvent(c.stream, c.up_done[c.cur], 0));
-        const int key = graph_key(nb, c.cur, c.scatter_ctiles, c.res_bits);
+        const int key = graph_key(nb, c.cur, c.scatter_ctiles, c.res_bits, c.fine);
         auto it = c.graphs.find(key);
         if (it == c.graphs.end()) {
             cudaGraph_t graph;
@@ -555,8 +568,8 @@ size_t dogm_state_bytes(const dogm_params* p) {
     b += B * (16 + 4 + 4);                            // newborns
     // per cell: record 64, measurement copy 16, free mass 2 x 4, {newborn mass, p_A} 8, cell weight 4
     b += C * (sizeof(dogm_grid_cell) + sizeof(dogm_measurement_cell) + 2 * 4 + 8 + 4);
-    b += (size_t)s.sort_tiles * (size_t)((s.cell_tiles + 3) & ~3) * 4;  // per-tile bucket counts
-    b += (size_t)s.cell_tiles * (16 + 12) + 4 + (size_t)s.res_tiles * 8;
+    b += (size_t)s.sort_tiles * (size_t)((s.buckets + 3) & ~3) * 4;  // per-tile bucket counts
+    b += (size_t)s.buckets * (4 + 16 + 8) + (size_t)s.cell_tiles * 8 + (size_t)s.res_tiles * 8;
     b += 2 * sizeof(Batch);  // the launch context's device batch of each mirror
     return b;
 }
@@ -581,8 +594,9 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
 
     GridDesc& g = h->desc;
     g.N = s.N; g.B = s.B; g.C = s.C; g.gs = s.gs;
-    g.ctiles = s.cell_tiles;
-    g.bucket_stride = (s.cell_tiles + 3) & ~3;
+    g.ctiles = s.buckets;
+    g.bucket_stride = (s.buckets + 3) & ~3;
+    g.bucket_bits = s.bucket_bits;
     g.q_shift = 61 - bitlen((unsigned long long)s.C);
     g.gs_div = (1ull << 42) / (unsigned long long)s.gs + 1ull;
     g.p_S = params->persistence_prob;
@@ -608,8 +622,8 @@ dogm_status dogm_create(const dogm_params* params, const dogm_options* opt, dogm
         cv.take(&fa, s.C); cv.take(&fb, s.C);
         cv.take(&g.rho_b, s.C); cv.take(&g.w_cell, s.C);
         cv.take(&g.hsort, (size_t)s.sort_tiles * g.bucket_stride);
-        cv.take(&g.ctile_cnt, s.cell_tiles); cv.take(&g.ctile_job, s.cell_tiles);
-        cv.take(&g.cell_sum, 2 * (size_t)s.cell_tiles);
+        cv.take(&g.ctile_cnt, s.buckets); cv.take(&g.ctile_job, s.buckets);
+        cv.take(&g.cell_sum, (size_t)s.buckets + s.cell_tiles);
         cv.take(&g.res_sum, s.res_tiles);
         cv.take(&g.fs, 1);
     };
@@ -1682,12 +1696,13 @@ dogm_status slot_prewarm(BatchSlot* s, int max_n) {
     Ctx& c = s->ctx;
     DeviceGuard dg(c.device);
     const int cur = c.cur;
-    for (int m = 0; m < 2; ++m) {
+    for (int m = 0; m < 4; ++m) {  // two mirrors, each with both job forms of the cell pass
         for (int nb = 1; nb <= graph_bucket(std::max(1, max_n)); nb <<= 1) {
             c.scatter_ctiles = 2048;  // streams of the serving loop have at most 2048 cell tiles
-            const int key = graph_key(nb, m, c.scatter_ctiles, c.res_bits);
+            c.fine = (m & 2) != 0;
+            const int key = graph_key(nb, m & 1, c.scatter_ctiles, c.res_bits, c.fine);
             if (c.graphs.count(key)) continue;
-            set_mirror(c, m);
+            set_mirror(c, m & 1);
             cudaGraph_t graph;
             DOGM_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
             cudaError_t e = frame_kernels(c, false, false);
