@@ -8,7 +8,10 @@ bit for bit, moments within 4e-6 of the cell's second moment (tests/test_gpu_par
   * particles uniformly random over the grid: every scatter tile holds nearly every bucket;
   * particles in reverse cell order;
   * a grid whose cell count is not a multiple of the 1024-cell tile, with particles on the last,
-    partial tile and outside the grid."""
+    partial tile and outside the grid;
+  * small dense grids, which sort by buckets finer than a cell tile and split a crowded tile into
+    several jobs of the cell pass: every particle in one cell (one bucket far above a job), and
+    particles uniformly random (buckets merged into whole-tile jobs)."""
 import numpy as np
 import pytest
 
@@ -92,3 +95,26 @@ def test_partial_last_tile_and_outside_particles(dogm, oracle, scene):
     state[:, 1] = rng.uniform(gs - 12.0, gs + 2.0, n).astype(np.float32)   # most on the last rows
     state[:, 2:] = rng.normal(0.0, 2.0, (n, 2)).astype(np.float32)
     _run(dogm, oracle, scene, p, state, (rng.random(n) < 0.3).astype(np.uint8))
+
+
+def test_fine_buckets_all_particles_in_one_cell(dogm, oracle, scene):
+    # 100 x 100 cells = 10 cell tiles and 60,000 particles (> 2048 per tile): buckets of 64 cells
+    p = _params(dogm, 10.0, 0.1, 60000, 6000)
+    n = p.particle_count
+    rng = np.random.default_rng(5)
+    state = np.zeros((n, 4), np.float32)
+    state[:, 0] = 40.5
+    state[:, 1] = 61.5
+    state[:, 2:] = rng.normal(0.0, 0.01, (n, 2)).astype(np.float32)
+    _run(dogm, oracle, scene, p, state, (rng.random(n) < 0.5).astype(np.uint8))
+
+
+def test_fine_buckets_particles_uniform(dogm, oracle, scene):
+    # 128 x 128 cells = 16 cell tiles, 100,000 particles: every tile is split into several jobs
+    p = _params(dogm, 12.8, 0.1, 100000, 10000)
+    n, gs = p.particle_count, 128
+    rng = np.random.default_rng(6)
+    state = np.zeros((n, 4), np.float32)
+    state[:, 0:2] = rng.uniform(0.0, gs, (n, 2)).astype(np.float32)
+    state[:, 2:] = rng.normal(0.0, 3.0, (n, 2)).astype(np.float32)
+    _run(dogm, oracle, scene, p, state, np.zeros(n, np.uint8))
