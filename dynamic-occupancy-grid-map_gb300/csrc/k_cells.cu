@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(kCellThreads, 2) k_cells(Batch* __restrict__ b
             else sm.free_prev[cl] = 0.0f;
         }
 
-        // ---- S: stable counting sort of the tile's bucket into S -------------------------
+        // ---- S: stable counting sort of the job's particles into S -----------------------
         const int np = p1 - p0;
         if (np > 0) sort_bucket(sm, g, base, p0, p1);  // block-uniform; ends with a barrier
         else __syncthreads();

@@ -1,8 +1,9 @@
 // Stable particle-to-cell sort, first half: a stable bucket scatter of the predicted particles
-// by cell tile (the 1024-cell tiles of the cell pass).  The second half, a stable counting sort
-// of each bucket by cell, runs inside the cell pass (k_cells.cu), which then holds the bucket in
-// shared memory anyway.  Together they give exactly the permutation of a stable sort by cell
-// index and replace thrust::sort_by_key with its zip payload (dogm/src/dogm.cu:262-281).
+// by cell tile (the 1024-cell tiles of the cell pass; by runs of 64-512 cells for a small dense
+// grid, GridDesc::bucket_bits).  The second half, a stable counting sort of each job's buckets
+// by cell, runs inside the cell pass (k_cells.cu), which then holds them in shared memory
+// anyway.  Together they give exactly the permutation of a stable sort by cell index and
+// replace thrust::sort_by_key with its zip payload (dogm/src/dogm.cu:262-281).
 //   predict      per 4096-particle tile, the particles per bucket (row written whole) and the
 //                particles per bucket over the whole grid (ctile_cnt)
 //   k_sort_scan  column scan of the [tile][bucket] counts -> the output offset of every
