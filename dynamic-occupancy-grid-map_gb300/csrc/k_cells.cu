@@ -1,6 +1,6 @@
 // Cell-side kernels.
 //  k_cells    : one pass over all cells and the particles in them; fuses the second half of
-//               the particle sort (a stable counting sort of the tile's bucket by cell), the
+//               the particle sort (a stable counting sort of the job's buckets by cell), the
 //               particle-to-cell segmented reduction, the mass update, reweighting, moments,
 //               ego shift of the free mass and the measurement copy.
 //  k_newborn  : newborn allocation over an exact scan of the newborn masses
