@@ -184,8 +184,11 @@ def peak_gbs() -> tuple[float, str]:
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
             peaks = json.load(f)
-        return float(peaks["hbm_gbs"]), "measured"
-    except (OSError, KeyError, ValueError):
+        v = peaks["hbm_gbs"]
+        if isinstance(v, dict):  # a record with its figure under a key of its own
+            v = next(v[k] for k in ("value", "gbs", "median", "mean") if k in v)
+        return float(v), "measured"
+    except (OSError, KeyError, ValueError, TypeError, StopIteration):
         return 6800.0, "fallback"
 
 
