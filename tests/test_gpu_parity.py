@@ -120,6 +120,29 @@ def test_deterministic_and_batch_equals_alone(dogm, scene):
         g.close()
 
 
+def test_batch_of_fine_and_tile_sorted_grids_equals_alone(dogm, scene):
+    """A batch holding grids sorted by finer buckets (small and dense) and grids sorted by cell
+    tile runs the kernel instances that read both; each grid still gives its bits alone."""
+    sizes = [(10.0, 0.1, 60000, 6000),    # 100^2 cells, 6 per cell: finer buckets
+             (25.6, 0.1, 50000, 5000),    # 256^2 cells, sparse: cell-tile buckets
+             (12.8, 0.1, 100000, 10000)]  # 128^2 cells, dense: finer buckets
+    params = [dogm.make_params(size=s, resolution=r, particle_count=n, new_born_particle_count=b)
+              for s, r, n, b in sizes]
+    alone = [dogm.DOGM(p, seed=9, stream_id=i) for i, p in enumerate(params)]
+    batch = [dogm.DOGM(p, seed=9, stream_id=i) for i, p in enumerate(params)]
+    for k in range(3):
+        meas = [scene.random_measurements(g.grid_size, seed=90 + 10 * k + i, occ_fraction=0.1)
+                for i, g in enumerate(alone)]
+        for i, g in enumerate(alone):
+            g.update_grid(meas[i], 0.0, 0.0, 0.0, 0.1)
+        dogm.update_batch(batch, meas, [0.0] * 3, [0.0] * 3, [0.0] * 3, [0.1] * 3)
+        for ga, gb in zip(alone, batch):
+            assert ga.get_grid_cells().tobytes() == gb.get_grid_cells().tobytes()
+            assert ga.get_particles()["state"].tobytes() == gb.get_particles()["state"].tobytes()
+    for g in alone + batch:
+        g.close()
+
+
 def test_lower_bound_matches_searchsorted(dogm):
     """The reference's multinomial search (resampling.cu:34-47): clamp, then lower_bound."""
     rng = np.random.default_rng(3)
